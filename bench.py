@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Benchmark of the PolyDG elastodynamics time loop (DOF-steps/s).
+
+Workload (default, one GPU): the 40^3 x 6 = 384,000-tetrahedron unit cube
+agglomerated by seeded BFS into ~48,000 polyhedra of 4..12 tetrahedra,
+degree p = 3 (60 DOFs per polyhedron), rho = 1, lambda = 2, mu = 1, SIPG
+(alpha = 10, theta = -1), manufactured solution, dt = 2e-5.  A "step" is one
+leapfrog step (TIME_STEP_MATRIX_FREE) over the whole mesh.
+
+  value    DOF-steps/s of K graph-launched steps, inputs resident in HBM,
+           CUDA events on the library stream.  Inputs (the operator blocks,
+           15 GB) are far larger than L2, so no flush is needed.
+  e2e      the same metric through the reference-facing C ABI with host
+           buffers: every step uploads u^{n-1}, u^n from page-locked host
+           memory, calls lymph_step and reads u^{n+1} back.
+  roofline the step kernel: algorithmic bytes per launch / average launch
+           duration (per-launch CUDA events), against the measured HBM copy
+           bandwidth; the FP64-ALU view is reported beside it.
+  cpu_baseline  the CPU oracle (restatement of the reference algorithm:
+           assembled element blocks + Cholesky solves) on all host cores,
+           on a bounded sample of the same workload (smaller cube, same
+           degree, grouping and material), per DOF-step.
+
+`--impl reference` times that CPU implementation alone (the reference arm).
+`--gpus N` runs N independent replicas (the path has no data-path exchange
+on one GPU per problem; see the design notes), value = sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CONFIGS = {
+    # reference-runnable case: 5^3 hex x 6 tets, one polyhedron per hexahedron, p = 2
+    "c0": dict(n=5, agglomeration="hex", group=(6, 6), seed=0, p=2, material=(1.0, 1.0, 1.0), lognormal=False,
+               dt=1e-4, sample_n=5),
+    # the headline configuration: 48k polyhedra, p = 3
+    "c1": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 2.0, 1.0), lognormal=False,
+               dt=2e-5, sample_n=10),
+    # 48k polyhedra, p = 4, lognormal lambda/mu per polyhedron
+    "c2": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=4, material=(1.0, 1.0, 1.0), lognormal=True,
+               dt=2e-5, sample_n=8),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_mesh(cfg, n=None):
+    from lymph3d_apsc_gb300 import mesh as M
+    n = n or cfg["n"]
+    m = M.cube(n, bc="dirichlet", agglomeration=cfg["agglomeration"], seed=cfg["seed"], group=cfg["group"],
+               material=cfg["material"])
+    if cfg["lognormal"]:
+        m = M.cube(n, bc="dirichlet", agglomeration=cfg["agglomeration"], seed=cfg["seed"], group=cfg["group"],
+                   poly_materials=M.lognormal_materials(m.n_poly, seed=1))
+    return m
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def step_traffic_per_launch(cfg_name, n_blocks):
+    """DRAM bytes per step-kernel launch from the committed ncu summary
+    (profiles/), scaled from the captured case to this workload by the
+    number of operator blocks; None when no capture is committed."""
+    p = ROOT / "profiles" / "step_kernel_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    e = d.get(cfg_name)
+    if not e:
+        return None
+    return float(e["dram_bytes_per_launch"]) * n_blocks / float(e["n_blocks"])
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the oracle (reference algorithm) on the host cores
+# ---------------------------------------------------------------------------
+def cpu_sample(cfg, steps=None, warmup=1, target_s=12.0, threads=None):
+    from oracle.oracle_py import Oracle, load as oracle_load
+    lib = oracle_load()
+    if threads:
+        lib.oracle_set_threads(threads)
+    cores = lib.oracle_num_threads()
+    m = make_mesh(cfg, cfg["sample_n"])
+    o = Oracle(m, cfg["p"], cfg["dt"])
+    o.make_matrices()
+    o.make_rhs(0, 0, 0, 0)
+    o.make_rhs(1, 1, 1, 1)
+    o.modal_project(0, 0)
+    o.modal_project(1, 2)
+    o.first_step(0.0)
+    t = cfg["dt"]
+    for _ in range(warmup):
+        o.step(t)
+        t += cfg["dt"]
+    if steps is None:
+        t0 = time.perf_counter()
+        o.step(t)
+        t += cfg["dt"]
+        one = time.perf_counter() - t0
+        steps = max(3, min(2000, int(target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    t, n = o.run_steps(t, 1e30, steps)
+    el = time.perf_counter() - t0
+    dofs = 3 * o.Np * m.n_poly
+    o.close()
+    return {"value": dofs * n / el, "unit": "DOF-steps/s", "cores": cores, "steps": n, "seconds": el,
+            "sample": f"{cfg['sample_n']}^3 x 6 = {m.n_tet} tets, {m.n_poly} polyhedra, p={cfg['p']}, "
+                      f"{n} leapfrog steps, assembled blocks + Cholesky solves, FP64, {cores} threads"}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def prepare(cfg, precision):
+    from lymph3d_apsc_gb300 import MatrixFree, _lib
+    t0 = time.perf_counter()
+    m = make_mesh(cfg)
+    t1 = time.perf_counter()
+    g = MatrixFree(m, cfg["p"], cfg["dt"], precision=precision)
+    g.MAKE_MATRICES_FREE()
+    g.MAKE_RHS_FREE(_lib.RHS_STAT, _lib.F_NULL, _lib.GD_NULL, _lib.GN_NULL)
+    g.MAKE_RHS_FREE(_lib.RHS_DYN, _lib.F_TIME, _lib.GD, _lib.GN)
+    g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_DISPLACEMENT, _lib.SLOT_U0)
+    g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_VELOCITY, _lib.SLOT_V0)
+    g.FIRST_TIME_STEP_MATRIX_FREE(0.0)
+    t2 = time.perf_counter()
+    log(f"[bench] mesh {m.n_tet} tets / {m.n_poly} polyhedra in {t1 - t0:.1f}s; device set-up {t2 - t1:.1f}s; "
+        f"{g.n_blocks} blocks, {g.device_bytes() / 1e9:.2f} GB on device")
+    return m, g
+
+
+def step_bytes(g, precision):
+    es = 4 if precision == 1 else 8
+    nd, Np = g.nd, g.Np
+    return g.n_blocks * nd * nd * es + g.n_poly * (3 * nd * 8 + 2 * Np * Np * 8 + 2 * nd * 8)
+
+
+def step_flops(g):
+    nd, Np = g.nd, g.Np
+    return 2.0 * g.n_blocks * nd * nd + g.n_poly * (3 * 2 * Np * Np + 6 * nd)
+
+
+def errors(g, t):
+    from lymph3d_apsc_gb300 import _lib, time_function
+    g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_UEX, _lib.SLOT_UEX, time_function(t))
+    return math.sqrt(g.COMPUTE_ERROR_L2_MATRIX_FREE()), math.sqrt(g.COMPUTE_ERROR_DG_MATRIX_FREE())
+
+
+def run_gpu(cfg, precision, steps, warmup, rank_info, want_e2e=True):
+    from lymph3d_apsc_gb300 import _lib
+    m, g = prepare(cfg, precision)
+    dofs = 3 * g.Np * g.n_poly
+    t = cfg["dt"]
+    t, nw, _, _ = g.run_steps(t, 1e30, warmup)
+    rank_info["barrier"]()
+    l0 = g.launch_count()
+    with ClockSampler(rank_info["gpu"]) as clk:
+        t, n, ms, _ = g.run_steps(t, 1e30, steps)
+    launches = g.launch_count() - l0
+    ms = rank_info["max"](ms)
+    # per-launch events for the roofline (same work, second timed region)
+    t, n2, ms2, mk = g.run_steps(t, 1e30, steps, kernel_timing=True)
+    out = {"dofs": dofs, "steps": n, "ms": ms, "kernel_ms_avg": mk / n2, "launches": launches,
+           "clocks": clk.summary(), "n_blocks": g.n_blocks, "n_poly": g.n_poly, "n_tet": m.n_tet, "Np": g.Np,
+           "bytes": step_bytes(g, precision), "flops": step_flops(g), "t": t}
+    if want_e2e:
+        out["e2e"] = run_e2e(g, t, steps)
+        t = out["e2e"]["t"]
+    out["err_L2"], out["err_DG"] = errors(g, t)
+    g.close()
+    return out
+
+
+def pinned_array(n):
+    """Page-locked host buffer (torch is used only as a host allocator here)."""
+    import numpy as np
+    try:
+        import torch
+        return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy(), True
+    except Exception:
+        return np.empty(n, np.float64), False
+
+
+def run_e2e(g, t, steps):
+    """K steps through the reference-facing C ABI with host buffers."""
+    from lymph3d_apsc_gb300 import _lib
+    nv = g.n_poly * g.nd
+    u0, p0 = pinned_array(nv)
+    un, _ = pinned_array(nv)
+    u0[:] = g.get_state(_lib.SLOT_U0).ravel()
+    un[:] = g.get_state(_lib.SLOT_UN).ravel()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.set_state(_lib.SLOT_U0, u0)
+        g.set_state(_lib.SLOT_UN, un)
+        g.TIME_STEP_MATRIX_FREE(t)
+        t += g.dt
+        u0, un = un, u0
+        g.lib.lymph_get_state(g.ctx, _lib.SLOT_UN, un.ctypes.data_as(_lib.P_F64), _lib.LAYOUT_POLY_MAJOR)
+    el = time.perf_counter() - t0
+    return {"value": g.n_poly * g.nd * steps / el, "seconds": el, "pinned": p0, "t": t,
+            "h2d_bytes_per_step": 2 * nv * 8, "d2h_bytes_per_step": nv * 8}
+
+
+def rank_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    info = {"world": world, "rank": rank, "gpu": local, "barrier": lambda: None, "max": lambda x: x,
+            "sum": lambda x: x}
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        import torch
+
+        def _red(x, op):
+            tt = torch.tensor([float(x)], dtype=torch.float64)
+            dist.all_reduce(tt, op=op)
+            return float(tt.item())
+        info["barrier"] = dist.barrier
+        info["max"] = lambda x: _red(x, dist.ReduceOp.MAX)
+        info["sum"] = lambda x: _red(x, dist.ReduceOp.SUM)
+        info["dist"] = dist
+    return info
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison run")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    cfg = CONFIGS[args.config]
+    info = rank_setup(args)
+    metric = "DOF-steps/s (PolyDG elastodynamics leapfrog, 3*Np*N_poly*steps / loop time)"
+    workload = (f"{cfg['n']}^3x6 tets, BFS polyhedra {cfg['group'][0]}-{cfg['group'][1]} tets (seed {cfg['seed']}), "
+                f"p={cfg['p']}, SIPG alpha=10, dt={cfg['dt']}")
+
+    if args.impl == "reference":
+        if info["rank"] != 0:
+            return
+        threads = os.cpu_count()
+        cb = cpu_sample(cfg, steps=args.steps, warmup=args.warmup, threads=threads)
+        line = {"impl": "reference", "metric": metric, "value": cb["value"], "unit": "DOF-steps/s",
+                "n_gpus": args.gpus, "steps": cb["steps"], "warmup": args.warmup,
+                "ms_per_step": 1e3 * cb["seconds"] / cb["steps"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated cube mesh, manufactured solution)",
+                "config": {"workload": workload, "sample": cb["sample"], "l2_flush": "not needed (CPU)"},
+                "cpu_baseline": {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",
+                                 "sample": cb["sample"]},
+                "e2e": {"value": cb["value"], "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    precision = 1 if args.precision == "mixed" else 0
+    r = run_gpu(cfg, precision, args.steps, args.warmup, info)
+    total_dof_steps = info["sum"](r["dofs"] * r["steps"])
+    value = total_dof_steps / (r["ms"] / 1e3)
+    peak, peak_kind = measured_peaks()
+    achieved = r["bytes"] / (r["kernel_ms_avg"] / 1e3) / 1e9
+    traffic = step_traffic_per_launch(args.config + ("_mixed" if precision else ""), r["n_blocks"])
+    line = {
+        "metric": metric, "value": value, "unit": "DOF-steps/s", "n_gpus": info["world"], "steps": r["steps"],
+        "warmup": args.warmup, "ms_per_step": r["ms"] / r["steps"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f32-blocks/f64",
+        "data": "synthetic (generated cube mesh, manufactured solution; no public dataset)",
+        "config": {"workload": workload, "n_tet": r["n_tet"], "n_poly": r["n_poly"], "dofs": r["dofs"],
+                   "n_blocks": r["n_blocks"], "precision": args.precision,
+                   "l2_flush": "inputs larger than L2 (operator blocks %.1f GB per step)" % (r["bytes"] / 1e9),
+                   "parallelism": "replicas" if info["world"] > 1 else "single GPU"},
+        "err_L2": r["err_L2"], "err_DG": r["err_DG"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "bytes_per_launch": r["bytes"], "kernel_ms": r["kernel_ms_avg"],
+                     "fp64_tflops": r["flops"] / (r["kernel_ms_avg"] / 1e3) / 1e12},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+    }
+    if "e2e" in r:
+        e = r["e2e"]
+        line["e2e"] = {"value": info["sum"](e["value"]), "unit": "DOF-steps/s",
+                       "h2d_bytes_per_step": e["h2d_bytes_per_step"], "d2h_bytes_per_step": e["d2h_bytes_per_step"],
+                       "pinned_host": e["pinned"]}
+    if info["rank"] == 0 and not args.no_cpu_baseline:
+        cb = cpu_sample(cfg)
+        line["cpu_baseline"] = {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",
+                                "sample": cb["sample"]}
+    if info["rank"] == 0 and precision == 0 and not args.no_mixed:
+        rm = run_gpu(cfg, 1, args.steps, args.warmup, {**info, "barrier": lambda: None, "max": lambda x: x},
+                     want_e2e=False)
+        vm = rm["dofs"] * rm["steps"] / (rm["ms"] / 1e3)
+        line["mixed"] = {"value": vm, "speedup_vs_fp64": vm / value * info["world"], "err_L2": rm["err_L2"],
+                         "err_DG": rm["err_DG"], "err_L2_ratio_vs_fp64": rm["err_L2"] / r["err_L2"],
+                         "kernel_ms": rm["kernel_ms_avg"],
+                         "achieved_gbs": rm["bytes"] / (rm["kernel_ms_avg"] / 1e3) / 1e9}
+    if info["rank"] == 0:
+        print(json.dumps(line), flush=True)
+    if info.get("dist"):
+        info["dist"].destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

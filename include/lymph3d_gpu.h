@@ -1,0 +1,239 @@
+/*
+ * lymph3d_gpu.h -- C ABI of the GB300 PolyDG elastodynamics hot path.
+ *
+ * This is the drop-in boundary for the matrix-free solver module of LYMPH3D
+ * (src/matrix_free.f90).  Every entry point below replaces one subroutine the
+ * Fortran driver src/Lymph3D.f90 calls; the citation next to each declaration
+ * names the reference interface it stands for.  All arguments are plain C
+ * types and host pointers; no device pointer, torch type or C++ type crosses
+ * this boundary.  Device memory, streams and kernels live behind the opaque
+ * context handle.
+ *
+ * Conventions
+ *  - Every function returns an int status: LYMPH_OK (0) or a code from the
+ *    reference's Poly_exit_codes module (src/Poly_global.f90:130-173), or one
+ *    of the LYMPH_ERR_* codes this library adds.  A failed call leaves a
+ *    one-line explanation in lymph_last_error().  Nothing calls exit/stop.
+ *  - Indices are 0-based (the Fortran side subtracts 1 once when flattening).
+ *  - Degrees of freedom of a polyhedron are ordered component-major:
+ *    dof = i*Np + m  (component i in 0..2, basis function m in 0..Np-1), the
+ *    reference's row = (i-1)*Np + m (src/matrix_free.f90:240-256).
+ *  - One context per host thread; calls are stream-ordered on the context's
+ *    own stream and synchronous at return.
+ *  - A polyhedron is a set of tetrahedra (tet_poly).  When every polyhedron
+ *    holds one tetrahedron the operator is exactly the reference's per-tet
+ *    operator; with agglomeration, volume integrals are summed over the
+ *    sub-tetrahedra and only faces between different polyhedra (or on the
+ *    boundary) carry face terms, the rule src/matrix_free.f90:290-309 applies.
+ */
+#ifndef LYMPH3D_GPU_H
+#define LYMPH3D_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LYMPH_OK                       0
+#define LYMPH_EXIT_INSTAB              2   /* NaN/Inf in the state (Poly_exit_codes EXIT_INSTAB) */
+#define LYMPH_EXIT_SETUP               4   /* inconsistent mesh / parameters (EXIT_SETUP) */
+#define LYMPH_EXIT_SINGULARMTX         5   /* mass matrix not SPD (EXIT_SINGULARMTX; cholesky stop) */
+#define LYMPH_EXIT_ELEM_ORIENT        11   /* tetrahedron with det J <= 0 (EXIT_ELEM_ORIENT) */
+#define LYMPH_EXIT_NEIGHBOUR_EL_ERROR 18   /* face neighbour table inconsistent (EXIT_NEIGHBOUR_EL_ERROR) */
+#define LYMPH_ERR_INVALID            100   /* bad argument */
+#define LYMPH_ERR_CUDA               101   /* CUDA runtime error */
+#define LYMPH_ERR_OOM                102   /* device allocation failed */
+#define LYMPH_ERR_ORDER              103   /* call made before its prerequisite */
+#define LYMPH_ERR_TIMEOUT            104   /* a bounded device-side wait expired */
+#define LYMPH_ERR_INDEX              105   /* device-side index check failed */
+
+/* ---- boundary markers in lymph_mesh_desc.neigh (BC_DIRI / BC_NEUM,
+ *      src/Poly_global.f90:420-421) ------------------------------------- */
+#define LYMPH_BC_DIRI (-1)
+#define LYMPH_BC_NEUM (-2)
+
+/* ---- precision of the operator apply ----------------------------------- */
+#define LYMPH_FP64   0   /* every operation in FP64 (the plain path) */
+#define LYMPH_MIXED  1   /* operator blocks and their mat-vec in FP32, FP32
+                            accumulation; geometry, assembly, mass inverse,
+                            time update and error norms in FP64 */
+
+/* ---- state slots (the driver's arrays, src/Lymph3D.f90:237-239) --------- */
+#define LYMPH_SLOT_U0   0   /* u0_loc: u^{n-1} (u^0 before the first step)   */
+#define LYMPH_SLOT_UN   1   /* un_loc: u^n                                   */
+#define LYMPH_SLOT_V0   2   /* v0_loc: initial velocity coefficients         */
+#define LYMPH_SLOT_UEX  3   /* modal coefficients of the exact solution      */
+#define LYMPH_NUM_SLOTS 4
+
+/* ---- host array layouts for get/set ------------------------------------ */
+#define LYMPH_LAYOUT_POLY_MAJOR 0  /* C array [n_poly][3*Np]                */
+#define LYMPH_LAYOUT_FORTRAN    1  /* reference u(ie, k): column-major with the
+                                      polyhedron index fastest, i.e. the C
+                                      array [3*Np][n_poly]                    */
+
+/* ---- RHS selector and data-function ids (procedure arguments of
+ *      MAKE_RHS_FREE / COMPUTE_MODAL_COEFFICIENTS_FREE become ids) -------- */
+#define LYMPH_RHS_STAT 0         /* rhs_stat_loc                              */
+#define LYMPH_RHS_DYN  1         /* rhs_dyn_loc (scaled by time_function(t))   */
+
+#define LYMPH_F_NULL   0         /* f_null          problem_data_and_properties.f90:72-82 */
+#define LYMPH_F_TIME   1         /* f_time                                 :48-70  */
+#define LYMPH_F_STAT   2         /* f (static manufactured forcing)        :26-45  */
+
+#define LYMPH_GD_NULL  0         /* gd_null   :84-92   */
+#define LYMPH_GD       1         /* gd        :130-154 */
+#define LYMPH_GD_STAT  2         /* gd_stat   :106-114 */
+
+#define LYMPH_GN_NULL  0         /* gn_null   :94-104  */
+#define LYMPH_GN       1         /* gn        :186-242 */
+#define LYMPH_GN_STAT  2         /* gn_stat   :116-128 */
+
+#define LYMPH_FUN_IC_DISPLACEMENT 0  /* ic_displacement :281-290 (zero) */
+#define LYMPH_FUN_IC_VELOCITY     1  /* ic_velocity     :292-301        */
+#define LYMPH_FUN_UEX             2  /* uex             :245-254        */
+#define LYMPH_FUN_UEX_STAT        3  /* uex_stat        :257-264 (zero) */
+
+/* ---- operator block selector for lymph_get_blocks ----------------------- */
+#define LYMPH_BLOCKS_K    0   /* stiffness blocks K_loc (K_loc(ie,1:5,:,:))   */
+#define LYMPH_BLOCKS_ADG  1   /* DG-norm blocks A_dg_loc                      */
+
+typedef struct lymph_ctx lymph_ctx;
+
+/* Flattened mesh: the parts of Mesh_Structure / Element / Polyhedron
+ * (src/Poly_mesh.f90:13-104) the hot path reads.  Geometry (Jacobians,
+ * normals, areas, bounding boxes, diameters) is derived on the device from
+ * these arrays, as src/Poly_ref_mappings.f90:18-75 and
+ * src/MAKE_PARTITION_AND_MPI_FILES.f90:1429-1580 derive it. */
+typedef struct lymph_mesh_desc {
+    int32_t n_node;
+    int32_t n_tet;
+    int32_t n_poly;
+    int32_t n_mat;
+    const double*  coords;    /* [n_node][3]                                  */
+    const int32_t* tet_vert;  /* [n_tet][4] node ids (Elem_loc%vert)          */
+    const int32_t* tet_poly;  /* [n_tet] polyhedron id (elem_in_poly)          */
+    const int32_t* tet_mat;   /* [n_tet] material id (Elem_loc%mat_prop)       */
+    const int32_t* neigh;     /* [n_tet][4] tet across face f, or LYMPH_BC_DIRI /
+                                 LYMPH_BC_NEUM (neigh_el(f,2)); face f joins
+                                 vertices {1,2,3},{1,2,4},{2,3,4},{3,1,4}
+                                 (1-based, MAKE_PARTITION_AND_MPI_FILES.f90:1087-1096) */
+    const int32_t* fun_tag;   /* [n_tet][4] boundary space-function tag
+                                 (neigh_el(f,5)); may be NULL (all 1)          */
+    const double*  mat;       /* [n_mat][3] rho, lambda, mu (prop_mat(:,1:3))  */
+} lymph_mesh_desc;
+
+typedef struct lymph_params {
+    int32_t degree;     /* polynomial degree p, 1..6 (Elem_loc%Degree)        */
+    int32_t precision;  /* LYMPH_FP64 or LYMPH_MIXED                          */
+    double  alpha;      /* penalty constant (set_properties: 10)              */
+    double  theta;      /* -1 SIPG, 0 IIPG, 1 NIPG (set_properties: -1)       */
+    double  dt;         /* time step (Poly.input TIMESTEP)                    */
+} lymph_params;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int lymph_version(void);
+
+/* Last error message of the calling thread ("" if none). */
+const char* lymph_last_error(void);
+
+/* Copies the mesh to the device, derives geometry and the block pattern.
+ * Replaces the flattening of Mesh_Structure the driver does before
+ * src/Lymph3D.f90:262 (no counterpart subroutine: the reference passes the
+ * derived type).  Keeps no host pointer. */
+int lymph_create(const lymph_mesh_desc* mesh, const lymph_params* prm, lymph_ctx** out);
+
+/* Frees every device resource of the context. */
+int lymph_destroy(lymph_ctx* ctx);
+
+/* Problem sizes: Np, number of polyhedra, number of operator blocks (self +
+ * neighbour blocks), number of face-sides carrying face terms. */
+int lymph_sizes(const lymph_ctx* ctx, int32_t* Np, int32_t* n_poly, int64_t* n_blocks, int64_t* n_face_sides);
+
+/* MAKE_MATRICES_FREE (src/matrix_free.f90:27-464) followed by the Cholesky
+ * factorisation of the mass matrices (src/Lymph3D.f90:264-271): assembles
+ * K_loc, M_loc, M_modal_loc and their factors on the device. */
+int lymph_make_matrices(lymph_ctx* ctx);
+
+/* MAKE_RHS_FREE (src/matrix_free.f90:467-843): which = LYMPH_RHS_STAT or
+ * LYMPH_RHS_DYN; the three procedure arguments become ids. */
+int lymph_make_rhs(lymph_ctx* ctx, int which, int forcing_id, int dirichlet_id, int neumann_id);
+
+/* COMPUTE_MODAL_COEFFICIENTS_FREE (src/matrix_free.f90:847-997): L2
+ * projection of the data function fun_id into state slot `slot`, then the
+ * slot is multiplied by `scale` (the driver's time_function(t) scaling,
+ * src/Lymph3D.f90:459-466; pass 1.0 for none). */
+int lymph_modal_project(lymph_ctx* ctx, int fun_id, int slot, double scale);
+
+/* FIRST_TIME_STEP_MATRIX_FREE (src/matrix_free.f90:1100-1227):
+ * UN <- U0 + dt V0 + dt^2/2 M^-1 (F_stat + F_dyn g(t) - K U0). */
+int lymph_first_step(lymph_ctx* ctx, double t);
+
+/* TIME_STEP_MATRIX_FREE (src/matrix_free.f90:1230-1385) plus the driver's
+ * array rotation (src/Lymph3D.f90:393-397): computes
+ * u^{n+1} = dt^2 M^-1 (F_stat + F_dyn g(t) - K u^n) + 2 u^n - u^{n-1},
+ * then U0 <- u^n, UN <- u^{n+1}.  The neighbour coefficients the reference
+ * receives through MPI_EXCHANGE_DOF (src/exchange_data.f90:153-258) are
+ * gathered on the device. */
+int lymph_step(lymph_ctx* ctx, double t);
+
+/* The time loop of src/Lymph3D.f90:389-418: while (*t_inout <= stop_time)
+ * { step(*t_inout); *t_inout += dt; }, at most max_steps steps
+ * (max_steps < 0: no cap).  The time function values are computed on the
+ * host with the reference's floating-point accumulation of t.  The loop is
+ * launched as a CUDA graph.  n_done receives the number of steps taken;
+ * ms_total (nullable) the device time of the loop measured with CUDA events
+ * on the context stream; ms_kernel (nullable, forces per-launch events
+ * instead of a graph) the summed durations of the step kernels alone. */
+int lymph_run_steps(lymph_ctx* ctx, double stop_time, int64_t max_steps, double* t_inout,
+                    int64_t* n_done, float* ms_total, float* ms_kernel);
+
+/* Copies a state slot to / from host memory in the given layout. */
+int lymph_get_state(lymph_ctx* ctx, int slot, double* host, int layout);
+int lymph_set_state(lymph_ctx* ctx, int slot, const double* host, int layout);
+
+/* COMPUTE_ERROR_L2_MATRIX_FREE (src/matrix_free.f90:1388-1418): sum over
+ * polyhedra and components of du^T M_modal du, du = slot_uh - slot_uex.
+ * Returns the sum of squares; the caller takes the square root, as the
+ * driver does after its MPI_REDUCE (src/Lymph3D.f90:496-514). */
+int lymph_error_l2(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
+
+/* COMPUTE_ERROR_DG_MATRIX_FREE (src/matrix_free.f90:1421-1504): sum over
+ * polyhedra of du_P^T (A_PP du_P + sum_Q A_PQ du_Q).  Assembles the A_dg
+ * blocks into a temporary device buffer for the duration of the call. */
+int lymph_error_dg(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
+
+/* Aliases with the names the project specification uses for the two error
+ * routines (COMPUTE_ERROR_L2_FREE / COMPUTE_ERROR_DG_FREE). */
+int lymph_compute_error_l2_free(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
+int lymph_compute_error_dg_free(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
+
+/* Debug / parity access to the assembled data (a3 of the reference path).
+ * lymph_get_pattern: row_ptr[n_poly+1], col[n_blocks] (neighbour polyhedron
+ * of each block; the self block comes first in each row).
+ * lymph_get_blocks: vals[n_blocks][3Np][3Np] row-major (row = test dof of the
+ * row polyhedron, column = trial dof of the column polyhedron), FP64 even in
+ * mixed precision (the FP32 values are widened). */
+int lymph_get_pattern(lymph_ctx* ctx, int32_t* row_ptr, int32_t* col);
+int lymph_get_blocks(lymph_ctx* ctx, int which, double* vals);
+/* Mass data per polyhedron, [n_poly][Np][Np] row-major: which = 0 M_loc (rho
+ * weighted), 1 M_modal_loc, 2 R_M_loc (upper Cholesky factor), 3 R_M_modal_loc. */
+int lymph_get_mass(lymph_ctx* ctx, int which, double* vals);
+/* RHS vectors [n_poly][3Np] (which = LYMPH_RHS_STAT / LYMPH_RHS_DYN). */
+int lymph_get_rhs(lymph_ctx* ctx, int which, double* vals);
+/* Per-polyhedron bounding box [n_poly][6] (xmin,xmax,ymin,ymax,zmin,zmax)
+ * and diameter hk [n_poly] (CREATE_BBOX_EL). */
+int lymph_get_poly_geometry(lymph_ctx* ctx, double* bbox, double* hk);
+
+/* Number of kernels this context launched so far (all kinds). */
+int lymph_launch_count(const lymph_ctx* ctx, int64_t* count);
+
+/* Device bytes the context holds (operator blocks, state, geometry). */
+int lymph_device_bytes(const lymph_ctx* ctx, int64_t* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LYMPH3D_GPU_H */

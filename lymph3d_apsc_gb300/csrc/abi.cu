@@ -1,0 +1,652 @@
+// abi.cu -- implementation of the C ABI declared in include/lymph3d_gpu.h.
+//
+// Host responsibilities: validate and copy the flattened mesh, build the
+// block pattern (which polyhedra couple through faces, which face-sides feed
+// which block), the reference quadrature tables, the time-function values of
+// a run, and the stream/graph orchestration.  Every floating-point operation
+// on the data runs in device kernels (setup.cu, step.cu); there is no host
+// compute fallback.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+// kernels (setup.cu, step.cu)
+int lymph_dev_geometry(lymph_ctx* c);
+int lymph_dev_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass);
+int lymph_dev_cholesky(lymph_ctx* c);
+int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scale, double* out);
+int lymph_dev_step(lymph_ctx* c, bool bump);
+int lymph_dev_first_step(lymph_ctx* c);
+int lymph_dev_bump(lymph_ctx* c);
+int lymph_dev_error_dg(lymph_ctx* c, const void* blocks, const double* uh, const double* uex, double* d_out);
+int lymph_dev_error_l2(lymph_ctx* c, const double* uh, const double* uex, double* d_out);
+
+namespace {
+
+thread_local std::string g_last_error;
+
+const double PI = 3.14159265358979323846;
+
+// 1D Gauss-Legendre nodes and weights in the reference's order
+// (basis_function.f90:77-124).  Standard tables; the reference's order is
+// kept because the tensor quadrature inherits it.
+void gl_table(int nqn, std::vector<double>& x, std::vector<double>& w) {
+    switch (nqn) {
+        case 1: x = {0.0}; w = {2.0}; break;
+        case 2: x = {std::sqrt(1.0 / 3.0), -std::sqrt(1.0 / 3.0)}; w = {1.0, 1.0}; break;
+        case 3: x = {0.0, std::sqrt(3.0 / 5.0), -std::sqrt(3.0 / 5.0)}; w = {8.0 / 9.0, 5.0 / 9.0, 5.0 / 9.0}; break;
+        case 4: {
+            double s = std::sqrt(30.0);
+            x = {0.3399810435848563, -0.3399810435848563, 0.8611363115940526, -0.8611363115940526};
+            w = {(18 + s) / 36.0, (18 + s) / 36.0, (18 - s) / 36.0, (18 - s) / 36.0};
+            break;
+        }
+        case 5: {
+            double s = std::sqrt(70.0);
+            x = {0.0, 0.5384693101056831, -0.5384693101056831, 0.9061798459386640, -0.9061798459386640};
+            w = {128.0 / 225.0, (322 + 13 * s) / 900.0, (322 + 13 * s) / 900.0, (322 - 13 * s) / 900.0,
+                 (322 - 13 * s) / 900.0};
+            break;
+        }
+        default: x.clear(); w.clear();
+    }
+}
+
+// Reference quadrature and maps for degree p: tensor Gauss-Legendre with
+// p+1 points per direction (quadrature, basis_function.f90:47-161) collapsed
+// onto the reference tetrahedron and triangle (mapping_quadrature_3D/2D,
+// Poly_ref_mappings.f90:137-186), face maps (tria2tetfaces_maps :79-134) and
+// the monomial degree list (basis_list, basis_function.f90:12-44).
+bool build_ref_tables(int p, RefTables& R) {
+    std::memset(&R, 0, sizeof(R));
+    int nqn = p + 1;
+    std::vector<double> x, w;
+    gl_table(nqn, x, w);
+    if ((int)x.size() != nqn) return false;
+    int c = 0;
+    for (int i = 0; i < nqn; ++i)
+        for (int j = 0; j < nqn; ++j)
+            for (int k = 0; k < nqn; ++k) {
+                double a = 0.5 * x[i] + 0.5, b = 0.5 * x[j] + 0.5, cc = 0.5 * x[k] + 0.5;
+                double wt = 0.125 * (w[i] * w[j] * w[k]);
+                R.nodtet3[c * 4 + 0] = a;
+                R.nodtet3[c * 4 + 1] = (1 - a) * b;
+                R.nodtet3[c * 4 + 2] = (1 - a) * (1 - b) * cc;
+                R.nodtet3[c * 4 + 3] = 1.0;
+                R.weitet3[c] = std::fabs((1 - b) * ((1 - a) * (1 - a))) * wt;
+                ++c;
+            }
+    c = 0;
+    for (int i = 0; i < nqn; ++i)
+        for (int j = 0; j < nqn; ++j) {
+            double s = x[i], t = x[j];
+            R.nodtria2[c * 4 + 0] = 0.5 * (1 + s);
+            R.nodtria2[c * 4 + 1] = 0.25 * (1 - s) * (1 + t);
+            R.nodtria2[c * 4 + 2] = 1.0;
+            R.nodtria2[c * 4 + 3] = 1.0;
+            R.weitria2[c] = std::fabs(0.125 * (1 - s)) * (w[i] * w[j]);
+            ++c;
+        }
+    // node_maps[f][row][col]
+    auto nm = [&](int f, int r, int cc) -> double& { return R.node_maps[f * 16 + r * 4 + cc]; };
+    nm(0, 0, 1) = 1; nm(0, 1, 0) = 1; nm(0, 3, 3) = 1;
+    nm(1, 0, 0) = 1; nm(1, 2, 1) = 1; nm(1, 3, 3) = 1;
+    nm(2, 0, 0) = 1; nm(2, 1, 1) = 1; nm(2, 2, 2) = 1; nm(2, 3, 3) = 1; nm(2, 2, 0) = -1; nm(2, 2, 1) = -1;
+    nm(3, 1, 1) = 1; nm(3, 2, 0) = 1; nm(3, 3, 3) = 1;
+    int ii = 0;
+    for (int q1 = p; q1 >= 0; --q1)
+        for (int q2 = p - q1; q2 >= 0; --q2)
+            for (int q3 = p - q1 - q2; q3 >= 0; --q3) {
+                R.blist[ii * 3 + 0] = q1; R.blist[ii * 3 + 1] = q2; R.blist[ii * 3 + 2] = q3;
+                ++ii;
+            }
+    return true;
+}
+
+template <typename T> int dalloc(lymph_ctx* c, T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        lymph_set_error(std::string("cudaMalloc(") + std::to_string(n * sizeof(T)) + " bytes): " + cudaGetErrorString(e));
+        return LYMPH_ERR_OOM;
+    }
+    c->device_bytes += (int64_t)(n * sizeof(T));
+    return LYMPH_OK;
+}
+
+template <typename T> int upload(lymph_ctx* c, T** p, const T* h, size_t n) {
+    LYMPH_TRY(dalloc(c, p, n));
+    if (n) LYMPH_CUDA_TRY(cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    return LYMPH_OK;
+}
+
+void dfree(void* p) {
+    if (p) cudaFree(p);
+}
+
+double time_function(double t) { return std::sin(std::sqrt(2.0) * PI * t); }  // problem_data_and_properties.f90:14-23
+
+int set_g(lymph_ctx* c, double g) {
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(c->d_gvals, &g, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    LYMPH_CUDA_TRY(cudaMemsetAsync(c->d_step_idx, 0, sizeof(int64_t), c->stream));
+    return LYMPH_OK;
+}
+
+bool valid_slot(int s) { return s >= 0 && s < LYMPH_NUM_SLOTS; }
+
+}  // namespace
+
+void lymph_set_error(const std::string& msg) { g_last_error = msg; }
+
+double* lymph_slot_ptr(lymph_ctx* c, int slot) {
+    switch (slot) {
+        case LYMPH_SLOT_U0: return c->d_buf[c->cur ^ 1];
+        case LYMPH_SLOT_UN: return c->d_buf[c->cur];
+        case LYMPH_SLOT_V0: return c->d_v0;
+        case LYMPH_SLOT_UEX: return c->d_uex;
+        default: return nullptr;
+    }
+}
+
+int lymph_sync_status(lymph_ctx* c, const char* where) {
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    int st = 0;
+    LYMPH_CUDA_TRY(cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st == 0) return LYMPH_OK;
+    LYMPH_CUDA_TRY(cudaMemset(c->d_status, 0, sizeof(int)));
+    std::string w(where);
+    if (st & ST_BAD_INDEX) { lymph_set_error(w + ": device index check failed"); return LYMPH_ERR_INDEX; }
+    if (st & ST_NOT_SPD) { lymph_set_error(w + ": Matrix is not positive definite!"); return LYMPH_EXIT_SINGULARMTX; }
+    if (st & ST_DEGENERATE) { lymph_set_error(w + ": degenerate tetrahedron or face"); return LYMPH_EXIT_SETUP; }
+    if (st & ST_NONFINITE) { lymph_set_error(w + ": non-finite value in the state"); return LYMPH_EXIT_INSTAB; }
+    lymph_set_error(w + ": device status " + std::to_string(st));
+    return LYMPH_ERR_CUDA;
+}
+
+extern "C" {
+
+int lymph_version(void) { return 10000; }
+
+const char* lymph_last_error(void) { return g_last_error.c_str(); }
+
+int lymph_destroy(lymph_ctx* c) {
+    if (!c) return LYMPH_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    void* ptrs[] = {c->d_coords, c->d_tet_vert, c->d_tet_poly, c->d_tet_mat, c->d_neigh, c->d_fun_tag, c->d_mat,
+                    c->d_ref, c->d_fk, c->d_jdet, c->d_normal, c->d_area, c->d_bbox, c->d_hk, c->d_poly_ptr,
+                    c->d_poly_tets, c->d_row_ptr, c->d_col, c->d_blk_row, c->d_bf_ptr, c->d_bf, c->d_K, c->d_M,
+                    c->d_Mm, c->d_R, c->d_Rm, c->d_RT, c->d_RmT, c->d_rhs_stat, c->d_rhs_dyn, c->d_buf[0], c->d_buf[1],
+                    c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status};
+    for (void* p : ptrs) dfree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return LYMPH_OK;
+}
+
+int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** out) {
+    if (!out) { lymph_set_error("lymph_create: null output"); return LYMPH_ERR_INVALID; }
+    *out = nullptr;
+    if (!m || !prm || !m->coords || !m->tet_vert || !m->tet_poly || !m->tet_mat || !m->neigh || !m->mat) {
+        lymph_set_error("lymph_create: null mesh array");
+        return LYMPH_ERR_INVALID;
+    }
+    if (prm->degree < 1 || prm->degree > MAX_DEGREE) {
+        lymph_set_error("lymph_create: degree must be 1..4 on the device");
+        return LYMPH_ERR_INVALID;
+    }
+    if (prm->precision != LYMPH_FP64 && prm->precision != LYMPH_MIXED) {
+        lymph_set_error("lymph_create: unknown precision");
+        return LYMPH_ERR_INVALID;
+    }
+    if (m->n_tet <= 0 || m->n_poly <= 0 || m->n_node <= 0 || m->n_mat <= 0) {
+        lymph_set_error("lymph_create: empty mesh");
+        return LYMPH_EXIT_SETUP;
+    }
+    if (!(prm->dt > 0.0) || !std::isfinite(prm->dt)) {
+        lymph_set_error("lymph_create: dt must be positive");
+        return LYMPH_ERR_INVALID;
+    }
+    const int nt = m->n_tet, np = m->n_poly;
+    // ---- validation ----
+    for (int64_t i = 0; i < (int64_t)nt * 4; ++i)
+        if (m->tet_vert[i] < 0 || m->tet_vert[i] >= m->n_node) { lymph_set_error("lymph_create: vertex id out of range"); return LYMPH_EXIT_SETUP; }
+    std::vector<int32_t> cnt(np, 0);
+    for (int t = 0; t < nt; ++t) {
+        if (m->tet_poly[t] < 0 || m->tet_poly[t] >= np) { lymph_set_error("lymph_create: polyhedron id out of range"); return LYMPH_EXIT_SETUP; }
+        if (m->tet_mat[t] < 0 || m->tet_mat[t] >= m->n_mat) { lymph_set_error("lymph_create: material id out of range"); return LYMPH_EXIT_SETUP; }
+        cnt[m->tet_poly[t]]++;
+    }
+    for (int P = 0; P < np; ++P)
+        if (cnt[P] == 0) { lymph_set_error("lymph_create: empty polyhedron " + std::to_string(P)); return LYMPH_EXIT_SETUP; }
+    for (int t = 0; t < nt; ++t)
+        for (int f = 0; f < 4; ++f) {
+            int e = m->neigh[t * 4 + f];
+            if (e == LYMPH_BC_DIRI || e == LYMPH_BC_NEUM) continue;
+            if (e < 0 || e >= nt || e == t) { lymph_set_error("lymph_create: bad neighbour entry"); return LYMPH_EXIT_NEIGHBOUR_EL_ERROR; }
+            bool back = false;
+            for (int g = 0; g < 4; ++g) back |= (m->neigh[e * 4 + g] == t);
+            if (!back) { lymph_set_error("lymph_create: neighbour table not symmetric"); return LYMPH_EXIT_NEIGHBOUR_EL_ERROR; }
+        }
+    lymph_ctx* c = new lymph_ctx();
+    c->p = prm->degree; c->Np = np_of(c->p); c->nd = 3 * c->Np;
+    c->nq3 = (c->p + 1) * (c->p + 1) * (c->p + 1); c->nq2 = (c->p + 1) * (c->p + 1);
+    c->precision = prm->precision; c->alpha = prm->alpha; c->theta = prm->theta; c->dt = prm->dt;
+    c->n_node = m->n_node; c->n_tet = nt; c->n_poly = np; c->n_mat = m->n_mat;
+    int rc = LYMPH_OK;
+    auto fail = [&](int code) { lymph_destroy(c); return code; };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        lymph_set_error("lymph_create: no CUDA device / stream");
+        delete c;
+        return LYMPH_ERR_CUDA;
+    }
+    // ---- polyhedron -> tets CSR, block pattern, per-block face lists ----
+    std::vector<int32_t> pptr(np + 1, 0), ptets(nt);
+    for (int t = 0; t < nt; ++t) pptr[m->tet_poly[t] + 1]++;
+    for (int P = 0; P < np; ++P) pptr[P + 1] += pptr[P];
+    {
+        std::vector<int32_t> fill(pptr.begin(), pptr.end() - 1);
+        for (int t = 0; t < nt; ++t) ptets[fill[m->tet_poly[t]]++] = t;
+    }
+    std::vector<int32_t> row_ptr(np + 1, 0), col, blk_row, bf;
+    std::vector<int64_t> bf_ptr(1, 0);
+    int64_t n_sides = 0;
+    for (int P = 0; P < np; ++P) {
+        std::vector<int32_t> self_faces;
+        std::map<int32_t, std::vector<int32_t>> nb;
+        for (int k = pptr[P]; k < pptr[P + 1]; ++k) {
+            int t = ptets[k];
+            for (int f = 0; f < 4; ++f) {
+                int e = m->neigh[t * 4 + f];
+                if (e == LYMPH_BC_NEUM) continue;
+                if (e == LYMPH_BC_DIRI) { self_faces.push_back(t * 4 + f); continue; }
+                int Q = m->tet_poly[e];
+                if (Q == P) continue;  // face inside the polyhedron (face_flag)
+                self_faces.push_back(t * 4 + f);
+                nb[Q].push_back(t * 4 + f);
+            }
+        }
+        n_sides += (int64_t)self_faces.size();
+        row_ptr[P] = (int32_t)col.size();
+        col.push_back(P); blk_row.push_back(P);
+        bf.insert(bf.end(), self_faces.begin(), self_faces.end());
+        bf_ptr.push_back((int64_t)bf.size());
+        for (auto& kv : nb) {
+            col.push_back(kv.first); blk_row.push_back(P);
+            bf.insert(bf.end(), kv.second.begin(), kv.second.end());
+            bf_ptr.push_back((int64_t)bf.size());
+        }
+    }
+    row_ptr[np] = (int32_t)col.size();
+    c->n_blocks = (int64_t)col.size();
+    c->n_face_sides = n_sides;
+    c->n_block_faces = (int64_t)bf.size();
+    c->h_row_ptr = row_ptr;
+    c->h_col = col;
+    RefTables ref;
+    if (!build_ref_tables(c->p, ref)) { lymph_set_error("lymph_create: no quadrature table"); return fail(LYMPH_ERR_INVALID); }
+    std::vector<int32_t> ftag(4 * (size_t)nt, 1);
+    if (m->fun_tag) std::memcpy(ftag.data(), m->fun_tag, sizeof(int32_t) * 4 * (size_t)nt);
+    // ---- device copies ----
+    if ((rc = upload(c, &c->d_coords, m->coords, 3 * (size_t)m->n_node))) return fail(rc);
+    if ((rc = upload(c, &c->d_tet_vert, m->tet_vert, 4 * (size_t)nt))) return fail(rc);
+    if ((rc = upload(c, &c->d_tet_poly, m->tet_poly, (size_t)nt))) return fail(rc);
+    if ((rc = upload(c, &c->d_tet_mat, m->tet_mat, (size_t)nt))) return fail(rc);
+    if ((rc = upload(c, &c->d_neigh, m->neigh, 4 * (size_t)nt))) return fail(rc);
+    if ((rc = upload(c, &c->d_fun_tag, ftag.data(), 4 * (size_t)nt))) return fail(rc);
+    if ((rc = upload(c, &c->d_mat, m->mat, 3 * (size_t)m->n_mat))) return fail(rc);
+    if ((rc = upload(c, &c->d_ref, &ref, 1))) return fail(rc);
+    if ((rc = upload(c, &c->d_poly_ptr, pptr.data(), pptr.size()))) return fail(rc);
+    if ((rc = upload(c, &c->d_poly_tets, ptets.data(), ptets.size()))) return fail(rc);
+    if ((rc = upload(c, &c->d_row_ptr, row_ptr.data(), row_ptr.size()))) return fail(rc);
+    if ((rc = upload(c, &c->d_col, col.data(), col.size()))) return fail(rc);
+    if ((rc = upload(c, &c->d_blk_row, blk_row.data(), blk_row.size()))) return fail(rc);
+    if ((rc = upload(c, &c->d_bf_ptr, bf_ptr.data(), bf_ptr.size()))) return fail(rc);
+    if ((rc = upload(c, &c->d_bf, bf.data(), bf.size()))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_fk, 12 * (size_t)nt))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_jdet, (size_t)nt))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_normal, 12 * (size_t)nt))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_area, 4 * (size_t)nt))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_bbox, 6 * (size_t)np))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_hk, (size_t)np))) return fail(rc);
+    size_t nv = (size_t)np * c->nd;
+    for (int b = 0; b < 2; ++b)
+        if ((rc = dalloc(c, &c->d_buf[b], nv))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_v0, nv))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_uex, nv))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_rhs_stat, nv))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_rhs_dyn, nv))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_partial, (size_t)np))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_scalar, 4))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_status, 1))) return fail(rc);
+    if ((rc = dalloc(c, &c->d_step_idx, 1))) return fail(rc);
+    c->gvals_cap = 4096;
+    if ((rc = dalloc(c, &c->d_gvals, (size_t)c->gvals_cap))) return fail(rc);
+    for (double* p : {c->d_buf[0], c->d_buf[1], c->d_v0, c->d_uex, c->d_rhs_stat, c->d_rhs_dyn})
+        if (cudaMemsetAsync(p, 0, nv * sizeof(double), c->stream) != cudaSuccess) return fail(LYMPH_ERR_CUDA);
+    if (cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream) != cudaSuccess) return fail(LYMPH_ERR_CUDA);
+    if (cudaMemsetAsync(c->d_step_idx, 0, sizeof(int64_t), c->stream) != cudaSuccess) return fail(LYMPH_ERR_CUDA);
+    if ((rc = lymph_dev_geometry(c))) return fail(rc);
+    if ((rc = lymph_sync_status(c, "lymph_create"))) return fail(rc);
+    *out = c;
+    return LYMPH_OK;
+}
+
+int lymph_sizes(const lymph_ctx* c, int32_t* Np, int32_t* n_poly, int64_t* n_blocks, int64_t* n_face_sides) {
+    if (!c) return LYMPH_ERR_INVALID;
+    if (Np) *Np = c->Np;
+    if (n_poly) *n_poly = c->n_poly;
+    if (n_blocks) *n_blocks = c->n_blocks;
+    if (n_face_sides) *n_face_sides = c->n_face_sides;
+    return LYMPH_OK;
+}
+
+int lymph_make_matrices(lymph_ctx* c) {
+    if (!c) return LYMPH_ERR_INVALID;
+    size_t es = (c->precision == LYMPH_MIXED) ? sizeof(float) : sizeof(double);
+    size_t nK = (size_t)c->n_blocks * c->nd * c->nd;
+    if (!c->d_K) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, nK * es);
+        if (e != cudaSuccess) {
+            lymph_set_error("lymph_make_matrices: cannot allocate " + std::to_string(nK * es) + " bytes of operator blocks");
+            return LYMPH_ERR_OOM;
+        }
+        c->d_K = p;
+        c->device_bytes += (int64_t)(nK * es);
+        size_t nm = (size_t)c->n_poly * c->Np * c->Np;
+        LYMPH_TRY(dalloc(c, &c->d_M, nm));
+        LYMPH_TRY(dalloc(c, &c->d_Mm, nm));
+        LYMPH_TRY(dalloc(c, &c->d_R, nm));
+        LYMPH_TRY(dalloc(c, &c->d_RT, nm));
+        LYMPH_TRY(dalloc(c, &c->d_Rm, nm));
+        LYMPH_TRY(dalloc(c, &c->d_RmT, nm));
+    }
+    LYMPH_TRY(lymph_dev_assemble(c, LYMPH_BLOCKS_K, c->d_K, c->precision == LYMPH_MIXED, true));
+    LYMPH_TRY(lymph_dev_cholesky(c));
+    LYMPH_TRY(lymph_sync_status(c, "lymph_make_matrices"));
+    c->have_matrices = true;
+    return LYMPH_OK;
+}
+
+int lymph_make_rhs(lymph_ctx* c, int which, int fid, int did, int nid) {
+    if (!c || (which != LYMPH_RHS_STAT && which != LYMPH_RHS_DYN)) return LYMPH_ERR_INVALID;
+    if (fid < 0 || fid > 2 || did < 0 || did > 2 || nid < 0 || nid > 2) {
+        lymph_set_error("lymph_make_rhs: unknown data function id");
+        return LYMPH_ERR_INVALID;
+    }
+    if (!c->have_matrices) { lymph_set_error("lymph_make_rhs: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    double* out = (which == LYMPH_RHS_STAT) ? c->d_rhs_stat : c->d_rhs_dyn;
+    LYMPH_TRY(lymph_dev_vector(c, 0, fid, did, nid, 1.0, out));
+    LYMPH_TRY(lymph_sync_status(c, "lymph_make_rhs"));
+    if (which == LYMPH_RHS_STAT) c->have_rhs_stat = true; else c->have_rhs_dyn = true;
+    return LYMPH_OK;
+}
+
+int lymph_modal_project(lymph_ctx* c, int fun_id, int slot, double scale) {
+    if (!c || !valid_slot(slot) || fun_id < 0 || fun_id > 3) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_modal_project: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    LYMPH_TRY(lymph_dev_vector(c, 1, fun_id, 0, 0, scale, lymph_slot_ptr(c, slot)));
+    return lymph_sync_status(c, "lymph_modal_project");
+}
+
+int lymph_first_step(lymph_ctx* c, double t) {
+    if (!c) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_first_step: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    LYMPH_TRY(set_g(c, time_function(t)));
+    LYMPH_TRY(lymph_dev_first_step(c));
+    return lymph_sync_status(c, "lymph_first_step");
+}
+
+int lymph_step(lymph_ctx* c, double t) {
+    if (!c) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_step: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    LYMPH_TRY(set_g(c, time_function(t)));
+    LYMPH_TRY(lymph_dev_step(c, false));
+    c->cur ^= 1;
+    return lymph_sync_status(c, "lymph_step");
+}
+
+int lymph_run_steps(lymph_ctx* c, double stop_time, int64_t max_steps, double* t_inout, int64_t* n_done,
+                    float* ms_total, float* ms_kernel) {
+    if (!c || !t_inout) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_run_steps: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    // time values with the reference's accumulation (Lymph3D.f90:389-418)
+    std::vector<double> g;
+    double t = *t_inout;
+    while (t <= stop_time && (max_steps < 0 || (int64_t)g.size() < max_steps)) {
+        g.push_back(time_function(t));
+        t = t + c->dt;
+    }
+    const int64_t n = (int64_t)g.size();
+    if (n_done) *n_done = n;
+    if (ms_total) *ms_total = 0.0f;
+    if (ms_kernel) *ms_kernel = 0.0f;
+    if (n == 0) { *t_inout = t; return LYMPH_OK; }
+    if (n > c->gvals_cap) {
+        dfree(c->d_gvals);
+        c->device_bytes -= c->gvals_cap * (int64_t)sizeof(double);
+        c->gvals_cap = n + 1024;
+        LYMPH_TRY(dalloc(c, &c->d_gvals, (size_t)c->gvals_cap));
+        if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    }
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(c->d_gvals, g.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    LYMPH_CUDA_TRY(cudaMemsetAsync(c->d_step_idx, 0, sizeof(int64_t), c->stream));
+    cudaEvent_t e0, e1;
+    LYMPH_CUDA_TRY(cudaEventCreate(&e0));
+    LYMPH_CUDA_TRY(cudaEventCreate(&e1));
+    int rc = LYMPH_OK;
+    if (ms_kernel) {
+        // per-launch events around every step kernel (no graph)
+        std::vector<cudaEvent_t> ev(2 * n);
+        for (auto& e : ev) cudaEventCreate(&e);
+        cudaEventRecord(e0, c->stream);
+        for (int64_t i = 0; i < n && rc == LYMPH_OK; ++i) {
+            cudaEventRecord(ev[2 * i], c->stream);
+            rc = lymph_dev_step(c, false);
+            cudaEventRecord(ev[2 * i + 1], c->stream);
+            if (rc == LYMPH_OK) rc = lymph_dev_bump(c);
+            c->cur ^= 1;
+        }
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float sum = 0.0f;
+        for (int64_t i = 0; i < n; ++i) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+            sum += ms;
+        }
+        *ms_kernel = sum;
+        for (auto& e : ev) cudaEventDestroy(e);
+    } else {
+        const int R = 16;  // steps per graph (even: returns to the same buffer parity)
+        if (c->graph_exec && (c->graph_steps != R || c->graph_parity != c->cur)) {
+            cudaGraphExecDestroy(c->graph_exec);
+            c->graph_exec = nullptr;
+        }
+        int64_t i = 0;
+        cudaEventRecord(e0, c->stream);
+        if (n >= R) {
+            if (!c->graph_exec) {
+                cudaGraph_t graph;
+                int cur0 = c->cur;
+                LYMPH_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                int64_t l0 = c->launches;
+                for (int j = 0; j < R; ++j) {
+                    lymph_dev_step(c, true);
+                    c->cur ^= 1;
+                }
+                c->launches = l0;
+                cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+                c->cur = cur0;
+                if (ce != cudaSuccess) { lymph_set_error(std::string("graph capture: ") + cudaGetErrorString(ce)); return LYMPH_ERR_CUDA; }
+                ce = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ce != cudaSuccess) { lymph_set_error(std::string("graph instantiate: ") + cudaGetErrorString(ce)); return LYMPH_ERR_CUDA; }
+                c->graph_steps = R;
+                c->graph_parity = cur0;
+            }
+            // the graph holds the buffer pointers of parity cur0; R is even, so
+            // the parity is the same after every launch
+            for (; i + R <= n; i += R) {
+                LYMPH_CUDA_TRY(cudaGraphLaunch(c->graph_exec, c->stream));
+                c->launches += 2 * R;
+            }
+        }
+        for (; i < n; ++i) {
+            LYMPH_TRY(lymph_dev_step(c, true));
+            c->cur ^= 1;
+        }
+        cudaEventRecord(e1, c->stream);
+    }
+    cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms_total) *ms_total = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *t_inout = t;
+    LYMPH_TRY(rc);
+    return lymph_sync_status(c, "lymph_run_steps");
+}
+
+int lymph_get_state(lymph_ctx* c, int slot, double* host, int layout) {
+    if (!c || !host || !valid_slot(slot)) return LYMPH_ERR_INVALID;
+    size_t nv = (size_t)c->n_poly * c->nd;
+    if (layout != LYMPH_LAYOUT_FORTRAN) {
+        // direct copy: a page-locked caller buffer moves by DMA
+        LYMPH_CUDA_TRY(cudaMemcpyAsync(host, lymph_slot_ptr(c, slot), nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        return LYMPH_OK;
+    }
+    std::vector<double> tmp(nv);
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(tmp.data(), lymph_slot_ptr(c, slot), nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (int P = 0; P < c->n_poly; ++P)
+        for (int k = 0; k < c->nd; ++k) host[(size_t)k * c->n_poly + P] = tmp[(size_t)P * c->nd + k];
+    return LYMPH_OK;
+}
+
+int lymph_set_state(lymph_ctx* c, int slot, const double* host, int layout) {
+    if (!c || !host || !valid_slot(slot)) return LYMPH_ERR_INVALID;
+    size_t nv = (size_t)c->n_poly * c->nd;
+    if (layout != LYMPH_LAYOUT_FORTRAN) {
+        LYMPH_CUDA_TRY(cudaMemcpyAsync(lymph_slot_ptr(c, slot), host, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        return LYMPH_OK;
+    }
+    std::vector<double> tmp(nv);
+    for (int P = 0; P < c->n_poly; ++P)
+        for (int k = 0; k < c->nd; ++k) tmp[(size_t)P * c->nd + k] = host[(size_t)k * c->n_poly + P];
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(lymph_slot_ptr(c, slot), tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return LYMPH_OK;
+}
+
+int lymph_error_l2(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) {
+    if (!c || !sumsq || !valid_slot(s_uh) || !valid_slot(s_uex)) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_error_l2: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    LYMPH_TRY(lymph_dev_error_l2(c, lymph_slot_ptr(c, s_uh), lymph_slot_ptr(c, s_uex), c->d_scalar));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(sumsq, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return lymph_sync_status(c, "lymph_error_l2");
+}
+
+int lymph_error_dg(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) {
+    if (!c || !sumsq || !valid_slot(s_uh) || !valid_slot(s_uex)) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_error_dg: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    size_t nK = (size_t)c->n_blocks * c->nd * c->nd;
+    double* A = nullptr;
+    if (cudaMalloc(&A, nK * sizeof(double)) != cudaSuccess) {
+        lymph_set_error("lymph_error_dg: cannot allocate the A_dg blocks");
+        return LYMPH_ERR_OOM;
+    }
+    int rc = lymph_dev_assemble(c, LYMPH_BLOCKS_ADG, A, 0, false);
+    if (rc == LYMPH_OK) rc = lymph_dev_error_dg(c, A, lymph_slot_ptr(c, s_uh), lymph_slot_ptr(c, s_uex), c->d_scalar);
+    if (rc == LYMPH_OK && cudaMemcpyAsync(sumsq, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+        rc = LYMPH_ERR_CUDA;
+    cudaStreamSynchronize(c->stream);
+    cudaFree(A);
+    LYMPH_TRY(rc);
+    return lymph_sync_status(c, "lymph_error_dg");
+}
+
+int lymph_compute_error_l2_free(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) { return lymph_error_l2(c, s_uh, s_uex, sumsq); }
+int lymph_compute_error_dg_free(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) { return lymph_error_dg(c, s_uh, s_uex, sumsq); }
+
+int lymph_get_pattern(lymph_ctx* c, int32_t* row_ptr, int32_t* col) {
+    if (!c) return LYMPH_ERR_INVALID;
+    if (row_ptr) std::memcpy(row_ptr, c->h_row_ptr.data(), sizeof(int32_t) * c->h_row_ptr.size());
+    if (col) std::memcpy(col, c->h_col.data(), sizeof(int32_t) * c->h_col.size());
+    return LYMPH_OK;
+}
+
+int lymph_get_blocks(lymph_ctx* c, int which, double* vals) {
+    if (!c || !vals || (which != LYMPH_BLOCKS_K && which != LYMPH_BLOCKS_ADG)) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_get_blocks: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    const int nd = c->nd;
+    size_t nK = (size_t)c->n_blocks * nd * nd;
+    std::vector<double> tmp(nK);
+    if (which == LYMPH_BLOCKS_K && c->precision == LYMPH_MIXED) {
+        std::vector<float> tf(nK);
+        LYMPH_CUDA_TRY(cudaMemcpy(tf.data(), c->d_K, nK * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nK; ++i) tmp[i] = tf[i];
+    } else if (which == LYMPH_BLOCKS_K) {
+        LYMPH_CUDA_TRY(cudaMemcpy(tmp.data(), c->d_K, nK * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        double* A = nullptr;
+        if (cudaMalloc(&A, nK * sizeof(double)) != cudaSuccess) { lymph_set_error("lymph_get_blocks: out of memory"); return LYMPH_ERR_OOM; }
+        int rc = lymph_dev_assemble(c, LYMPH_BLOCKS_ADG, A, 0, false);
+        if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+        if (rc == LYMPH_OK && cudaMemcpy(tmp.data(), A, nK * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+        cudaFree(A);
+        LYMPH_TRY(rc);
+    }
+    // device blocks are column-major; return row-major
+    for (int64_t b = 0; b < c->n_blocks; ++b)
+        for (int r = 0; r < nd; ++r)
+            for (int cc = 0; cc < nd; ++cc) vals[((size_t)b * nd + r) * nd + cc] = tmp[((size_t)b * nd + cc) * nd + r];
+    return lymph_sync_status(c, "lymph_get_blocks");
+}
+
+int lymph_get_mass(lymph_ctx* c, int which, double* vals) {
+    if (!c || !vals || which < 0 || which > 3) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_get_mass: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    const double* src[4] = {c->d_M, c->d_Mm, c->d_R, c->d_Rm};
+    LYMPH_CUDA_TRY(cudaMemcpy(vals, src[which], sizeof(double) * (size_t)c->n_poly * c->Np * c->Np, cudaMemcpyDeviceToHost));
+    return LYMPH_OK;
+}
+
+int lymph_get_rhs(lymph_ctx* c, int which, double* vals) {
+    if (!c || !vals || (which != LYMPH_RHS_STAT && which != LYMPH_RHS_DYN)) return LYMPH_ERR_INVALID;
+    LYMPH_CUDA_TRY(cudaMemcpy(vals, which == LYMPH_RHS_STAT ? c->d_rhs_stat : c->d_rhs_dyn,
+                              sizeof(double) * (size_t)c->n_poly * c->nd, cudaMemcpyDeviceToHost));
+    return LYMPH_OK;
+}
+
+int lymph_get_poly_geometry(lymph_ctx* c, double* bbox, double* hk) {
+    if (!c) return LYMPH_ERR_INVALID;
+    if (bbox) LYMPH_CUDA_TRY(cudaMemcpy(bbox, c->d_bbox, sizeof(double) * 6 * (size_t)c->n_poly, cudaMemcpyDeviceToHost));
+    if (hk) LYMPH_CUDA_TRY(cudaMemcpy(hk, c->d_hk, sizeof(double) * (size_t)c->n_poly, cudaMemcpyDeviceToHost));
+    return LYMPH_OK;
+}
+
+int lymph_launch_count(const lymph_ctx* c, int64_t* count) {
+    if (!c || !count) return LYMPH_ERR_INVALID;
+    *count = c->launches;
+    return LYMPH_OK;
+}
+
+int lymph_device_bytes(const lymph_ctx* c, int64_t* bytes) {
+    if (!c || !bytes) return LYMPH_ERR_INVALID;
+    *bytes = c->device_bytes;
+    return LYMPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,171 @@
+// common.cuh -- context, error plumbing and shared device helpers of the
+// GB300 PolyDG library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/lymph3d_gpu.h"
+
+// ---------------------------------------------------------------------------
+// error plumbing
+// ---------------------------------------------------------------------------
+void lymph_set_error(const std::string& msg);
+
+#define LYMPH_CUDA_TRY(expr)                                                             \
+    do {                                                                                 \
+        cudaError_t _e = (expr);                                                         \
+        if (_e != cudaSuccess) {                                                         \
+            lymph_set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));         \
+            return (_e == cudaErrorMemoryAllocation) ? LYMPH_ERR_OOM : LYMPH_ERR_CUDA;   \
+        }                                                                                \
+    } while (0)
+
+#define LYMPH_TRY(expr)            \
+    do {                           \
+        int _rc = (expr);          \
+        if (_rc != LYMPH_OK) return _rc; \
+    } while (0)
+
+// Device status word bits (set by kernels, read back by the host).
+enum : int {
+    ST_NOT_SPD = 1,      // Cholesky pivot <= 0
+    ST_NONFINITE = 2,    // NaN/Inf in a state vector
+    ST_BAD_INDEX = 4,    // an index failed its bounds check
+    ST_DEGENERATE = 8,   // zero-volume tetrahedron / zero-area face
+};
+
+constexpr int MAX_DEGREE = 4;     // device path supports p = 1..4 (Np <= 35)
+constexpr int MAX_NP = 35;
+constexpr int MAX_NQ3 = 125;
+constexpr int MAX_NQ2 = 25;
+
+// ---------------------------------------------------------------------------
+// reference tables in device memory (one copy per context, degree-specific)
+// ---------------------------------------------------------------------------
+struct RefTables {
+    double nodtet3[MAX_NQ3 * 4];   // [q][4]  mapped Duffy nodes (xi, eta, zeta, 1)
+    double weitet3[MAX_NQ3];
+    double nodtria2[MAX_NQ2 * 4];  // [q][4]  (s, t, 1, 1)
+    double weitria2[MAX_NQ2];
+    double node_maps[4 * 16];      // [face][row][col]
+    int blist[MAX_NP * 3];         // [f][3]
+};
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct lymph_ctx {
+    // method
+    int p = 1, Np = 4, nd = 12, nq3 = 8, nq2 = 4, precision = LYMPH_FP64;
+    double alpha = 10.0, theta = -1.0, dt = 1e-3;
+    // sizes
+    int n_node = 0, n_tet = 0, n_poly = 0, n_mat = 0;
+    int64_t n_blocks = 0, n_face_sides = 0, n_block_faces = 0;
+    cudaStream_t stream = nullptr;
+    // host copies needed for set-up logic
+    std::vector<int32_t> h_row_ptr, h_col;
+    // device mesh
+    double* d_coords = nullptr;
+    int32_t *d_tet_vert = nullptr, *d_tet_poly = nullptr, *d_tet_mat = nullptr, *d_neigh = nullptr, *d_fun_tag = nullptr;
+    double* d_mat = nullptr;
+    RefTables* d_ref = nullptr;
+    // derived geometry
+    double *d_fk = nullptr, *d_jdet = nullptr, *d_normal = nullptr, *d_area = nullptr;
+    double *d_bbox = nullptr, *d_hk = nullptr;
+    int32_t *d_poly_ptr = nullptr, *d_poly_tets = nullptr;
+    // block pattern: row_ptr[n_poly+1], col[n_blocks], blk_row[n_blocks],
+    // face lists per block bf_ptr[n_blocks+1] / bf[...] (encoded t*4+f)
+    int32_t *d_row_ptr = nullptr, *d_col = nullptr, *d_blk_row = nullptr;
+    int64_t* d_bf_ptr = nullptr;
+    int32_t* d_bf = nullptr;
+    // operator
+    void* d_K = nullptr;            // [n_blocks][nd][nd] column-major per block (FP64 or FP32)
+    double *d_M = nullptr, *d_Mm = nullptr, *d_R = nullptr, *d_Rm = nullptr, *d_RT = nullptr, *d_RmT = nullptr;
+    double *d_rhs_stat = nullptr, *d_rhs_dyn = nullptr;
+    // state: two rotating step buffers + V0 + UEX
+    double* d_buf[2] = {nullptr, nullptr};
+    int cur = 1;                    // d_buf[cur] holds UN, d_buf[cur^1] holds U0
+    double *d_v0 = nullptr, *d_uex = nullptr;
+    // misc
+    double* d_gvals = nullptr;      // time-function values of a run
+    int64_t gvals_cap = 0;
+    int64_t* d_step_idx = nullptr;
+    double* d_partial = nullptr;    // per-polyhedron partial sums (error norms)
+    double* d_scalar = nullptr;
+    int* d_status = nullptr;
+    bool have_matrices = false, have_rhs_stat = false, have_rhs_dyn = false;
+    int64_t launches = 0;
+    int64_t device_bytes = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_steps = 0;
+    int graph_parity = -1;
+};
+
+double* lymph_slot_ptr(lymph_ctx* c, int slot);
+
+// ---------------------------------------------------------------------------
+// device helpers: the reference's Legendre evaluation on a bounding-box
+// interval (basis_function.f90:268-437), one point, one degree.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline double lp_nonnorm(double xp, int p) {
+    double x2 = xp * xp, x3 = x2 * xp, x4 = x2 * x2, x5 = x4 * xp, x6 = x3 * x3;
+    switch (p) {
+        case 0: return 1.0;
+        case 1: return xp;
+        case 2: return (3 * x2 - 1) / 2;
+        case 3: return (5 * x3 - 3 * xp) / 2;
+        case 4: return (35 * x4 - 30 * x2 + 3) / 8;
+        case 5: return (63 * x5 - 70 * x3 + 15 * xp) / 8;
+        case 6: return (231 * x6 - 315 * x4 + 105 * x2 - 5) / 16;
+        default: return 0.0;
+    }
+}
+
+__host__ __device__ inline double lp_der_nonnorm(double xp, int p) {
+    double x2 = xp * xp, x3 = x2 * xp, x4 = x2 * x2, x5 = x4 * xp;
+    switch (p) {
+        case 0: return 0.0;
+        case 1: return 1.0;
+        case 2: return 3 * xp;
+        case 3: return (15 * x2 - 3) / 2;
+        case 4: return (35 * x3 - 15 * xp) / 2;
+        case 5: return (315 * x4 - 210 * x2 + 15) / 8;
+        case 6: return (1386 * x5 - 1260 * x3 + 210 * xp - 5) / 16;
+        default: return 0.0;
+    }
+}
+
+// Value and derivative of the scaled Legendre polynomial of degree p on
+// [a,b] at x: L_p(xp)/sqrt(hb) and L'_p(xp)/(hb sqrt(hb)) with
+// xp = (x - mb)/hb (LegendreP / GradLegendreP).
+__host__ __device__ inline void legendre_1d(double x, int p, double a, double b, double* v, double* d) {
+    double hb = (b - a) / 2.0, mb = (b + a) / 2.0;
+    double xp = (x - mb) / hb;
+    double sh = sqrt(hb);
+    *v = lp_nonnorm(xp, p) / sh;
+    *d = lp_der_nonnorm(xp, p) / (hb * sh);
+}
+
+// Basis function f and its gradient at physical point pt for bounding box
+// bb (xmin,xmax,ymin,ymax,zmin,zmax): phi = Lx Ly Lz, dphi = (Lx' Ly Lz,
+// Lx Ly' Lz, Lx Ly Lz') (basis, basis_function.f90:508-513).
+__host__ __device__ inline void basis_eval(const double pt[3], const double* bb, const int* bl, double* phi,
+                                           double* dphi) {
+    double vx, dx, vy, dy, vz, dz;
+    legendre_1d(pt[0], bl[0], bb[0], bb[1], &vx, &dx);
+    legendre_1d(pt[1], bl[1], bb[2], bb[3], &vy, &dy);
+    legendre_1d(pt[2], bl[2], bb[4], bb[5], &vz, &dz);
+    *phi = vx * vy * vz;
+    dphi[0] = dx * vy * vz;
+    dphi[1] = vx * dy * vz;
+    dphi[2] = vx * vy * dz;
+}
+
+inline int np_of(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }
+
+// launch helpers (defined in abi.cu)
+int lymph_sync_status(lymph_ctx* c, const char* where);

@@ -1,0 +1,284 @@
+// step.cu -- the per-step hot kernel and the error norms.
+//
+// One CTA per polyhedron P fuses what TIME_STEP_MATRIX_FREE
+// (src/matrix_free.f90:1230-1385) does for one element:
+//   1. y = sum_b K_{P,col(b)} u_{col(b)}     (self + neighbour blocks; the
+//      neighbour coefficients the reference receives by MPI_EXCHANGE_DOF are
+//      gathered from global memory, L2-resident)
+//   2. tmp = -y + F_stat + F_dyn g(t)
+//   3. per component solve_LU(R^T, R, tmp)   (vet_mat_operations.f90:123-153)
+//   4. u^{n+1} = dt^2 x + 2 u^n - u^{n-1}    (written over u^{n-1} in place)
+// Blocks are stored column-major so that thread r (row r) reads
+// K[c][r] for consecutive r: coalesced, streamed once per step with an
+// evict-first hint so the state vectors stay in L2.  Threads are laid out as
+// S column slices x ND rows, S chosen per degree so that ND*S fills whole
+// warps; the S partial sums of a row are combined in a fixed order.
+
+#include "common.cuh"
+
+namespace {
+
+template <int P> struct Deg {
+    static constexpr int NP = (P + 1) * (P + 2) * (P + 3) / 6;
+    static constexpr int ND = 3 * NP;
+};
+
+// column slices per degree: ND*S = 96, 240, 480, 315 threads
+template <int P> struct Slices { static constexpr int S = P == 1 ? 8 : (P == 2 ? 8 : (P == 3 ? 8 : 3)); };
+
+constexpr int NBB = 16;   // neighbour blocks staged in shared memory at once
+
+enum { MODE_STEP = 0, MODE_FIRST = 1, MODE_DG = 2 };
+
+struct StepArgs {
+    const int32_t* row_ptr;
+    const int32_t* col;
+    const void* K;             // [n_blocks][ND][ND] column-major (double or float)
+    const double* R;           // [n_poly][NP][NP] upper Cholesky factor of M_loc
+    const double* RT;          // its transpose
+    const double* rhs_stat;
+    const double* rhs_dyn;
+    const double* gvals;       // time-function values
+    const int64_t* step_idx;   // index into gvals (device counter)
+    const double* u0;          // u^{n-1} (MODE_STEP), u^0 (MODE_FIRST), u_h (MODE_DG)
+    const double* un;          // u^n (MODE_STEP), v^0 (MODE_FIRST), u_ex (MODE_DG)
+    double* out;               // u^{n+1} (MODE_STEP: may alias u0), u^1 (MODE_FIRST)
+    double* partial;           // MODE_DG: per-polyhedron du . (A du)
+    double dt;
+    int* status;
+    int n_poly;
+};
+
+__device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+
+__device__ inline void warp_solve_rtr(int NP, const double* __restrict__ R, const double* __restrict__ RT, double* b,
+                                      int lane) {
+    for (int j = 0; j < NP; ++j) {
+        const double yj = b[j] / R[j * NP + j];
+        __syncwarp();
+        for (int i = j + 1 + lane; i < NP; i += 32) b[i] = b[i] - R[j * NP + i] * yj;
+        if (lane == 0) b[j] = yj;
+        __syncwarp();
+    }
+    for (int j = NP - 1; j >= 0; --j) {
+        const double xj = b[j] / R[j * NP + j];
+        __syncwarp();
+        for (int i = lane; i < j; i += 32) b[i] = b[i] - RT[j * NP + i] * xj;
+        if (lane == 0) b[j] = xj;
+        __syncwarp();
+    }
+}
+
+template <int PD, typename KT, int MODE>
+__global__ void __launch_bounds__(((Deg<PD>::ND * Slices<PD>::S + 31) / 32) * 32)
+k_step(StepArgs A) {
+    constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND, S = Slices<PD>::S;
+    constexpr int T = ((ND * S + 31) / 32) * 32;
+    constexpr int CPT = (ND + S - 1) / S;
+    using AT = KT;  // accumulation type: FP64 blocks accumulate in FP64, FP32 blocks in FP32
+    __shared__ AT s_u[NBB * ND];
+    __shared__ AT s_red[S * ND];
+    __shared__ double s_b[ND];
+
+    const int P = blockIdx.x;
+    const int tid = threadIdx.x;
+    const int r = tid % ND, s = tid / ND;
+    const bool act = tid < ND * S;
+    const int rb = A.row_ptr[P], re = A.row_ptr[P + 1];
+    const KT* Kbase = (const KT*)A.K;
+
+    AT acc0 = 0, acc1 = 0;
+    for (int b0 = rb; b0 < re; b0 += NBB) {
+        const int nb = (re - b0) < NBB ? (re - b0) : NBB;
+        __syncthreads();
+        for (int i = tid; i < nb * ND; i += T) {
+            const int bb = i / ND, c = i % ND;
+            const int64_t q = (int64_t)A.col[b0 + bb] * ND + c;
+            double v = A.u0[q];
+            if (MODE == MODE_STEP) v = A.un[q];
+            if (MODE == MODE_DG) v = A.u0[q] - A.un[q];
+            s_u[i] = (AT)v;
+        }
+        __syncthreads();
+        if (act) {
+            for (int bb = 0; bb < nb; ++bb) {
+                const KT* Kb = Kbase + (int64_t)(b0 + bb) * ND * ND + r;
+                const AT* ub = s_u + bb * ND;
+#pragma unroll
+                for (int j = 0; j < CPT; j += 2) {
+                    const int c0 = s + j * S;
+                    if (c0 < ND) acc0 += (AT)ld_stream(Kb + (int64_t)c0 * ND) * ub[c0];
+                    const int c1 = s + (j + 1) * S;
+                    if (j + 1 < CPT && c1 < ND) acc1 += (AT)ld_stream(Kb + (int64_t)c1 * ND) * ub[c1];
+                }
+            }
+        }
+    }
+    if (act) s_red[s * ND + r] = acc0 + acc1;
+    __syncthreads();
+    if (MODE == MODE_DG) {
+        if (tid == 0) {
+            double e = 0.0;
+            for (int rr = 0; rr < ND; ++rr) {
+                double y = 0.0;
+                for (int ss = 0; ss < S; ++ss) y += (double)s_red[ss * ND + rr];
+                const int64_t q = (int64_t)P * ND + rr;
+                e = e + (A.u0[q] - A.un[q]) * y;
+            }
+            A.partial[P] = e;
+        }
+        return;
+    }
+    const double g = A.gvals[*A.step_idx];
+    if (tid < ND) {
+        double y = 0.0;
+        for (int ss = 0; ss < S; ++ss) y += (double)s_red[ss * ND + tid];
+        const int64_t q = (int64_t)P * ND + tid;
+        s_b[tid] = -y + A.rhs_stat[q] + A.rhs_dyn[q] * g;
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp < 3)
+        warp_solve_rtr(NP, A.R + (int64_t)P * NP * NP, A.RT + (int64_t)P * NP * NP, &s_b[warp * NP], lane);
+    __syncthreads();
+    if (tid < ND) {
+        const int64_t q = (int64_t)P * ND + tid;
+        double v;
+        if (MODE == MODE_STEP) {
+            const double dt2 = A.dt * A.dt;
+            v = dt2 * s_b[tid] + 2.0 * A.un[q] - A.u0[q];
+        } else {
+            const double half_dt2 = 0.5 * (A.dt * A.dt);
+            v = half_dt2 * s_b[tid] + A.u0[q] + A.dt * A.un[q];
+        }
+        if (!isfinite(v)) atomicOr(A.status, ST_NONFINITE);
+        A.out[q] = v;
+    }
+}
+
+__global__ void k_bump(int64_t* idx) { *idx += 1; }
+
+// COMPUTE_ERROR_L2_MATRIX_FREE body per polyhedron: sum_i du_i^T M du_i.
+__global__ void k_l2_partial(int n_poly, int NP, const double* __restrict__ Mm, const double* __restrict__ uh,
+                             const double* __restrict__ uex, double* partial) {
+    const int P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= n_poly) return;
+    const int ND = 3 * NP;
+    double err = 0.0;
+    const double* M = Mm + (int64_t)P * NP * NP;
+    for (int i = 0; i < 3; ++i) {
+        double e = 0.0;
+        for (int rr = 0; rr < NP; ++rr) {
+            double t = 0.0;
+            for (int c = 0; c < NP; ++c) {
+                const int64_t qc = (int64_t)P * ND + i * NP + c;
+                t = t + M[rr * NP + c] * (uh[qc] - uex[qc]);
+            }
+            const int64_t qr = (int64_t)P * ND + i * NP + rr;
+            e = e + (uh[qr] - uex[qr]) * t;
+        }
+        err = err + e;
+    }
+    partial[P] = err;
+}
+
+// Deterministic sum of n values: fixed per-thread strided order, then a
+// fixed shared-memory tree.
+__global__ void k_sum(int64_t n, const double* __restrict__ v, double* out) {
+    __shared__ double red[1024];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += v[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+template <int PD, typename KT, int MODE>
+int launch_step_t(lymph_ctx* c, const StepArgs& A) {
+    constexpr int T = ((Deg<PD>::ND * Slices<PD>::S + 31) / 32) * 32;
+    k_step<PD, KT, MODE><<<c->n_poly, T, 0, c->stream>>>(A);
+    c->launches++;
+    return LYMPH_OK;
+}
+
+template <typename KT, int MODE>
+int launch_step_p(lymph_ctx* c, const StepArgs& A) {
+    switch (c->p) {
+        case 1: return launch_step_t<1, KT, MODE>(c, A);
+        case 2: return launch_step_t<2, KT, MODE>(c, A);
+        case 3: return launch_step_t<3, KT, MODE>(c, A);
+        case 4: return launch_step_t<4, KT, MODE>(c, A);
+        default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
+    }
+}
+
+template <int MODE>
+int launch_step_mode(lymph_ctx* c, const StepArgs& A, bool fp32) {
+    return fp32 ? launch_step_p<float, MODE>(c, A) : launch_step_p<double, MODE>(c, A);
+}
+
+StepArgs base_args(lymph_ctx* c) {
+    StepArgs A;
+    A.row_ptr = c->d_row_ptr; A.col = c->d_col; A.K = c->d_K; A.R = c->d_R; A.RT = c->d_RT;
+    A.rhs_stat = c->d_rhs_stat; A.rhs_dyn = c->d_rhs_dyn; A.gvals = c->d_gvals; A.step_idx = c->d_step_idx;
+    A.u0 = nullptr; A.un = nullptr; A.out = nullptr; A.partial = c->d_partial; A.dt = c->dt; A.status = c->d_status;
+    A.n_poly = c->n_poly;
+    return A;
+}
+
+}  // namespace
+
+// One leapfrog step on the context stream (no rotation): reads U0/UN buffers,
+// writes u^{n+1} over U0.  The caller flips c->cur afterwards.
+int lymph_dev_step(lymph_ctx* c, bool bump) {
+    StepArgs A = base_args(c);
+    A.u0 = c->d_buf[c->cur ^ 1];
+    A.un = c->d_buf[c->cur];
+    A.out = c->d_buf[c->cur ^ 1];
+    LYMPH_TRY(launch_step_mode<MODE_STEP>(c, A, c->precision == LYMPH_MIXED));
+    if (bump) {
+        k_bump<<<1, 1, 0, c->stream>>>(c->d_step_idx);
+        c->launches++;
+    }
+    return LYMPH_OK;
+}
+
+int lymph_dev_bump(lymph_ctx* c) {
+    k_bump<<<1, 1, 0, c->stream>>>(c->d_step_idx);
+    c->launches++;
+    return LYMPH_OK;
+}
+
+int lymph_dev_first_step(lymph_ctx* c) {
+    StepArgs A = base_args(c);
+    A.u0 = c->d_buf[c->cur ^ 1];
+    A.un = c->d_v0;
+    A.out = c->d_buf[c->cur];
+    return launch_step_mode<MODE_FIRST>(c, A, c->precision == LYMPH_MIXED);
+}
+
+// du . (A du) per polyhedron with FP64 A_dg blocks in `blocks`, then the sum.
+int lymph_dev_error_dg(lymph_ctx* c, const void* blocks, const double* uh, const double* uex, double* d_out) {
+    StepArgs A = base_args(c);
+    A.K = blocks;
+    A.u0 = uh;
+    A.un = uex;
+    LYMPH_TRY(launch_step_mode<MODE_DG>(c, A, false));
+    k_sum<<<1, 1024, 0, c->stream>>>(c->n_poly, c->d_partial, d_out);
+    c->launches++;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+int lymph_dev_error_l2(lymph_ctx* c, const double* uh, const double* uex, double* d_out) {
+    k_l2_partial<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->Np, c->d_Mm, uh, uex, c->d_partial);
+    k_sum<<<1, 1024, 0, c->stream>>>(c->n_poly, c->d_partial, d_out);
+    c->launches += 2;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
