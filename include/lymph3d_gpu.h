@@ -218,7 +218,8 @@ int lymph_compute_error_dg_free(lymph_ctx* ctx, int slot_uh, int slot_uex, doubl
 int lymph_get_pattern(lymph_ctx* ctx, int32_t* row_ptr, int32_t* col);
 int lymph_get_blocks(lymph_ctx* ctx, int which, double* vals);
 /* Mass data per polyhedron, [n_poly][Np][Np] row-major: which = 0 M_loc (rho
- * weighted), 1 M_modal_loc, 2 R_M_loc (upper Cholesky factor), 3 R_M_modal_loc. */
+ * weighted), 1 M_modal_loc, 2 R_M_loc (upper Cholesky factor), 3 R_M_modal_loc,
+ * 4 the inverse of M_loc the step kernel applies. */
 int lymph_get_mass(lymph_ctx* ctx, int which, double* vals);
 /* RHS vectors [n_poly][3Np] (which = LYMPH_RHS_STAT / LYMPH_RHS_DYN). */
 int lymph_get_rhs(lymph_ctx* ctx, int which, double* vals);

@@ -183,7 +183,7 @@ int lymph_destroy(lymph_ctx* c) {
     void* ptrs[] = {c->d_coords, c->d_tet_vert, c->d_tet_poly, c->d_tet_mat, c->d_neigh, c->d_fun_tag, c->d_mat,
                     c->d_ref, c->d_fk, c->d_jdet, c->d_normal, c->d_area, c->d_bbox, c->d_hk, c->d_poly_ptr,
                     c->d_poly_tets, c->d_row_ptr, c->d_col, c->d_blk_row, c->d_bf_ptr, c->d_bf, c->d_K, c->d_M,
-                    c->d_Mm, c->d_R, c->d_Rm, c->d_RT, c->d_RmT, c->d_rhs_stat, c->d_rhs_dyn, c->d_buf[0], c->d_buf[1],
+                    c->d_Mm, c->d_R, c->d_Rm, c->d_RT, c->d_RmT, c->d_Minv, c->d_rhs_stat, c->d_rhs_dyn, c->d_buf[0], c->d_buf[1],
                     c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status};
     for (void* p : ptrs) dfree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -368,6 +368,7 @@ int lymph_make_matrices(lymph_ctx* c) {
         LYMPH_TRY(dalloc(c, &c->d_RT, nm));
         LYMPH_TRY(dalloc(c, &c->d_Rm, nm));
         LYMPH_TRY(dalloc(c, &c->d_RmT, nm));
+        LYMPH_TRY(dalloc(c, &c->d_Minv, nm));
     }
     LYMPH_TRY(lymph_dev_assemble(c, LYMPH_BLOCKS_K, c->d_K, c->precision == LYMPH_MIXED, true));
     LYMPH_TRY(lymph_dev_cholesky(c));
@@ -616,10 +617,20 @@ int lymph_get_blocks(lymph_ctx* c, int which, double* vals) {
 }
 
 int lymph_get_mass(lymph_ctx* c, int which, double* vals) {
-    if (!c || !vals || which < 0 || which > 3) return LYMPH_ERR_INVALID;
+    if (!c || !vals || which < 0 || which > 4) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_get_mass: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
-    const double* src[4] = {c->d_M, c->d_Mm, c->d_R, c->d_Rm};
-    LYMPH_CUDA_TRY(cudaMemcpy(vals, src[which], sizeof(double) * (size_t)c->n_poly * c->Np * c->Np, cudaMemcpyDeviceToHost));
+    const double* src[5] = {c->d_M, c->d_Mm, c->d_R, c->d_Rm, c->d_Minv};
+    const size_t nm = (size_t)c->n_poly * c->Np * c->Np;
+    LYMPH_CUDA_TRY(cudaMemcpy(vals, src[which], sizeof(double) * nm, cudaMemcpyDeviceToHost));
+    if (which == 4) {  // stored column-major per polyhedron
+        const int Np = c->Np;
+        std::vector<double> t(Np * Np);
+        for (int P = 0; P < c->n_poly; ++P) {
+            double* b = vals + (size_t)P * Np * Np;
+            for (int i = 0; i < Np * Np; ++i) t[(i % Np) * Np + i / Np] = b[i];
+            std::memcpy(b, t.data(), sizeof(double) * Np * Np);
+        }
+    }
     return LYMPH_OK;
 }
 

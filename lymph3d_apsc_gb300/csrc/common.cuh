@@ -85,6 +85,7 @@ struct lymph_ctx {
     // operator
     void* d_K = nullptr;            // [n_blocks][nd][nd] column-major per block (FP64 or FP32)
     double *d_M = nullptr, *d_Mm = nullptr, *d_R = nullptr, *d_Rm = nullptr, *d_RT = nullptr, *d_RmT = nullptr;
+    double* d_Minv = nullptr;       // [n_poly][Np][Np] column-major inverse of M_loc
     double *d_rhs_stat = nullptr, *d_rhs_dyn = nullptr;
     // state: two rotating step buffers + V0 + UEX
     double* d_buf[2] = {nullptr, nullptr};

@@ -418,6 +418,31 @@ __global__ void k_cholesky(int n_poly, int NP, const double* __restrict__ A, dou
     }
 }
 
+// Inverse of the mass matrix from its Cholesky factor: column k of M^-1 is
+// solve_LU(R^T, R, e_k) (vet_mat_operations.f90:123-153, reference operation
+// order), one lane per column.  Stored column-major: Minv[c*NP + r] = (M^-1)(r,c),
+// so that lane r of a warp reads consecutive addresses when applying it.
+__global__ void k_mass_inverse(int n_poly, int NP, const double* __restrict__ R, double* Minv) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n_poly) return;
+    const double* r = R + (int64_t)warp * NP * NP;
+    double* out = Minv + (int64_t)warp * NP * NP;
+    for (int k = lane; k < NP; k += 32) {
+        double* x = out + (int64_t)k * NP;  // column k, solved in place
+        for (int i = 0; i < NP; ++i) x[i] = (i == k) ? 1.0 : 0.0;
+        for (int i = 0; i < NP; ++i) {
+            double y = x[i];
+            for (int j = 0; j < i; ++j) y = y - r[j * NP + i] * x[j];
+            x[i] = y / r[i * NP + i];
+        }
+        for (int i = NP - 1; i >= 0; --i) {
+            double v = x[i];
+            for (int j = i + 1; j < NP; ++j) v = v - r[i * NP + j] * x[j];
+            x[i] = v / r[i * NP + i];
+        }
+    }
+}
+
 // ---- data functions (problem_data_and_properties.f90) ----
 __device__ inline void dev_u_space(const double p[3], double r[3]) {
     const double PI = 3.141592653589793;
@@ -727,7 +752,8 @@ int lymph_dev_cholesky(lymph_ctx* c) {
     unsigned grid = (unsigned)((c->n_poly + warps_per_block - 1) / warps_per_block);
     k_cholesky<<<grid, 32 * warps_per_block, smem, c->stream>>>(c->n_poly, c->Np, c->d_M, c->d_R, c->d_RT, c->d_status);
     k_cholesky<<<grid, 32 * warps_per_block, smem, c->stream>>>(c->n_poly, c->Np, c->d_Mm, c->d_Rm, c->d_RmT, c->d_status);
-    c->launches += 2;
+    k_mass_inverse<<<grid, 32 * warps_per_block, 0, c->stream>>>(c->n_poly, c->Np, c->d_R, c->d_Minv);
+    c->launches += 3;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
 }

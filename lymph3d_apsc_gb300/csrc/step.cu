@@ -6,7 +6,9 @@
 //      neighbour coefficients the reference receives by MPI_EXCHANGE_DOF are
 //      gathered from global memory, L2-resident)
 //   2. tmp = -y + F_stat + F_dyn g(t)
-//   3. per component solve_LU(R^T, R, tmp)   (vet_mat_operations.f90:123-153)
+//   3. x = M^-1 tmp per component: the value of the reference's
+//      solve_LU(R^T, R, tmp) (vet_mat_operations.f90:123-153), applied as a
+//      dense FP64 product with the inverse built once from the same factor
 //   4. u^{n+1} = dt^2 x + 2 u^n - u^{n-1}    (written over u^{n-1} in place)
 // Blocks are stored column-major so that thread r (row r) reads
 // K[c][r] for consecutive r: coalesced, streamed once per step with an
@@ -23,8 +25,14 @@ template <int P> struct Deg {
     static constexpr int ND = 3 * NP;
 };
 
-// column slices per degree: ND*S = 96, 240, 480, 315 threads
-template <int P> struct Slices { static constexpr int S = P == 1 ? 8 : (P == 2 ? 8 : (P == 3 ? 8 : 3)); };
+// Thread shape per degree: S column slices x ND rows (ND*S fills whole warps
+// but for a few lanes), and the CTAs per SM the launch bounds ask for.
+template <int P> struct Shape {
+    static constexpr int ND = Deg<P>::ND;
+    static constexpr int S = P == 1 ? 8 : (P == 2 ? 8 : (P == 3 ? 4 : 3));
+    static constexpr int T = ((ND * S + 31) / 32) * 32;       // 96, 256, 256, 320
+    static constexpr int MINB = P == 1 ? 16 : (P == 4 ? 4 : 6);
+};
 
 constexpr int NBB = 16;   // neighbour blocks staged in shared memory at once
 
@@ -34,8 +42,7 @@ struct StepArgs {
     const int32_t* row_ptr;
     const int32_t* col;
     const void* K;             // [n_blocks][ND][ND] column-major (double or float)
-    const double* R;           // [n_poly][NP][NP] upper Cholesky factor of M_loc
-    const double* RT;          // its transpose
+    const double* Minv;        // [n_poly][NP][NP] column-major inverse of M_loc
     const double* rhs_stat;
     const double* rhs_dyn;
     const double* gvals;       // time-function values
@@ -52,31 +59,17 @@ struct StepArgs {
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 
-__device__ inline void warp_solve_rtr(int NP, const double* __restrict__ R, const double* __restrict__ RT, double* b,
-                                      int lane) {
-    for (int j = 0; j < NP; ++j) {
-        const double yj = b[j] / R[j * NP + j];
-        __syncwarp();
-        for (int i = j + 1 + lane; i < NP; i += 32) b[i] = b[i] - R[j * NP + i] * yj;
-        if (lane == 0) b[j] = yj;
-        __syncwarp();
-    }
-    for (int j = NP - 1; j >= 0; --j) {
-        const double xj = b[j] / R[j * NP + j];
-        __syncwarp();
-        for (int i = lane; i < j; i += 32) b[i] = b[i] - RT[j * NP + i] * xj;
-        if (lane == 0) b[j] = xj;
-        __syncwarp();
-    }
-}
-
+// One CTA per polyhedron.  The block row of P is one contiguous column-major
+// [ND x nb*ND] matrix (its blocks are adjacent in memory), multiplied by the
+// gathered coefficients of the column polyhedra.  The mass-matrix inverse is
+// applied in FP64 as a dense Np x Np product per component (precomputed from
+// the Cholesky factor), which replaces the reference's two triangular solves
+// per component with a parallel product of the same value.
 template <int PD, typename KT, int MODE>
-__global__ void __launch_bounds__(((Deg<PD>::ND * Slices<PD>::S + 31) / 32) * 32)
-k_step(StepArgs A) {
-    constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND, S = Slices<PD>::S;
-    constexpr int T = ((ND * S + 31) / 32) * 32;
+__global__ void __launch_bounds__(Shape<PD>::T, Shape<PD>::MINB) k_step(StepArgs A) {
+    constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND, S = Shape<PD>::S, T = Shape<PD>::T;
     constexpr int CPT = (ND + S - 1) / S;
-    using AT = KT;  // accumulation type: FP64 blocks accumulate in FP64, FP32 blocks in FP32
+    using AT = KT;  // FP64 blocks accumulate in FP64, FP32 blocks in FP32
     __shared__ AT s_u[NBB * ND];
     __shared__ AT s_red[S * ND];
     __shared__ double s_b[ND];
@@ -95,9 +88,10 @@ k_step(StepArgs A) {
         for (int i = tid; i < nb * ND; i += T) {
             const int bb = i / ND, c = i % ND;
             const int64_t q = (int64_t)A.col[b0 + bb] * ND + c;
-            double v = A.u0[q];
+            double v;
             if (MODE == MODE_STEP) v = A.un[q];
-            if (MODE == MODE_DG) v = A.u0[q] - A.un[q];
+            else if (MODE == MODE_FIRST) v = A.u0[q];
+            else v = A.u0[q] - A.un[q];
             s_u[i] = (AT)v;
         }
         __syncthreads();
@@ -105,12 +99,19 @@ k_step(StepArgs A) {
             for (int bb = 0; bb < nb; ++bb) {
                 const KT* Kb = Kbase + (int64_t)(b0 + bb) * ND * ND + r;
                 const AT* ub = s_u + bb * ND;
+                KT kv[CPT];
 #pragma unroll
-                for (int j = 0; j < CPT; j += 2) {
-                    const int c0 = s + j * S;
-                    if (c0 < ND) acc0 += (AT)ld_stream(Kb + (int64_t)c0 * ND) * ub[c0];
-                    const int c1 = s + (j + 1) * S;
-                    if (j + 1 < CPT && c1 < ND) acc1 += (AT)ld_stream(Kb + (int64_t)c1 * ND) * ub[c1];
+                for (int j = 0; j < CPT; ++j) {
+                    const int c = s + j * S;
+                    kv[j] = (c < ND) ? ld_stream(Kb + (int64_t)c * ND) : (KT)0;
+                }
+#pragma unroll
+                for (int j = 0; j < CPT; ++j) {
+                    const int c = s + j * S;
+                    if (c < ND) {
+                        if (j & 1) acc1 += (AT)kv[j] * ub[c];
+                        else acc0 += (AT)kv[j] * ub[c];
+                    }
                 }
             }
         }
@@ -138,19 +139,25 @@ k_step(StepArgs A) {
         s_b[tid] = -y + A.rhs_stat[q] + A.rhs_dyn[q] * g;
     }
     __syncthreads();
-    const int warp = tid >> 5, lane = tid & 31;
-    if (warp < 3)
-        warp_solve_rtr(NP, A.R + (int64_t)P * NP * NP, A.RT + (int64_t)P * NP * NP, &s_b[warp * NP], lane);
-    __syncthreads();
     if (tid < ND) {
+        const int i = tid / NP, m = tid % NP;
+        const double* Mi = A.Minv + (int64_t)P * NP * NP + m;
+        const double* bi = s_b + i * NP;
+        double x0 = 0.0, x1 = 0.0;
+#pragma unroll
+        for (int c = 0; c < NP; c += 2) {
+            x0 += Mi[c * NP] * bi[c];
+            if (c + 1 < NP) x1 += Mi[(c + 1) * NP] * bi[c + 1];
+        }
+        const double x = x0 + x1;
         const int64_t q = (int64_t)P * ND + tid;
         double v;
         if (MODE == MODE_STEP) {
             const double dt2 = A.dt * A.dt;
-            v = dt2 * s_b[tid] + 2.0 * A.un[q] - A.u0[q];
+            v = dt2 * x + 2.0 * A.un[q] - A.u0[q];
         } else {
             const double half_dt2 = 0.5 * (A.dt * A.dt);
-            v = half_dt2 * s_b[tid] + A.u0[q] + A.dt * A.un[q];
+            v = half_dt2 * x + A.u0[q] + A.dt * A.un[q];
         }
         if (!isfinite(v)) atomicOr(A.status, ST_NONFINITE);
         A.out[q] = v;
@@ -200,8 +207,7 @@ __global__ void k_sum(int64_t n, const double* __restrict__ v, double* out) {
 
 template <int PD, typename KT, int MODE>
 int launch_step_t(lymph_ctx* c, const StepArgs& A) {
-    constexpr int T = ((Deg<PD>::ND * Slices<PD>::S + 31) / 32) * 32;
-    k_step<PD, KT, MODE><<<c->n_poly, T, 0, c->stream>>>(A);
+    k_step<PD, KT, MODE><<<c->n_poly, Shape<PD>::T, 0, c->stream>>>(A);
     c->launches++;
     return LYMPH_OK;
 }
@@ -224,7 +230,7 @@ int launch_step_mode(lymph_ctx* c, const StepArgs& A, bool fp32) {
 
 StepArgs base_args(lymph_ctx* c) {
     StepArgs A;
-    A.row_ptr = c->d_row_ptr; A.col = c->d_col; A.K = c->d_K; A.R = c->d_R; A.RT = c->d_RT;
+    A.row_ptr = c->d_row_ptr; A.col = c->d_col; A.K = c->d_K; A.Minv = c->d_Minv;
     A.rhs_stat = c->d_rhs_stat; A.rhs_dyn = c->d_rhs_dyn; A.gvals = c->d_gvals; A.step_idx = c->d_step_idx;
     A.u0 = nullptr; A.un = nullptr; A.out = nullptr; A.partial = c->d_partial; A.dt = c->dt; A.status = c->d_status;
     A.n_poly = c->n_poly;

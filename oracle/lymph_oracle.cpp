@@ -49,6 +49,34 @@ const int BC_DIRI = -1, BC_NEUM = -2, BC_ABSO = -3;  // Poly_global.f90:420-422
 
 thread_local std::string g_err;
 
+// Noise-floor instrument for the tests: when non-zero, every value a data
+// function returns is moved by +-g_perturb_ulps units in the last place, the
+// sign drawn from a hash of the evaluation point.  It models the 1-2 ulp
+// differences between two libm implementations of sin/cos.
+int g_perturb_ulps = 0;
+
+// Second instrument: when set, the operator apply of the time steps sums the
+// blocks of a row and the entries of every row dot product in reverse order.
+// The spread between the two orders is the algorithm's own rounding floor.
+int g_reverse_sums = 0;
+
+double perturb(double v, const double p[3], int comp) {
+    if (g_perturb_ulps == 0 || v == 0.0) return v;
+    uint64_t h = 1469598103934665603ull ^ (uint64_t)comp;
+    for (int k = 0; k < 3; ++k) {
+        uint64_t b;
+        std::memcpy(&b, &p[k], 8);
+        h = (h ^ b) * 1099511628211ull;
+    }
+    double dir = (h >> 63) ? 1e308 : -1e308;
+    for (int k = 0; k < g_perturb_ulps; ++k) v = std::nextafter(v, dir);
+    return v;
+}
+
+void perturb3(double r[3], const double p[3]) {
+    for (int i = 0; i < 3; ++i) r[i] = perturb(r[i], p, i);
+}
+
 // ---------------------------------------------------------------------------
 // vet_mat_operations.f90
 // ---------------------------------------------------------------------------
@@ -372,6 +400,7 @@ void f_forcing(int id, double lambda, double mu, const double p[3], double rho, 
     } else {  // f_null :72-82
         r[0] = r[1] = r[2] = 0.0;
     }
+    perturb3(r, p);
 }
 
 void u_space(const double p[3], double r[3]) {  // uex :245-254
@@ -389,6 +418,7 @@ void g_dirichlet(int id, const double p[3], int tag, double r[3]) {
     } else {
         r[0] = r[1] = r[2] = 0.0;
     }
+    perturb3(r, p);
 }
 
 void g_neumann(int id, double lambda, double mu, const double n[3], const double p[3], int tag, double r[3]) {
@@ -403,6 +433,7 @@ void g_neumann(int id, double lambda, double mu, const double n[3], const double
     s[1][2] = 2.0 * mu * PI * std::cos(PI * p[1]) * std::cos(PI * p[2]) * std::sin(PI * p[0]); s[2][1] = s[1][2];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) r[i] = r[i] + s[i][j] * n[j];
+    perturb3(r, p);
 }
 
 void f_analytic(int id, const double p[3], double r[3]) {
@@ -415,6 +446,7 @@ void f_analytic(int id, const double p[3], double r[3]) {
     } else {  // ic_displacement, uex_stat: zero
         r[0] = r[1] = r[2] = 0.0;
     }
+    perturb3(r, p);
 }
 
 // ---------------------------------------------------------------------------
@@ -928,13 +960,18 @@ void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, in
     int nd = o.nd, Np = o.Np;
     std::vector<double> tmp(nd, 0.0), v(Np), x(Np);
     double g = time_function(t);
-    for (size_t b = 0; b < o.nbr[P].size(); ++b) {
+    const size_t nb = o.nbr[P].size();
+    for (size_t bi = 0; bi < nb; ++bi) {
+        size_t b = g_reverse_sums ? nb - 1 - bi : bi;
         int Qp = o.nbr[P][b];
         const double* Kb = &o.K[P][b * nd * nd];
         const double* uq = &u[(size_t)Qp * nd];
         for (int r = 0; r < nd; ++r) {
             double s = 0.0;  // matmul row r
-            for (int c = 0; c < nd; ++c) s = s + Kb[r * nd + c] * uq[c];
+            if (g_reverse_sums)
+                for (int c = nd - 1; c >= 0; --c) s = s + Kb[r * nd + c] * uq[c];
+            else
+                for (int c = 0; c < nd; ++c) s = s + Kb[r * nd + c] * uq[c];
             tmp[r] = tmp[r] + s;
         }
     }
@@ -955,6 +992,10 @@ void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, in
 extern "C" {
 
 const char* oracle_last_error(void) { return g_err.c_str(); }
+
+void oracle_set_data_perturbation(int ulps) { g_perturb_ulps = ulps; }
+
+void oracle_set_reverse_sums(int on) { g_reverse_sums = on; }
 
 int oracle_num_threads(void) {
 #ifdef _OPENMP

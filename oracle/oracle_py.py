@@ -35,6 +35,8 @@ def load():
         sigs = {
             "oracle_last_error": (c_char_p, []),
             "oracle_num_threads": (c_int, []),
+            "oracle_set_data_perturbation": (None, [c_int]),
+            "oracle_set_reverse_sums": (None, [c_int]),
             "oracle_set_threads": (None, [c_int]),
             "oracle_create": (c_int, [c_void_p, c_int, c_double, c_double, c_double, POINTER(c_void_p)]),
             "oracle_destroy": (c_int, [c_void_p]),
