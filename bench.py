@@ -47,6 +47,10 @@ CONFIGS = {
     # the headline configuration: 48k polyhedra, p = 3
     "c1": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 2.0, 1.0), lognormal=False,
                dt=2e-5, sample_n=10),
+    # a 16^3 x 6 cut of c1 (~3,000 polyhedra, ~1 GB of FP64 blocks): the small
+    # case the ncu captures use
+    "c1s": dict(n=16, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 2.0, 1.0), lognormal=False,
+                dt=2e-5, sample_n=8),
     # 48k polyhedra, p = 4, lognormal lambda/mu per polyhedron
     "c2": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=4, material=(1.0, 1.0, 1.0), lognormal=True,
                dt=2e-5, sample_n=8),

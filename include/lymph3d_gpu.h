@@ -227,6 +227,45 @@ int lymph_get_rhs(lymph_ctx* ctx, int which, double* vals);
  * and diameter hk [n_poly] (CREATE_BBOX_EL). */
 int lymph_get_poly_geometry(lymph_ctx* ctx, double* bbox, double* hk);
 
+/* Point source for the rhs selected by `which`: rhs[P] = dir_i phi_m(x0) for
+ * the polyhedron P of tetrahedron `tet` (find it with lymph_mesh_find_tet),
+ * zero elsewhere; its time dependence (e.g. a Ricker wavelet) comes through
+ * the time-function values of lymph_batch_run.  No counterpart in the
+ * reference's path (its only source is the double couple of
+ * src/matrix_free.f90:602-664, modelled on FIND_ELEM_FROM_POINT,
+ * src/find_tet.f90:82-124, for the point lookup). */
+int lymph_make_rhs_point(lymph_ctx* ctx, int which, int32_t tet, const double* x0, const double* dir);
+
+/* Time step after creation (e.g. from a CFL bound). */
+int lymph_set_dt(lymph_ctx* ctx, double dt);
+int lymph_get_dt(const lymph_ctx* ctx, double* dt);
+
+/* Largest eigenvalue modulus of M^-1 K by `iters` power iterations on the
+ * device operator; the leapfrog scheme is stable for dt < 2/sqrt(lam).
+ * Replaces the placeholder COMPUTE_CFL (src/checks.f90:14-39), which only
+ * tests dt against hmax. */
+int lymph_max_eigenvalue(lymph_ctx* ctx, int32_t iters, double* lam);
+
+/* ---- many problems in one persistent launch per step -------------------
+ * No counterpart in the reference (one problem per MPI job).  A batch
+ * references n assembled contexts (same precision; any degrees, meshes and
+ * dt).  lymph_batch_run advances every problem n_steps leapfrog steps
+ * (TIME_STEP_MATRIX_FREE each) with one persistent kernel per step over all
+ * (problem, polyhedron) items, launched as CUDA graphs; gvals holds the
+ * time-function value of every problem at every step, [n][n_steps].  Results
+ * equal stepping each context alone, bit for bit. */
+typedef struct lymph_batch lymph_batch;
+int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out);
+int lymph_batch_destroy(lymph_batch* batch);
+int lymph_batch_run(lymph_batch* batch, int64_t n_steps, const double* gvals, float* ms_total);
+/* Times trial_steps steps for each candidate (1..4 persistent CTAs per SM,
+ * items largest-cost-first or problem-major) and keeps the fastest; the
+ * problems' states are restored afterwards.  The choice is cached per batch
+ * signature in $LYMPH_TUNE_CACHE (default ~/.cache/lymph3d_gb300_tune.txt)
+ * and reused when use_cache is non-zero. */
+int lymph_batch_autotune(lymph_batch* batch, int32_t trial_steps, int32_t use_cache, int32_t* grid, int32_t* order);
+int lymph_batch_launch_count(const lymph_batch* batch, int64_t* count);
+
 /* Number of kernels this context launched so far (all kinds). */
 int lymph_launch_count(const lymph_ctx* ctx, int64_t* count);
 

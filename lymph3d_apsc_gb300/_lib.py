@@ -94,6 +94,15 @@ _SIGS = {
     "lymph_get_mass": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_get_rhs": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_get_poly_geometry": (c_int, [c_void_p, P_F64, P_F64]),
+    "lymph_make_rhs_point": (c_int, [c_void_p, c_int, c_int32, P_F64, P_F64]),
+    "lymph_set_dt": (c_int, [c_void_p, c_double]),
+    "lymph_get_dt": (c_int, [c_void_p, P_F64]),
+    "lymph_max_eigenvalue": (c_int, [c_void_p, c_int32, P_F64]),
+    "lymph_batch_create": (c_int, [POINTER(c_void_p), c_int32, POINTER(c_void_p)]),
+    "lymph_batch_destroy": (c_int, [c_void_p]),
+    "lymph_batch_run": (c_int, [c_void_p, c_int64, P_F64, POINTER(c_float)]),
+    "lymph_batch_autotune": (c_int, [c_void_p, c_int32, c_int32, P_I32, P_I32]),
+    "lymph_batch_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_device_bytes": (c_int, [c_void_p, POINTER(c_int64)]),
     # mesh utilities (lymph3d_mesh.h)

@@ -23,6 +23,8 @@ int lymph_dev_cholesky(lymph_ctx* c);
 int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scale, double* out);
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
+int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);
+int lymph_dev_point_source(lymph_ctx* c, int P, const double x0[3], const double dir[3], double* out);
 int lymph_dev_bump(lymph_ctx* c);
 int lymph_dev_error_dg(lymph_ctx* c, const void* blocks, const double* uh, const double* uex, double* d_out);
 int lymph_dev_error_l2(lymph_ctx* c, const double* uh, const double* uex, double* d_out);
@@ -646,6 +648,71 @@ int lymph_get_poly_geometry(lymph_ctx* c, double* bbox, double* hk) {
     if (bbox) LYMPH_CUDA_TRY(cudaMemcpy(bbox, c->d_bbox, sizeof(double) * 6 * (size_t)c->n_poly, cudaMemcpyDeviceToHost));
     if (hk) LYMPH_CUDA_TRY(cudaMemcpy(hk, c->d_hk, sizeof(double) * (size_t)c->n_poly, cudaMemcpyDeviceToHost));
     return LYMPH_OK;
+}
+
+int lymph_make_rhs_point(lymph_ctx* c, int which, int32_t tet, const double* x0, const double* dir) {
+    if (!c || !x0 || !dir || (which != LYMPH_RHS_STAT && which != LYMPH_RHS_DYN)) return LYMPH_ERR_INVALID;
+    if (tet < 0 || tet >= c->n_tet) { lymph_set_error("lymph_make_rhs_point: tetrahedron out of range"); return LYMPH_ERR_INVALID; }
+    if (!c->have_matrices) { lymph_set_error("lymph_make_rhs_point: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    int32_t P = 0;
+    LYMPH_CUDA_TRY(cudaMemcpy(&P, c->d_tet_poly + tet, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    double* out = (which == LYMPH_RHS_STAT) ? c->d_rhs_stat : c->d_rhs_dyn;
+    LYMPH_TRY(lymph_dev_point_source(c, P, x0, dir, out));
+    LYMPH_TRY(lymph_sync_status(c, "lymph_make_rhs_point"));
+    if (which == LYMPH_RHS_STAT) c->have_rhs_stat = true; else c->have_rhs_dyn = true;
+    return LYMPH_OK;
+}
+
+int lymph_set_dt(lymph_ctx* c, double dt) {
+    if (!c || !(dt > 0.0) || !std::isfinite(dt)) return LYMPH_ERR_INVALID;
+    c->dt = dt;
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    return LYMPH_OK;
+}
+
+int lymph_get_dt(const lymph_ctx* c, double* dt) {
+    if (!c || !dt) return LYMPH_ERR_INVALID;
+    *dt = c->dt;
+    return LYMPH_OK;
+}
+
+int lymph_max_eigenvalue(lymph_ctx* c, int32_t iters, double* lam) {
+    if (!c || !lam || iters < 1) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_max_eigenvalue: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    const size_t nv = (size_t)c->n_poly * c->nd;
+    std::vector<double> x(nv), y(nv);
+    uint64_t st = 0x243F6A8885A308D3ull;
+    for (size_t i = 0; i < nv; ++i) {
+        st = st * 6364136223846793005ull + 1442695040888963407ull;
+        x[i] = ((double)(st >> 11) / 9007199254740992.0) - 0.5;
+    }
+    double *dx = nullptr, *dy = nullptr;
+    if (cudaMalloc(&dx, nv * sizeof(double)) != cudaSuccess || cudaMalloc(&dy, nv * sizeof(double)) != cudaSuccess) {
+        if (dx) cudaFree(dx);
+        lymph_set_error("lymph_max_eigenvalue: out of memory");
+        return LYMPH_ERR_OOM;
+    }
+    int rc = LYMPH_OK;
+    double est = 0.0;
+    for (int it = 0; it < iters && rc == LYMPH_OK; ++it) {
+        double nx = 0.0;
+        for (double v : x) nx += v * v;
+        nx = std::sqrt(nx);
+        for (double& v : x) v /= nx;
+        if (cudaMemcpyAsync(dx, x.data(), nv * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+        if (rc == LYMPH_OK) rc = lymph_dev_apply(c, dx, dy);
+        if (rc == LYMPH_OK && cudaMemcpyAsync(y.data(), dy, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+        if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+        double ny = 0.0;
+        for (double v : y) ny += v * v;
+        est = std::sqrt(ny);  // |M^-1 K x| with |x| = 1
+        x.swap(y);
+    }
+    cudaFree(dx);
+    cudaFree(dy);
+    LYMPH_TRY(rc);
+    *lam = est;
+    return lymph_sync_status(c, "lymph_max_eigenvalue");
 }
 
 int lymph_launch_count(const lymph_ctx* c, int64_t* count) {

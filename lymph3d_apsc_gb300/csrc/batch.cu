@@ -1,0 +1,412 @@
+// batch.cu -- many independent problems advanced by one persistent launch
+// per time step (no counterpart in the reference, which runs one problem
+// per MPI job).
+//
+// Every problem keeps its own context (operator blocks, mass inverse, RHS,
+// state, degree, dt); the batch flattens all (problem, polyhedron) pairs
+// into one work list.  A persistent grid of CTAs pulls items from an atomic
+// queue and runs the same per-polyhedron body as the single-problem kernel
+// (step_body.cuh) with the degree of the item's problem, so results are
+// bit-identical to stepping each context alone.  A 1-thread kernel after
+// each step advances the step counter (which selects each problem's buffer
+// parity and time-function value) and resets the queue; the loop is launched
+// as CUDA graphs of 16 steps.  The grid size and the item order (largest
+// cost first or problem-major) are picked by a timing autotuner whose choice
+// is cached per batch signature.
+
+#include <algorithm>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "step_body.cuh"
+
+using namespace stepk;
+
+namespace {
+
+constexpr int BATCH_THREADS = 320;   // the p = 4 shape; lower degrees leave lanes idle
+constexpr int BATCH_MINB = 4;
+
+struct BatchProblem {
+    StepArgs a;        // per-problem pointers; u0/un/out are filled per step
+    double* buf[2];
+    int cur0;          // buffer parity of the problem when the run started
+    int p;
+};
+
+template <typename KT> struct BatchSmem {
+    static constexpr size_t b1 = SmemSize<1, KT>::bytes, b2 = SmemSize<2, KT>::bytes, b3 = SmemSize<3, KT>::bytes,
+                            b4 = SmemSize<4, KT>::bytes;
+    static constexpr size_t m12 = b1 > b2 ? b1 : b2, m34 = b3 > b4 ? b3 : b4;
+    static constexpr size_t bytes = m12 > m34 ? m12 : m34;
+};
+
+template <typename KT>
+__global__ void __launch_bounds__(BATCH_THREADS, BATCH_MINB)
+k_step_batch(const BatchProblem* __restrict__ probs, const int2* __restrict__ items, int n_items, int* queue,
+             const int64_t* step_idx, const double* gvals, int64_t g_stride) {
+    __shared__ __align__(16) char smem[BatchSmem<KT>::bytes];
+    __shared__ int s_item;
+    const int64_t k = *step_idx;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const int2 w = items[it];
+        StepArgs A = probs[w.x].a;
+        const int cur = probs[w.x].cur0 ^ (int)(k & 1);
+        A.un = probs[w.x].buf[cur];
+        A.u0 = probs[w.x].buf[cur ^ 1];
+        A.out = probs[w.x].buf[cur ^ 1];
+        A.gvals = gvals + (int64_t)w.x * g_stride;
+        A.step_idx = step_idx;
+        switch (probs[w.x].p) {
+            case 1: step_poly<1, KT, MODE_STEP>(A, w.y, smem); break;
+            case 2: step_poly<2, KT, MODE_STEP>(A, w.y, smem); break;
+            case 3: step_poly<3, KT, MODE_STEP>(A, w.y, smem); break;
+            default: step_poly<4, KT, MODE_STEP>(A, w.y, smem); break;
+        }
+    }
+}
+
+__global__ void k_batch_bump(int64_t* idx, int* queue) {
+    *idx += 1;
+    *queue = 0;
+}
+
+std::string tune_cache_path() {
+    const char* e = std::getenv("LYMPH_TUNE_CACHE");
+    if (e && *e) return e;
+    const char* h = std::getenv("HOME");
+    return std::string(h ? h : "/tmp") + "/.cache/lymph3d_gb300_tune.txt";
+}
+
+std::mutex g_tune_mu;
+
+bool tune_lookup(const std::string& key, int* grid, int* order) {
+    std::lock_guard<std::mutex> l(g_tune_mu);
+    std::ifstream f(tune_cache_path());
+    std::string k;
+    int g, o;
+    while (f >> k >> g >> o)
+        if (k == key) { *grid = g; *order = o; return true; }
+    return false;
+}
+
+void tune_store(const std::string& key, int grid, int order) {
+    std::lock_guard<std::mutex> l(g_tune_mu);
+    std::string path = tune_cache_path();
+    size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        std::string dir = path.substr(0, slash);
+        std::string cmd = "mkdir -p '" + dir + "'";
+        if (std::system(cmd.c_str()) != 0) return;
+    }
+    std::ofstream f(path, std::ios::app);
+    f << key << " " << grid << " " << order << "\n";
+}
+
+}  // namespace
+
+struct lymph_batch {
+    std::vector<lymph_ctx*> ctx;
+    int precision = LYMPH_FP64;
+    cudaStream_t stream = nullptr;
+    BatchProblem* d_probs = nullptr;
+    int2* d_items = nullptr;
+    int n_items = 0;
+    std::vector<int2> items_lpt, items_natural;
+    int order = 0;       // 0 = largest cost first, 1 = problem-major
+    int grid = 0;
+    int* d_queue = nullptr;
+    int64_t* d_step_idx = nullptr;
+    double* d_gvals = nullptr;
+    int64_t gvals_cap = 0;
+    int* d_status = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    int64_t launches = 0;
+    int sms = 0;
+    std::string key;
+};
+
+namespace {
+
+int upload_items(lymph_batch* b) {
+    const std::vector<int2>& v = b->order == 0 ? b->items_lpt : b->items_natural;
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(b->d_items, v.data(), v.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    return LYMPH_OK;
+}
+
+int refresh_problems(lymph_batch* b) {
+    std::vector<BatchProblem> h(b->ctx.size());
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+        lymph_ctx* c = b->ctx[i];
+        BatchProblem& P = h[i];
+        P = BatchProblem();
+        P.a.row_ptr = c->d_row_ptr;
+        P.a.col = c->d_col;
+        P.a.K = c->d_K;
+        P.a.Minv = c->d_Minv;
+        P.a.rhs_stat = c->d_rhs_stat;
+        P.a.rhs_dyn = c->d_rhs_dyn;
+        P.a.partial = nullptr;
+        P.a.dt = c->dt;
+        P.a.status = b->d_status;
+        P.a.n_poly = c->n_poly;
+        P.buf[0] = c->d_buf[0];
+        P.buf[1] = c->d_buf[1];
+        P.cur0 = c->cur;
+        P.p = c->p;
+    }
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(b->d_probs, h.data(), h.size() * sizeof(BatchProblem), cudaMemcpyHostToDevice, b->stream));
+    return LYMPH_OK;
+}
+
+int launch_step(lymph_batch* b, int64_t g_stride) {
+    if (b->precision == LYMPH_MIXED)
+        k_step_batch<float><<<b->grid, BATCH_THREADS, 0, b->stream>>>(b->d_probs, b->d_items, b->n_items, b->d_queue,
+                                                                     b->d_step_idx, b->d_gvals, g_stride);
+    else
+        k_step_batch<double><<<b->grid, BATCH_THREADS, 0, b->stream>>>(b->d_probs, b->d_items, b->n_items, b->d_queue,
+                                                                      b->d_step_idx, b->d_gvals, g_stride);
+    k_batch_bump<<<1, 1, 0, b->stream>>>(b->d_step_idx, b->d_queue);
+    b->launches += 2;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+// Runs n steps with the current grid/order; the time-function values are
+// already on the device with stride g_stride per problem.
+int run_loop(lymph_batch* b, int64_t n, int64_t g_stride, bool use_graph) {
+    LYMPH_TRY(refresh_problems(b));
+    LYMPH_CUDA_TRY(cudaMemsetAsync(b->d_step_idx, 0, sizeof(int64_t), b->stream));
+    LYMPH_CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
+    const int R = 16;
+    int64_t i = 0;
+    if (use_graph && n >= R) {
+        if (b->graph && b->graph_steps != (int)g_stride) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        if (!b->graph) {
+            cudaGraph_t g;
+            LYMPH_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            int64_t l0 = b->launches;
+            for (int j = 0; j < R; ++j) launch_step(b, g_stride);
+            b->launches = l0;
+            cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            if (e != cudaSuccess) { lymph_set_error(std::string("batch graph capture: ") + cudaGetErrorString(e)); return LYMPH_ERR_CUDA; }
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { lymph_set_error(std::string("batch graph instantiate: ") + cudaGetErrorString(e)); return LYMPH_ERR_CUDA; }
+            b->graph_steps = (int)g_stride;
+        }
+        for (; i + R <= n; i += R) {
+            LYMPH_CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
+            b->launches += 2 * R;
+        }
+    }
+    for (; i < n; ++i) LYMPH_TRY(launch_step(b, g_stride));
+    // each problem's buffers flipped n times
+    if (n & 1)
+        for (lymph_ctx* c : b->ctx) c->cur ^= 1;
+    return LYMPH_OK;
+}
+
+int upload_g(lymph_batch* b, const double* g, int64_t n_steps) {
+    int64_t need = (int64_t)b->ctx.size() * n_steps;
+    if (need > b->gvals_cap) {
+        if (b->d_gvals) cudaFree(b->d_gvals);
+        b->d_gvals = nullptr;
+        b->gvals_cap = need;
+        if (cudaMalloc(&b->d_gvals, sizeof(double) * (size_t)need) != cudaSuccess) {
+            lymph_set_error("lymph_batch: cannot allocate the time-function table");
+            return LYMPH_ERR_OOM;
+        }
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    }
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(b->d_gvals, g, sizeof(double) * (size_t)need, cudaMemcpyHostToDevice, b->stream));
+    return LYMPH_OK;
+}
+
+int batch_status(lymph_batch* b, const char* where) {
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int st = 0;
+    LYMPH_CUDA_TRY(cudaMemcpy(&st, b->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) {
+        LYMPH_CUDA_TRY(cudaMemset(b->d_status, 0, sizeof(int)));
+        lymph_set_error(std::string(where) + ": non-finite value in a problem's state");
+        return LYMPH_EXIT_INSTAB;
+    }
+    return LYMPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out) {
+    if (!out || !ctxs || n <= 0) { lymph_set_error("lymph_batch_create: bad argument"); return LYMPH_ERR_INVALID; }
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!ctxs[i]) { lymph_set_error("lymph_batch_create: null context"); return LYMPH_ERR_INVALID; }
+        if (!ctxs[i]->have_matrices) { lymph_set_error("lymph_batch_create: every context needs lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+        if (ctxs[i]->precision != ctxs[0]->precision) { lymph_set_error("lymph_batch_create: mixed precisions in one batch"); return LYMPH_ERR_INVALID; }
+    }
+    lymph_batch* b = new lymph_batch();
+    b->ctx.assign(ctxs, ctxs + n);
+    b->precision = ctxs[0]->precision;
+    auto fail = [&](int rc) { lymph_batch_destroy(b); return rc; };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) { delete b; lymph_set_error("lymph_batch_create: stream"); return LYMPH_ERR_CUDA; }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    // work items and their cost (bytes of blocks streamed)
+    std::vector<std::pair<int64_t, int2>> cost;
+    std::ostringstream key;
+    key << "sm" << b->sms << "_prec" << b->precision;
+    std::map<int, int64_t> per_p;
+    for (int i = 0; i < n; ++i) {
+        lymph_ctx* c = ctxs[i];
+        for (int P = 0; P < c->n_poly; ++P) {
+            int64_t nb = c->h_row_ptr[P + 1] - c->h_row_ptr[P];
+            cost.push_back({nb * (int64_t)c->nd * c->nd, make_int2(i, P)});
+            b->items_natural.push_back(make_int2(i, P));
+        }
+        per_p[c->p] += c->n_blocks;
+    }
+    for (auto& kv : per_p) key << "_p" << kv.first << "b" << kv.second;
+    b->key = key.str();
+    std::stable_sort(cost.begin(), cost.end(), [](const std::pair<int64_t, int2>& x, const std::pair<int64_t, int2>& y) { return x.first > y.first; });
+    for (auto& c : cost) b->items_lpt.push_back(c.second);
+    b->n_items = (int)b->items_natural.size();
+    if (cudaMalloc(&b->d_probs, sizeof(BatchProblem) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_items, sizeof(int2) * b->n_items) != cudaSuccess ||
+        cudaMalloc(&b->d_queue, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_step_idx, sizeof(int64_t)) != cudaSuccess ||
+        cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess) {
+        lymph_set_error("lymph_batch_create: device allocation failed");
+        return fail(LYMPH_ERR_OOM);
+    }
+    cudaMemsetAsync(b->d_status, 0, sizeof(int), b->stream);
+    b->grid = 4 * b->sms;
+    b->order = 0;
+    int g, o;
+    if (tune_lookup(b->key, &g, &o)) { b->grid = g; b->order = o; }
+    int rc = upload_items(b);
+    if (rc) return fail(rc);
+    *out = b;
+    return LYMPH_OK;
+}
+
+int lymph_batch_destroy(lymph_batch* b) {
+    if (!b) return LYMPH_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (void* p : {(void*)b->d_probs, (void*)b->d_items, (void*)b->d_queue, (void*)b->d_step_idx, (void*)b->d_gvals,
+                    (void*)b->d_status})
+        if (p) cudaFree(p);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return LYMPH_OK;
+}
+
+int lymph_batch_run(lymph_batch* b, int64_t n_steps, const double* gvals, float* ms_total) {
+    if (!b || n_steps < 0 || (n_steps > 0 && !gvals)) return LYMPH_ERR_INVALID;
+    if (ms_total) *ms_total = 0.0f;
+    if (n_steps == 0) return LYMPH_OK;
+    for (lymph_ctx* c : b->ctx) cudaStreamSynchronize(c->stream);  // contexts' own work first
+    LYMPH_TRY(upload_g(b, gvals, n_steps));
+    cudaEvent_t e0, e1;
+    LYMPH_CUDA_TRY(cudaEventCreate(&e0));
+    LYMPH_CUDA_TRY(cudaEventCreate(&e1));
+    cudaEventRecord(e0, b->stream);
+    int rc = run_loop(b, n_steps, n_steps, true);
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms_total) *ms_total = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    LYMPH_TRY(rc);
+    return batch_status(b, "lymph_batch_run");
+}
+
+int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache, int32_t* grid, int32_t* order) {
+    if (!b || trial_steps < 1) return LYMPH_ERR_INVALID;
+    int g0, o0;
+    if (use_cache && tune_lookup(b->key, &g0, &o0)) {
+        b->grid = g0;
+        b->order = o0;
+        LYMPH_TRY(upload_items(b));
+    } else {
+        // candidates: persistent grids of 1..4 CTAs per SM, two item orders.
+        // The trial steps advance the real state, so the state is saved and
+        // restored around the trials.
+        std::vector<std::vector<double>> save(b->ctx.size() * 2);
+        for (size_t i = 0; i < b->ctx.size(); ++i) {
+            lymph_ctx* c = b->ctx[i];
+            size_t nv = (size_t)c->n_poly * c->nd;
+            for (int k = 0; k < 2; ++k) {
+                save[2 * i + k].resize(nv);
+                LYMPH_CUDA_TRY(cudaMemcpy(save[2 * i + k].data(), c->d_buf[k], nv * sizeof(double), cudaMemcpyDeviceToHost));
+            }
+        }
+        std::vector<int> curs;
+        for (lymph_ctx* c : b->ctx) curs.push_back(c->cur);
+        std::vector<double> g((size_t)b->ctx.size() * (trial_steps + 1), 0.0);
+        LYMPH_TRY(upload_g(b, g.data(), trial_steps + 1));
+        float best = 1e30f;
+        int bg = b->grid, bo = b->order;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        for (int ord = 0; ord < 2; ++ord)
+            for (int mult = 1; mult <= BATCH_MINB; ++mult) {
+                b->order = ord;
+                b->grid = mult * b->sms;
+                LYMPH_TRY(upload_items(b));
+                LYMPH_TRY(run_loop(b, 1, trial_steps + 1, false));  // warm-up
+                cudaEventRecord(e0, b->stream);
+                LYMPH_TRY(run_loop(b, trial_steps, trial_steps + 1, false));
+                cudaEventRecord(e1, b->stream);
+                cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) { best = ms; bg = b->grid; bo = ord; }
+            }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        for (size_t i = 0; i < b->ctx.size(); ++i) {
+            lymph_ctx* c = b->ctx[i];
+            size_t nv = (size_t)c->n_poly * c->nd;
+            for (int k = 0; k < 2; ++k)
+                LYMPH_CUDA_TRY(cudaMemcpy(c->d_buf[k], save[2 * i + k].data(), nv * sizeof(double), cudaMemcpyHostToDevice));
+            c->cur = curs[i];
+        }
+        LYMPH_CUDA_TRY(cudaMemset(b->d_status, 0, sizeof(int)));
+        b->grid = bg;
+        b->order = bo;
+        LYMPH_TRY(upload_items(b));
+        tune_store(b->key, bg, bo);
+    }
+    if (grid) *grid = b->grid;
+    if (order) *order = b->order;
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    return LYMPH_OK;
+}
+
+int lymph_batch_launch_count(const lymph_batch* b, int64_t* count) {
+    if (!b || !count) return LYMPH_ERR_INVALID;
+    *count = b->launches;
+    return LYMPH_OK;
+}
+
+}  // extern "C"

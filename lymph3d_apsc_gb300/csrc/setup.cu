@@ -590,9 +590,14 @@ __global__ void __launch_bounds__(VEC_THREADS) k_vector(VecArgs A) {
         __syncthreads();
         for (int r = tid; r < ND; r += VEC_THREADS) {
             const int i = r / NP, m = r % NP;
-            double s = 0.0;
+            // RHS: per-tetrahedron integral added to the polyhedron's vector
+            // (MAKE_RHS_VOLUME then the row copy, matrix_free.f90:711-717);
+            // projection: one running integral over all sub-tetrahedra
+            // (uex_integral, matrix_free.f90:960-972)
+            double s = (A.mode == 0) ? 0.0 : s_acc[r];
             for (int q = 0; q < NQ3; ++q) s = s + s_w[q] * s_dat[q * 3 + i] * s_phi[q * NP + m];
-            s_acc[r] += s;
+            if (A.mode == 0) s_acc[r] += s;
+            else s_acc[r] = s;
         }
         if (A.mode != 0) continue;
         // boundary faces of this tetrahedron (only boundary faces are added, :809-819)
@@ -677,6 +682,23 @@ __global__ void __launch_bounds__(VEC_THREADS) k_vector(VecArgs A) {
     for (int r = tid; r < ND; r += VEC_THREADS) A.out[(int64_t)P * ND + r] = s_acc[r] * A.scale;
 }
 
+// Point source: rhs[P][i*Np + m] = dir_i phi_m(x0) for the polyhedron P
+// that contains x0 (one block of Np threads); the rest of rhs was zeroed by
+// the caller.  The spatial part of a Ricker source f = dir delta(x - x0) R(t),
+// whose time part R(t) enters through the time-function values.
+__global__ void k_point_source(int Np, int P, const double* __restrict__ bbox, const RefTables* __restrict__ ref,
+                               double x, double y, double z, double dx, double dy, double dz, double* rhs) {
+    const int m = threadIdx.x;
+    if (m >= Np) return;
+    const double pt[3] = {x, y, z};
+    double ph, dp[3];
+    basis_eval(pt, &bbox[P * 6], &ref->blist[m * 3], &ph, dp);
+    const int64_t base = (int64_t)P * 3 * Np;
+    rhs[base + 0 * Np + m] = dx * ph;
+    rhs[base + 1 * Np + m] = dy * ph;
+    rhs[base + 2 * Np + m] = dz * ph;
+}
+
 template <int PD>
 int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {
     size_t smem = asm_smem<PD>();
@@ -754,6 +776,14 @@ int lymph_dev_cholesky(lymph_ctx* c) {
     k_cholesky<<<grid, 32 * warps_per_block, smem, c->stream>>>(c->n_poly, c->Np, c->d_Mm, c->d_Rm, c->d_RmT, c->d_status);
     k_mass_inverse<<<grid, 32 * warps_per_block, 0, c->stream>>>(c->n_poly, c->Np, c->d_R, c->d_Minv);
     c->launches += 3;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+int lymph_dev_point_source(lymph_ctx* c, int P, const double x0[3], const double dir[3], double* out) {
+    LYMPH_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * (size_t)c->n_poly * c->nd, c->stream));
+    k_point_source<<<1, 64, 0, c->stream>>>(c->Np, P, c->d_bbox, c->d_ref, x0[0], x0[1], x0[2], dir[0], dir[1], dir[2], out);
+    c->launches++;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
 }

@@ -16,152 +16,17 @@
 // S column slices x ND rows, S chosen per degree so that ND*S fills whole
 // warps; the S partial sums of a row are combined in a fixed order.
 
-#include "common.cuh"
+#include "step_body.cuh"
 
 namespace {
 
-template <int P> struct Deg {
-    static constexpr int NP = (P + 1) * (P + 2) * (P + 3) / 6;
-    static constexpr int ND = 3 * NP;
-};
+using namespace stepk;
 
-// Thread shape per degree: S column slices x ND rows (ND*S fills whole warps
-// but for a few lanes), and the CTAs per SM the launch bounds ask for.
-template <int P> struct Shape {
-    static constexpr int ND = Deg<P>::ND;
-    static constexpr int S = P == 1 ? 8 : (P == 2 ? 8 : (P == 3 ? 4 : 3));
-    static constexpr int T = ((ND * S + 31) / 32) * 32;       // 96, 256, 256, 320
-    static constexpr int MINB = P == 1 ? 16 : (P == 4 ? 4 : 6);
-};
-
-constexpr int NBB = 16;   // neighbour blocks staged in shared memory at once
-
-enum { MODE_STEP = 0, MODE_FIRST = 1, MODE_DG = 2 };
-
-struct StepArgs {
-    const int32_t* row_ptr;
-    const int32_t* col;
-    const void* K;             // [n_blocks][ND][ND] column-major (double or float)
-    const double* Minv;        // [n_poly][NP][NP] column-major inverse of M_loc
-    const double* rhs_stat;
-    const double* rhs_dyn;
-    const double* gvals;       // time-function values
-    const int64_t* step_idx;   // index into gvals (device counter)
-    const double* u0;          // u^{n-1} (MODE_STEP), u^0 (MODE_FIRST), u_h (MODE_DG)
-    const double* un;          // u^n (MODE_STEP), v^0 (MODE_FIRST), u_ex (MODE_DG)
-    double* out;               // u^{n+1} (MODE_STEP: may alias u0), u^1 (MODE_FIRST)
-    double* partial;           // MODE_DG: per-polyhedron du . (A du)
-    double dt;
-    int* status;
-    int n_poly;
-};
-
-__device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
-__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
-
-// One CTA per polyhedron.  The block row of P is one contiguous column-major
-// [ND x nb*ND] matrix (its blocks are adjacent in memory), multiplied by the
-// gathered coefficients of the column polyhedra.  The mass-matrix inverse is
-// applied in FP64 as a dense Np x Np product per component (precomputed from
-// the Cholesky factor), which replaces the reference's two triangular solves
-// per component with a parallel product of the same value.
+// One CTA per polyhedron.
 template <int PD, typename KT, int MODE>
 __global__ void __launch_bounds__(Shape<PD>::T, Shape<PD>::MINB) k_step(StepArgs A) {
-    constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND, S = Shape<PD>::S, T = Shape<PD>::T;
-    constexpr int CPT = (ND + S - 1) / S;
-    using AT = KT;  // FP64 blocks accumulate in FP64, FP32 blocks in FP32
-    __shared__ AT s_u[NBB * ND];
-    __shared__ AT s_red[S * ND];
-    __shared__ double s_b[ND];
-
-    const int P = blockIdx.x;
-    const int tid = threadIdx.x;
-    const int r = tid % ND, s = tid / ND;
-    const bool act = tid < ND * S;
-    const int rb = A.row_ptr[P], re = A.row_ptr[P + 1];
-    const KT* Kbase = (const KT*)A.K;
-
-    AT acc0 = 0, acc1 = 0;
-    for (int b0 = rb; b0 < re; b0 += NBB) {
-        const int nb = (re - b0) < NBB ? (re - b0) : NBB;
-        __syncthreads();
-        for (int i = tid; i < nb * ND; i += T) {
-            const int bb = i / ND, c = i % ND;
-            const int64_t q = (int64_t)A.col[b0 + bb] * ND + c;
-            double v;
-            if (MODE == MODE_STEP) v = A.un[q];
-            else if (MODE == MODE_FIRST) v = A.u0[q];
-            else v = A.u0[q] - A.un[q];
-            s_u[i] = (AT)v;
-        }
-        __syncthreads();
-        if (act) {
-            for (int bb = 0; bb < nb; ++bb) {
-                const KT* Kb = Kbase + (int64_t)(b0 + bb) * ND * ND + r;
-                const AT* ub = s_u + bb * ND;
-                KT kv[CPT];
-#pragma unroll
-                for (int j = 0; j < CPT; ++j) {
-                    const int c = s + j * S;
-                    kv[j] = (c < ND) ? ld_stream(Kb + (int64_t)c * ND) : (KT)0;
-                }
-#pragma unroll
-                for (int j = 0; j < CPT; ++j) {
-                    const int c = s + j * S;
-                    if (c < ND) {
-                        if (j & 1) acc1 += (AT)kv[j] * ub[c];
-                        else acc0 += (AT)kv[j] * ub[c];
-                    }
-                }
-            }
-        }
-    }
-    if (act) s_red[s * ND + r] = acc0 + acc1;
-    __syncthreads();
-    if (MODE == MODE_DG) {
-        if (tid == 0) {
-            double e = 0.0;
-            for (int rr = 0; rr < ND; ++rr) {
-                double y = 0.0;
-                for (int ss = 0; ss < S; ++ss) y += (double)s_red[ss * ND + rr];
-                const int64_t q = (int64_t)P * ND + rr;
-                e = e + (A.u0[q] - A.un[q]) * y;
-            }
-            A.partial[P] = e;
-        }
-        return;
-    }
-    const double g = A.gvals[*A.step_idx];
-    if (tid < ND) {
-        double y = 0.0;
-        for (int ss = 0; ss < S; ++ss) y += (double)s_red[ss * ND + tid];
-        const int64_t q = (int64_t)P * ND + tid;
-        s_b[tid] = -y + A.rhs_stat[q] + A.rhs_dyn[q] * g;
-    }
-    __syncthreads();
-    if (tid < ND) {
-        const int i = tid / NP, m = tid % NP;
-        const double* Mi = A.Minv + (int64_t)P * NP * NP + m;
-        const double* bi = s_b + i * NP;
-        double x0 = 0.0, x1 = 0.0;
-#pragma unroll
-        for (int c = 0; c < NP; c += 2) {
-            x0 += Mi[c * NP] * bi[c];
-            if (c + 1 < NP) x1 += Mi[(c + 1) * NP] * bi[c + 1];
-        }
-        const double x = x0 + x1;
-        const int64_t q = (int64_t)P * ND + tid;
-        double v;
-        if (MODE == MODE_STEP) {
-            const double dt2 = A.dt * A.dt;
-            v = dt2 * x + 2.0 * A.un[q] - A.u0[q];
-        } else {
-            const double half_dt2 = 0.5 * (A.dt * A.dt);
-            v = half_dt2 * x + A.u0[q] + A.dt * A.un[q];
-        }
-        if (!isfinite(v)) atomicOr(A.status, ST_NONFINITE);
-        A.out[q] = v;
-    }
+    __shared__ __align__(16) char smem[SmemSize<PD, KT>::bytes];
+    step_poly<PD, KT, MODE>(A, blockIdx.x, smem);
 }
 
 __global__ void k_bump(int64_t* idx) { *idx += 1; }
@@ -258,6 +123,15 @@ int lymph_dev_bump(lymph_ctx* c) {
     k_bump<<<1, 1, 0, c->stream>>>(c->d_step_idx);
     c->launches++;
     return LYMPH_OK;
+}
+
+// out = M^-1 K u (u read from `u`), for the power iteration of the CFL bound.
+int lymph_dev_apply(lymph_ctx* c, const double* u, double* out) {
+    StepArgs A = base_args(c);
+    A.un = u;
+    A.u0 = u;
+    A.out = out;
+    return launch_step_mode<MODE_APPLY>(c, A, c->precision == LYMPH_MIXED);
 }
 
 int lymph_dev_first_step(lymph_ctx* c) {

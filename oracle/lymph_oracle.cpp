@@ -60,6 +60,11 @@ int g_perturb_ulps = 0;
 // The spread between the two orders is the algorithm's own rounding floor.
 int g_reverse_sums = 0;
 
+// Third instrument: when set, the time steps apply M^-1 as an explicit
+// inverse (columns solved once with solve_LU) instead of the two triangular
+// solves, the way the device kernel applies it.
+int g_explicit_inverse = 0;
+
 double perturb(double v, const double p[3], int comp) {
     if (g_perturb_ulps == 0 || v == 0.0) return v;
     uint64_t h = 1469598103934665603ull ^ (uint64_t)comp;
@@ -977,6 +982,21 @@ void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, in
     }
     for (int r = 0; r < nd; ++r) tmp[r] = -tmp[r] + o.rhs_stat[(size_t)P * nd + r] + o.rhs_dyn[(size_t)P * nd + r] * g;
     out.assign(nd, 0.0);
+    if (g_explicit_inverse) {
+        std::vector<double> inv((size_t)Np * Np), e(Np), col(Np);
+        for (int k = 0; k < Np; ++k) {
+            for (int m = 0; m < Np; ++m) e[m] = (m == k) ? 1.0 : 0.0;
+            solve_LU_RT_R(&o.R[(size_t)P * Np * Np], e.data(), Np, col.data());
+            for (int m = 0; m < Np; ++m) inv[(size_t)m * Np + k] = col[m];
+        }
+        for (int i = 0; i < 3; ++i)
+            for (int m = 0; m < Np; ++m) {
+                double x = 0.0;
+                for (int c = 0; c < Np; ++c) x = x + inv[(size_t)m * Np + c] * tmp[i * Np + c];
+                out[i * Np + m] = x;
+            }
+        return;
+    }
     for (int i = 0; i < 3; ++i) {
         for (int m = 0; m < Np; ++m) v[m] = tmp[i * Np + m];
         solve_LU_RT_R(&o.R[(size_t)P * Np * Np], v.data(), Np, x.data());
@@ -996,6 +1016,8 @@ const char* oracle_last_error(void) { return g_err.c_str(); }
 void oracle_set_data_perturbation(int ulps) { g_perturb_ulps = ulps; }
 
 void oracle_set_reverse_sums(int on) { g_reverse_sums = on; }
+
+void oracle_set_explicit_inverse(int on) { g_explicit_inverse = on; }
 
 int oracle_num_threads(void) {
 #ifdef _OPENMP
