@@ -204,6 +204,25 @@ int lymph_error_l2(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
  * blocks into a temporary device buffer for the duration of the call. */
 int lymph_error_dg(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
 
+/* L2 error without any device allocation.  No counterpart in the reference:
+ * it is the body of COMPUTE_ERROR_L2_MATRIX_FREE for callers that cannot
+ * allocate device memory when they need the norm (a driver that gives all
+ * device memory to its own pool, a process already at its device-memory cap,
+ * a loop that must not take the synchronisation a cudaMalloc/cudaFree can
+ * cause).  The caller passes device pointers to its own data:
+ * d_mass_modal [n_poly][Np][Np] row-major (M_modal_loc), d_uh and d_uex
+ * [n_poly][3Np]; the sum of squares is written to the host pointer sumsq.
+ * The partial sums live in a static device array of 262,144 + 1 doubles
+ * (2 MiB) that every GPU loading the library holds until the process exits;
+ * n_poly above 262,144 is rejected with LYMPH_ERR_INVALID.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  Kernels run on the legacy
+ * default stream and the result is copied back synchronously.  All calls
+ * share the one array: calls that overlap on the GPU (from several host
+ * threads, or concurrently with other work on the same device array) race. */
+int lymph_error_l2_noalloc(const double* d_mass_modal, const double* d_uh, const double* d_uex, int32_t n_poly,
+                           int32_t Np, double* sumsq);
+
 /* Aliases with the names the project specification uses for the two error
  * routines (COMPUTE_ERROR_L2_FREE / COMPUTE_ERROR_DG_FREE). */
 int lymph_compute_error_l2_free(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);

@@ -87,6 +87,7 @@ _SIGS = {
     "lymph_set_state": (c_int, [c_void_p, c_int, P_F64, c_int]),
     "lymph_error_l2": (c_int, [c_void_p, c_int, c_int, P_F64]),
     "lymph_error_dg": (c_int, [c_void_p, c_int, c_int, P_F64]),
+    "lymph_error_l2_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, P_F64]),
     "lymph_compute_error_l2_free": (c_int, [c_void_p, c_int, c_int, P_F64]),
     "lymph_compute_error_dg_free": (c_int, [c_void_p, c_int, c_int, P_F64]),
     "lymph_get_pattern": (c_int, [c_void_p, P_I32, P_I32]),
