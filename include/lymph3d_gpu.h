@@ -178,6 +178,12 @@ int lymph_first_step(lymph_ctx* ctx, double t);
  * gathered on the device. */
 int lymph_step(lymph_ctx* ctx, double t);
 
+/* The two steps above with the time-function value g supplied by the caller
+ * instead of sin(sqrt(2) pi t) (problem_data_and_properties.f90:14-23), for
+ * sources with another time dependence (e.g. a Ricker wavelet). */
+int lymph_first_step_g(lymph_ctx* ctx, double g);
+int lymph_step_g(lymph_ctx* ctx, double g);
+
 /* The time loop of src/Lymph3D.f90:389-418: while (*t_inout <= stop_time)
  * { step(*t_inout); *t_inout += dt; }, at most max_steps steps
  * (max_steps < 0: no cap).  The time function values are computed on the

@@ -81,6 +81,8 @@ _SIGS = {
     "lymph_modal_project": (c_int, [c_void_p, c_int, c_int, c_double]),
     "lymph_first_step": (c_int, [c_void_p, c_double]),
     "lymph_step": (c_int, [c_void_p, c_double]),
+    "lymph_first_step_g": (c_int, [c_void_p, c_double]),
+    "lymph_step_g": (c_int, [c_void_p, c_double]),
     "lymph_run_steps": (c_int, [c_void_p, c_double, c_int64, P_F64, POINTER(c_int64), POINTER(c_float),
                                 POINTER(c_float)]),
     "lymph_get_state": (c_int, [c_void_p, c_int, P_F64, c_int]),

@@ -24,6 +24,7 @@ int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double s
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
 int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);
+int lymph_dev_power_iteration(lymph_ctx* c, double* x, double* y, double* d_ss, int iters);
 int lymph_dev_point_source(lymph_ctx* c, int P, const double x0[3], const double dir[3], double* out);
 int lymph_dev_bump(lymph_ctx* c);
 int lymph_dev_error_dg(lymph_ctx* c, const void* blocks, const double* uh, const double* uex, double* d_out);
@@ -417,6 +418,23 @@ int lymph_step(lymph_ctx* c, double t) {
     return lymph_sync_status(c, "lymph_step");
 }
 
+int lymph_first_step_g(lymph_ctx* c, double g) {
+    if (!c || !std::isfinite(g)) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_first_step_g: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    LYMPH_TRY(set_g(c, g));
+    LYMPH_TRY(lymph_dev_first_step(c));
+    return lymph_sync_status(c, "lymph_first_step_g");
+}
+
+int lymph_step_g(lymph_ctx* c, double g) {
+    if (!c || !std::isfinite(g)) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_step_g: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    LYMPH_TRY(set_g(c, g));
+    LYMPH_TRY(lymph_dev_step(c, false));
+    c->cur ^= 1;
+    return lymph_sync_status(c, "lymph_step_g");
+}
+
 int lymph_run_steps(lymph_ctx* c, double stop_time, int64_t max_steps, double* t_inout, int64_t* n_done,
                     float* ms_total, float* ms_kernel) {
     if (!c || !t_inout) return LYMPH_ERR_INVALID;
@@ -680,8 +698,8 @@ int lymph_max_eigenvalue(lymph_ctx* c, int32_t iters, double* lam) {
     if (!c || !lam || iters < 1) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_max_eigenvalue: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
     const size_t nv = (size_t)c->n_poly * c->nd;
-    std::vector<double> x(nv), y(nv);
-    uint64_t st = 0x243F6A8885A308D3ull;
+    std::vector<double> x(nv);
+    uint64_t st = 0x243F6A8885A308D3ull;  // fixed pseudo-random start vector
     for (size_t i = 0; i < nv; ++i) {
         st = st * 6364136223846793005ull + 1442695040888963407ull;
         x[i] = ((double)(st >> 11) / 9007199254740992.0) - 0.5;
@@ -693,25 +711,16 @@ int lymph_max_eigenvalue(lymph_ctx* c, int32_t iters, double* lam) {
         return LYMPH_ERR_OOM;
     }
     int rc = LYMPH_OK;
-    double est = 0.0;
-    for (int it = 0; it < iters && rc == LYMPH_OK; ++it) {
-        double nx = 0.0;
-        for (double v : x) nx += v * v;
-        nx = std::sqrt(nx);
-        for (double& v : x) v /= nx;
-        if (cudaMemcpyAsync(dx, x.data(), nv * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
-        if (rc == LYMPH_OK) rc = lymph_dev_apply(c, dx, dy);
-        if (rc == LYMPH_OK && cudaMemcpyAsync(y.data(), dy, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
-        if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
-        double ny = 0.0;
-        for (double v : y) ny += v * v;
-        est = std::sqrt(ny);  // |M^-1 K x| with |x| = 1
-        x.swap(y);
-    }
+    if (cudaMemcpyAsync(dx, x.data(), nv * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+    if (rc == LYMPH_OK) rc = lymph_dev_power_iteration(c, dx, dy, c->d_scalar, iters);
+    double ss = 0.0;
+    if (rc == LYMPH_OK && cudaMemcpyAsync(&ss, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+        rc = LYMPH_ERR_CUDA;
+    cudaStreamSynchronize(c->stream);
     cudaFree(dx);
     cudaFree(dy);
     LYMPH_TRY(rc);
-    *lam = est;
+    *lam = std::sqrt(ss);  // |M^-1 K x| with |x| = 1
     return lymph_sync_status(c, "lymph_max_eigenvalue");
 }
 

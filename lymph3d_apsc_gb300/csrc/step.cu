@@ -70,6 +70,27 @@ __global__ void k_sum(int64_t n, const double* __restrict__ v, double* out) {
     if (threadIdx.x == 0) *out = red[0];
 }
 
+// Sum of squares of v into *out (one CTA, fixed order).
+__global__ void k_sumsq(int64_t n, const double* __restrict__ v, double* out) {
+    __shared__ double red[1024];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += v[i] * v[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+// x = y / sqrt(*ss)
+__global__ void k_normalize(int64_t n, const double* __restrict__ y, const double* __restrict__ ss, double* x) {
+    const double inv = 1.0 / sqrt(*ss);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = y[i] * inv;
+}
+
 template <int PD, typename KT, int MODE>
 int launch_step_t(lymph_ctx* c, const StepArgs& A) {
     k_step<PD, KT, MODE><<<c->n_poly, Shape<PD>::T, 0, c->stream>>>(A);
@@ -132,6 +153,27 @@ int lymph_dev_apply(lymph_ctx* c, const double* u, double* out) {
     A.u0 = u;
     A.out = out;
     return launch_step_mode<MODE_APPLY>(c, A, c->precision == LYMPH_MIXED);
+}
+
+// `iters` power iterations x <- M^-1 K x / |M^-1 K x| entirely on the
+// device; x must hold a nonzero start vector, y is scratch; *d_ss receives
+// |M^-1 K x|^2 of the last iteration (x normalised before it).
+int lymph_dev_power_iteration(lymph_ctx* c, double* x, double* y, double* d_ss, int iters) {
+    const int64_t n = (int64_t)c->n_poly * c->nd;
+    k_sumsq<<<1, 1024, 0, c->stream>>>(n, x, d_ss);
+    k_normalize<<<1024, 256, 0, c->stream>>>(n, x, d_ss, x);
+    c->launches += 2;
+    for (int it = 0; it < iters; ++it) {
+        LYMPH_TRY(lymph_dev_apply(c, x, y));
+        k_sumsq<<<1, 1024, 0, c->stream>>>(n, y, d_ss);
+        c->launches++;
+        if (it + 1 < iters) {
+            k_normalize<<<1024, 256, 0, c->stream>>>(n, y, d_ss, x);
+            c->launches++;
+        }
+    }
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
 }
 
 int lymph_dev_first_step(lymph_ctx* c) {
