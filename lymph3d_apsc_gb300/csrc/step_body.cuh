@@ -47,9 +47,14 @@ struct StepArgs {
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 
+// Shared-memory layout of one polyhedron's step: the gathered coefficients
+// and the row partial sums in the accumulation type, then the FP64 right-hand
+// side at an offset rounded up to 16 bytes (with FP32 blocks and odd ND the
+// raw offset is not 8-byte aligned).
 template <int PD, typename KT> struct SmemSize {
     static constexpr int ND = Deg<PD>::ND, S = Shape<PD>::S;
-    static constexpr size_t bytes = sizeof(KT) * (NBB * ND + S * ND) + sizeof(double) * ND;
+    static constexpr size_t b_offset = ((sizeof(KT) * (size_t)(NBB * ND + S * ND)) + 15) & ~(size_t)15;
+    static constexpr size_t bytes = b_offset + sizeof(double) * ND;
 };
 
 // The block row of polyhedron P is one contiguous column-major
@@ -67,7 +72,8 @@ __device__ __forceinline__ void step_poly(const StepArgs& A, int P, char* smem) 
     using AT = KT;  // FP64 blocks accumulate in FP64, FP32 blocks in FP32
     AT* s_u = (AT*)smem;
     AT* s_red = s_u + NBB * ND;
-    double* s_b = (double*)(s_red + S * ND);
+    double* s_b = (double*)(smem + SmemSize<PD, KT>::b_offset);
+    static_assert(SmemSize<PD, KT>::b_offset % 16 == 0, "FP64 rhs must be 16-byte aligned");
     const int nthr = blockDim.x;
     const int tid = threadIdx.x;
     const int r = tid % ND, s = tid / ND;
