@@ -195,6 +195,9 @@ int lymph_step_g(lymph_ctx* ctx, double g);
 int lymph_run_steps(lymph_ctx* ctx, double stop_time, int64_t max_steps, double* t_inout,
                     int64_t* n_done, float* ms_total, float* ms_kernel);
 
+/* Device-to-device copy between two state slots. */
+int lymph_copy_state(lymph_ctx* ctx, int dst_slot, int src_slot);
+
 /* Copies a state slot to / from host memory in the given layout. */
 int lymph_get_state(lymph_ctx* ctx, int slot, double* host, int layout);
 int lymph_set_state(lymph_ctx* ctx, int slot, const double* host, int layout);
@@ -228,6 +231,58 @@ int lymph_error_dg(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
  * threads, or concurrently with other work on the same device array) race. */
 int lymph_error_l2_noalloc(const double* d_mass_modal, const double* d_uh, const double* d_uex, int32_t n_poly,
                            int32_t Np, double* sumsq);
+
+/* Discrete energy of the leapfrog pair (u^a = slot_a, u^b = slot_b, one step
+ * apart): E = 1/2 |(u^b - u^a)/dt|^2_M + 1/2 u^b . K u^a, the quantity the
+ * scheme conserves without forcing when K is symmetric (SIPG, lambda = mu).
+ * No counterpart in the reference; the learned surrogate's acceptance check. */
+int lymph_energy(lymph_ctx* ctx, int slot_a, int slot_b, double* energy);
+
+/* ---- learned surrogate network (no counterpart in the reference) -------
+ * A per-polyhedron message-passing network, trained and evaluated by this
+ * library's own CUDA kernels (BF16 weight copies, FP32 activations and
+ * accumulation, FP32 Adam masters):
+ *   h = relu(x W0 + b0);  L times: m = relu(h Wm + bm), a = W m,
+ *   h += relu([h a g] Wu + bu);  y = h Wo + bo
+ * W is a row-normalised face-area weight matrix (CSR), g the aggregated
+ * shared-face geometry.  Parameters travel as one FP32 array in the order
+ * W0 b0 (Wm bm Wu bu)xL Wo bo, matrices row-major [in x out]. */
+typedef struct lymph_mpnn lymph_mpnn;
+int lymph_mpnn_create(int32_t F, int32_t H, int32_t O, int32_t L, int32_t G, lymph_mpnn** out);
+int lymph_mpnn_destroy(lymph_mpnn* net);
+int64_t lymph_mpnn_num_params(const lymph_mpnn* net);
+int lymph_mpnn_set_params(lymph_mpnn* net, const float* params);
+int lymph_mpnn_get_params(lymph_mpnn* net, float* params, float* grads);
+int lymph_mpnn_set_graph(lymph_mpnn* net, int32_t n_nodes, const int32_t* w_ptr, const int32_t* w_idx,
+                         const float* w_val, const float* g);
+int lymph_mpnn_forward(lymph_mpnn* net, const float* x, float* y);
+int lymph_mpnn_loss_grad(lymph_mpnn* net, const float* x, const float* target, double* loss);
+int lymph_mpnn_adam(lymph_mpnn* net, float lr, float beta1, float beta2, float eps);
+int lymph_mpnn_launch_count(const lymph_mpnn* net, int64_t* count);
+
+/* One surrogate block: with V0 = u^{n-1}, U0 = u^n, UN = u^{n+1} in the
+ * context, predicts u^{n+1+k} for k = K-3, K-2, K-1 as the
+ * constant-second-difference extrapolation u1 + k d1 + k(k+1)/2 d2
+ * (d1 = u1 - u0, d2 = u1 - 2u0 + um) plus the network's correction
+ * sc (y3 phi3(k) + y4 phi4(k)) in the Newton basis phi3 = k(k+1)(k+2)/K^3,
+ * phi4 = phi3 (k+3)/K, sc = (s3^2/s2) K^3/6 with s1..s3 the RMS of u1, d1,
+ * d2 (use_net = 0: the extrapolation alone).  The features [u1/s1, d1/s2,
+ * d2/s3, log10 s2/s1, log10 s3/s2, lambda, mu, rho] are built on the device;
+ * the network's O = 2 * 3Np outputs are [y3 | y4].  Afterwards V0 and UEX
+ * hold u^n, u^{n+1} (for a fallback), U0 and UN the predicted u^{n+K-2},
+ * u^{n+K-1}, and the network object the predicted u^{n+K}.  K >= 4.
+ * scales (nullable) receives s1, s2, s3. */
+int lymph_surrogate_predict(lymph_ctx* ctx, lymph_mpnn* net, int32_t K, int32_t use_net, double* scales);
+
+/* After one plain step from the predicted pair (U0 = u^{n+K-1}, UN = the
+ * stepped u^{n+K}): residual = |UN - predicted u^{n+K}| / |UN|. */
+int lymph_surrogate_residual(lymph_ctx* ctx, lymph_mpnn* net, double* residual);
+
+/* Judge of a block on the device.  phase 0 keeps the pair (U0, UN) in the
+ * network's scratch; phase 1, after the block was redone plainly, returns
+ * rel = |(U0, UN) - kept| / |(U0, UN)|.  Phase 1 must precede the next
+ * lymph_surrogate_predict (they share the scratch). */
+int lymph_surrogate_judge(lymph_ctx* ctx, lymph_mpnn* net, int32_t phase, double* rel);
 
 /* Aliases with the names the project specification uses for the two error
  * routines (COMPUTE_ERROR_L2_FREE / COMPUTE_ERROR_DG_FREE). */

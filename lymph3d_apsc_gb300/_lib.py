@@ -87,6 +87,7 @@ _SIGS = {
                                 POINTER(c_float)]),
     "lymph_get_state": (c_int, [c_void_p, c_int, P_F64, c_int]),
     "lymph_set_state": (c_int, [c_void_p, c_int, P_F64, c_int]),
+    "lymph_copy_state": (c_int, [c_void_p, c_int, c_int]),
     "lymph_error_l2": (c_int, [c_void_p, c_int, c_int, P_F64]),
     "lymph_error_dg": (c_int, [c_void_p, c_int, c_int, P_F64]),
     "lymph_error_l2_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_int32, P_F64]),
@@ -106,6 +107,20 @@ _SIGS = {
     "lymph_batch_run": (c_int, [c_void_p, c_int64, P_F64, POINTER(c_float)]),
     "lymph_batch_autotune": (c_int, [c_void_p, c_int32, c_int32, P_I32, P_I32]),
     "lymph_batch_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
+    "lymph_energy": (c_int, [c_void_p, c_int, c_int, P_F64]),
+    "lymph_mpnn_create": (c_int, [c_int32, c_int32, c_int32, c_int32, c_int32, POINTER(c_void_p)]),
+    "lymph_mpnn_destroy": (c_int, [c_void_p]),
+    "lymph_mpnn_num_params": (c_int64, [c_void_p]),
+    "lymph_mpnn_set_params": (c_int, [c_void_p, POINTER(c_float)]),
+    "lymph_mpnn_get_params": (c_int, [c_void_p, POINTER(c_float), POINTER(c_float)]),
+    "lymph_mpnn_set_graph": (c_int, [c_void_p, c_int32, P_I32, P_I32, POINTER(c_float), POINTER(c_float)]),
+    "lymph_mpnn_forward": (c_int, [c_void_p, POINTER(c_float), POINTER(c_float)]),
+    "lymph_mpnn_loss_grad": (c_int, [c_void_p, POINTER(c_float), POINTER(c_float), P_F64]),
+    "lymph_mpnn_adam": (c_int, [c_void_p, c_float, c_float, c_float, c_float]),
+    "lymph_mpnn_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
+    "lymph_surrogate_predict": (c_int, [c_void_p, c_void_p, c_int32, c_int32, P_F64]),
+    "lymph_surrogate_residual": (c_int, [c_void_p, c_void_p, P_F64]),
+    "lymph_surrogate_judge": (c_int, [c_void_p, c_void_p, c_int32, P_F64]),
     "lymph_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_device_bytes": (c_int, [c_void_p, POINTER(c_int64)]),
     # mesh utilities (lymph3d_mesh.h)

@@ -29,6 +29,7 @@ int lymph_dev_point_source(lymph_ctx* c, int P, const double x0[3], const double
 int lymph_dev_bump(lymph_ctx* c);
 int lymph_dev_error_dg(lymph_ctx* c, const void* blocks, const double* uh, const double* uex, double* d_out);
 int lymph_dev_error_l2(lymph_ctx* c, const double* uh, const double* uex, double* d_out);
+int lymph_dev_energy(lymph_ctx* c, const double* ua, const double* ub, double* d_out);
 
 namespace {
 
@@ -571,6 +572,15 @@ int lymph_set_state(lymph_ctx* c, int slot, const double* host, int layout) {
     return LYMPH_OK;
 }
 
+int lymph_copy_state(lymph_ctx* c, int dst, int src) {
+    if (!c || !valid_slot(dst) || !valid_slot(src)) return LYMPH_ERR_INVALID;
+    if (dst == src) return LYMPH_OK;
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(lymph_slot_ptr(c, dst), lymph_slot_ptr(c, src), sizeof(double) * (size_t)c->n_poly * c->nd,
+                                   cudaMemcpyDeviceToDevice, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return LYMPH_OK;
+}
+
 int lymph_error_l2(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) {
     if (!c || !sumsq || !valid_slot(s_uh) || !valid_slot(s_uex)) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_error_l2: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
@@ -596,6 +606,17 @@ int lymph_error_dg(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) {
     cudaFree(A);
     LYMPH_TRY(rc);
     return lymph_sync_status(c, "lymph_error_dg");
+}
+
+int lymph_energy(lymph_ctx* c, int slot_a, int slot_b, double* energy) {
+    if (!c || !energy || !valid_slot(slot_a) || !valid_slot(slot_b)) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_energy: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    LYMPH_TRY(lymph_dev_energy(c, lymph_slot_ptr(c, slot_a), lymph_slot_ptr(c, slot_b), c->d_scalar));
+    double t[2];
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(t, c->d_scalar, sizeof(t), cudaMemcpyDeviceToHost, c->stream));
+    LYMPH_TRY(lymph_sync_status(c, "lymph_energy"));
+    *energy = 0.5 * t[0] / (c->dt * c->dt) + 0.5 * t[1];
+    return LYMPH_OK;
 }
 
 int lymph_compute_error_l2_free(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) { return lymph_error_l2(c, s_uh, s_uex, sumsq); }

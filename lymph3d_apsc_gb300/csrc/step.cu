@@ -197,6 +197,21 @@ int lymph_dev_error_dg(lymph_ctx* c, const void* blocks, const double* uh, const
     return LYMPH_OK;
 }
 
+// Leapfrog energy terms: d_out[0] = |ub - ua|^2_M (rho-weighted mass),
+// d_out[1] = ub . K ua.
+int lymph_dev_energy(lymph_ctx* c, const double* ua, const double* ub, double* d_out) {
+    k_l2_partial<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->Np, c->d_M, ub, ua, c->d_partial);
+    k_sum<<<1, 1024, 0, c->stream>>>(c->n_poly, c->d_partial, d_out);
+    StepArgs A = base_args(c);
+    A.u0 = ua;
+    A.un = ub;
+    LYMPH_TRY(launch_step_mode<MODE_BILIN>(c, A, c->precision == LYMPH_MIXED));
+    k_sum<<<1, 1024, 0, c->stream>>>(c->n_poly, c->d_partial, d_out + 1);
+    c->launches += 3;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
 int lymph_dev_error_l2(lymph_ctx* c, const double* uh, const double* uex, double* d_out) {
     k_l2_partial<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->Np, c->d_Mm, uh, uex, c->d_partial);
     k_sum<<<1, 1024, 0, c->stream>>>(c->n_poly, c->d_partial, d_out);

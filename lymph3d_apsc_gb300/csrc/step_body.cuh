@@ -24,7 +24,8 @@ template <int P> struct Shape {
 constexpr int NBB = 16;   // neighbour blocks staged in shared memory at once
 
 // MODE_APPLY: out = M^-1 K u (power iteration for the CFL bound)
-enum { MODE_STEP = 0, MODE_FIRST = 1, MODE_DG = 2, MODE_APPLY = 3 };
+// MODE_BILIN: partial[P] = un_P . (K u0)_P (the bilinear form of the leapfrog energy)
+enum { MODE_STEP = 0, MODE_FIRST = 1, MODE_DG = 2, MODE_APPLY = 3, MODE_BILIN = 4 };
 
 struct StepArgs {
     const int32_t* row_ptr;
@@ -90,7 +91,7 @@ __device__ __forceinline__ void step_poly(const StepArgs& A, int P, char* smem) 
             const int64_t q = (int64_t)A.col[b0 + bb] * ND + c;
             double v;
             if (MODE == MODE_STEP || MODE == MODE_APPLY) v = A.un[q];
-            else if (MODE == MODE_FIRST) v = A.u0[q];
+            else if (MODE == MODE_FIRST || MODE == MODE_BILIN) v = A.u0[q];
             else v = A.u0[q] - A.un[q];
             s_u[i] = (AT)v;
         }
@@ -118,14 +119,14 @@ __device__ __forceinline__ void step_poly(const StepArgs& A, int P, char* smem) 
     }
     if (act) s_red[s * ND + r] = acc0 + acc1;
     __syncthreads();
-    if (MODE == MODE_DG) {
+    if (MODE == MODE_DG || MODE == MODE_BILIN) {
         if (tid == 0) {
             double e = 0.0;
             for (int rr = 0; rr < ND; ++rr) {
                 double y = 0.0;
                 for (int ss = 0; ss < S; ++ss) y += (double)s_red[ss * ND + rr];
                 const int64_t q = (int64_t)P * ND + rr;
-                e = e + (A.u0[q] - A.un[q]) * y;
+                e = e + (MODE == MODE_DG ? (A.u0[q] - A.un[q]) : A.un[q]) * y;
             }
             A.partial[P] = e;
         }

@@ -56,7 +56,8 @@ thread_local std::string g_err;
 int g_perturb_ulps = 0;
 
 // Second instrument: when set, the operator apply of the time steps sums the
-// blocks of a row and the entries of every row dot product in reverse order.
+// blocks of a row and the entries of every row dot product in reverse order,
+// with fused multiply-adds.
 // The spread between the two orders is the algorithm's own rounding floor.
 int g_reverse_sums = 0;
 
@@ -973,8 +974,8 @@ void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, in
         const double* uq = &u[(size_t)Qp * nd];
         for (int r = 0; r < nd; ++r) {
             double s = 0.0;  // matmul row r
-            if (g_reverse_sums)
-                for (int c = nd - 1; c >= 0; --c) s = s + Kb[r * nd + c] * uq[c];
+            if (g_reverse_sums)  // the floor variant also contracts to FMA, as the device does
+                for (int c = nd - 1; c >= 0; --c) s = std::fma(Kb[r * nd + c], uq[c], s);
             else
                 for (int c = 0; c < nd; ++c) s = s + Kb[r * nd + c] * uq[c];
             tmp[r] = tmp[r] + s;
@@ -992,7 +993,7 @@ void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, in
         for (int i = 0; i < 3; ++i)
             for (int m = 0; m < Np; ++m) {
                 double x = 0.0;
-                for (int c = 0; c < Np; ++c) x = x + inv[(size_t)m * Np + c] * tmp[i * Np + c];
+                for (int c = 0; c < Np; ++c) x = std::fma(inv[(size_t)m * Np + c], tmp[i * Np + c], x);
                 out[i * Np + m] = x;
             }
         return;

@@ -1,0 +1,144 @@
+"""CPU FP64 reference of the learned surrogate's network (TEST INFRASTRUCTURE).
+
+Used by tests/ as the checker of the CUDA forward/backward kernels
+(lymph3d_apsc_gb300/csrc/mpnn.cu); the product never imports it.  The
+reference code has no learned component, so this restates the network the
+CUDA kernels implement, in plain numpy, and checks its own backward pass
+against finite differences.
+
+Network (per polyhedron = node; H hidden units, L message-passing layers):
+    h   = relu(x W0 + b0)                                  x: [N, F]
+    for l in 1..L:
+        m   = relu(h Wm_l + bm_l)                          [N, H]
+        a_i = sum_j w_ij m_j          (w: face-area weights, rows sum to 1)
+        z   = [h, a, g] Wu_l + bu_l   (g_i = sum_j w_ij e_ij, edge geometry)
+        h   = h + relu(z)
+    y   = h Wo + bo                                        [N, O]
+Weights are stored in BF16 on the device (here: the same BF16-rounded
+values), activations and accumulation in FP32 (here: FP64).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def bf16_round(a: np.ndarray) -> np.ndarray:
+    """Round float values to the nearest BF16 (ties to even), returned as float64."""
+    f = np.asarray(a, dtype=np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    lsb = (u >> 16) & 1
+    r = ((u + 0x7FFF + lsb) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def shapes(F: int, H: int, O: int, L: int, G: int):
+    s = {"W0": (F, H), "b0": (H,)}
+    for l in range(L):
+        s[f"Wm{l}"] = (H, H)
+        s[f"bm{l}"] = (H,)
+        s[f"Wu{l}"] = (2 * H + G, H)
+        s[f"bu{l}"] = (H,)
+    s["Wo"] = (H, O)
+    s["bo"] = (O,)
+    return s
+
+
+def init_params(F, H, O, L, G, seed=0):
+    rng = np.random.default_rng(seed)
+    p = {}
+    for k, sh in shapes(F, H, O, L, G).items():
+        if k.startswith("W"):
+            p[k] = rng.standard_normal(sh) * np.sqrt(2.0 / sh[0]) * (0.1 if k == "Wo" else 1.0)
+        else:
+            p[k] = np.zeros(sh)
+    return p
+
+
+def aggregate(w_ptr, w_idx, w_val, m):
+    out = np.zeros_like(m)
+    for i in range(len(w_ptr) - 1):
+        for k in range(w_ptr[i], w_ptr[i + 1]):
+            out[i] += w_val[k] * m[w_idx[k]]
+    return out
+
+
+def aggregate_T(w_ptr, w_idx, w_val, da):
+    """Adjoint of aggregate: dm_j = sum_i w_ij da_i."""
+    out = np.zeros_like(da)
+    for i in range(len(w_ptr) - 1):
+        for k in range(w_ptr[i], w_ptr[i + 1]):
+            out[w_idx[k]] += w_val[k] * da[i]
+    return out
+
+
+def forward(params, x, graph, L, keep=False):
+    w_ptr, w_idx, w_val, g = graph
+    cache = {}
+    z0 = x @ params["W0"] + params["b0"]
+    h = np.maximum(z0, 0.0)
+    cache["x"], cache["z0"] = x, z0
+    for l in range(L):
+        zm = h @ params[f"Wm{l}"] + params[f"bm{l}"]
+        m = np.maximum(zm, 0.0)
+        a = aggregate(w_ptr, w_idx, w_val, m)
+        cat = np.concatenate([h, a, g], axis=1)
+        zu = cat @ params[f"Wu{l}"] + params[f"bu{l}"]
+        cache[l] = (h, zm, m, cat, zu)
+        h = h + np.maximum(zu, 0.0)
+    y = h @ params["Wo"] + params["bo"]
+    cache["hL"] = h
+    return (y, cache) if keep else y
+
+
+def loss_and_grad(params, x, graph, target, L):
+    """Mean squared error over all entries and its gradient."""
+    w_ptr, w_idx, w_val, g = graph
+    y, c = forward(params, x, graph, L, keep=True)
+    diff = y - target
+    n = diff.size
+    loss = float(np.sum(diff * diff) / n)
+    dy = 2.0 * diff / n
+    grads = {}
+    grads["Wo"] = c["hL"].T @ dy
+    grads["bo"] = dy.sum(0)
+    dh = dy @ params["Wo"].T
+    H = dh.shape[1]
+    for l in reversed(range(L)):
+        h, zm, m, cat, zu = c[l]
+        dzu = dh * (zu > 0)
+        grads[f"Wu{l}"] = cat.T @ dzu
+        grads[f"bu{l}"] = dzu.sum(0)
+        dcat = dzu @ params[f"Wu{l}"].T
+        dh_prev = dh + dcat[:, :H]
+        da = dcat[:, H:2 * H]
+        dm = aggregate_T(w_ptr, w_idx, w_val, da)
+        dzm = dm * (zm > 0)
+        grads[f"Wm{l}"] = h.T @ dzm
+        grads[f"bm{l}"] = dzm.sum(0)
+        dh = dh_prev + dzm @ params[f"Wm{l}"].T
+    dz0 = dh * (c["z0"] > 0)
+    grads["W0"] = c["x"].T @ dz0
+    grads["b0"] = dz0.sum(0)
+    return loss, grads
+
+
+def finite_difference_check(params, x, graph, target, L, n_probe=12, eps=1e-6, seed=0):
+    """Largest relative mismatch between the analytic gradient and central
+    differences on n_probe random entries of every parameter."""
+    rng = np.random.default_rng(seed)
+    _, grads = loss_and_grad(params, x, graph, target, L)
+    worst = 0.0
+    for k, v in params.items():
+        flat = v.reshape(-1)
+        for idx in rng.choice(flat.size, size=min(n_probe, flat.size), replace=False):
+            old = flat[idx]
+            flat[idx] = old + eps
+            lp, _ = loss_and_grad(params, x, graph, target, L)
+            flat[idx] = old - eps
+            lm, _ = loss_and_grad(params, x, graph, target, L)
+            flat[idx] = old
+            fd = (lp - lm) / (2 * eps)
+            an = grads[k].reshape(-1)[idx]
+            scale = max(abs(fd), abs(an), 1e-8)
+            worst = max(worst, abs(fd - an) / scale)
+    return worst

@@ -6,8 +6,9 @@ Bars (written in each assertion):
   * modal coefficients after every step, both sides started from the same
     coefficients: ||u_gpu - u_ref|| / ||u_ref|| <= max(1e-12, 4 x floor),
     floor = the oracle's own spread when its operator apply sums in reverse
-    order and applies M^-1 as an explicit inverse (both equally valid
-    evaluations of the same step; the ill-conditioned mass matrix lifts that
+    order with fused multiply-adds and applies M^-1 as an explicit inverse
+    (the operations the device uses, in another order: an equally valid
+    evaluation of the same step; the ill-conditioned mass matrix lifts that
     spread above 1e-12 at p = 4); and
     <= 1e-12 in the mass-matrix norm (the L2 norm of the field);
   * L2 projections (COMPUTE_MODAL_COEFFICIENTS_FREE) solve with the mass
