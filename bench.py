@@ -61,6 +61,13 @@ CONFIGS = {
     # 48k polyhedra, p = 4, lognormal lambda/mu per polyhedron
     "c2": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=4, material=(1.0, 1.0, 1.0), lognormal=True,
                dt=2e-5, sample_n=8),
+    # learned surrogate: trained on 200 seeded solver runs (p = 3, 4^3..10^3
+    # meshes, Ricker sources from rest, lognormal materials), evaluated on the
+    # c2 mesh at p = 3, dt = 2e-5, a 50 Hz Ricker point source at the centre,
+    # 2000 steps after 600 plain ones, K = 8
+    "c4": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 1.0, 1.0), lognormal=True,
+               dt=2e-5, sample_n=None, surrogate=dict(n_traj=200, iters=20000, K=8, f0=50.0, warm=600,
+                                                      res_tols=(1e-6, 1e-5), sizes=(4, 5, 6, 8, 10))),
 }
 
 
@@ -321,6 +328,79 @@ def run_ensemble(cfg, precision, steps, warmup, info):
             "grid": grid, "order": order, "finite": finite, "meta": meta}
 
 
+def run_surrogate(cfg, steps):
+    """Config c4: trains the network on the GPU, then times the plain stepper
+    against the surrogate blocks (cubic Taylor predictor alone, and with the
+    network's correction) on the same 2000 steps, reporting the relative L2
+    (mass-norm) distance of each final state from the plain one."""
+    import numpy as np
+    from lymph3d_apsc_gb300 import MatrixFree, _lib
+    from lymph3d_apsc_gb300 import ensemble as E
+    from lymph3d_apsc_gb300 import surrogate as S
+    sc = cfg["surrogate"]
+    K = sc["K"]
+    net, hist, t_data, t_train = S.train_surrogate(cfg["p"], n_traj=sc["n_traj"], iters=sc["iters"], K=K,
+                                                   sizes=sc["sizes"])
+    held = S.held_out_errors(net, cfg["p"])
+    log(f"[bench] surrogate trained: data {t_data:.1f}s, training {t_train:.1f}s, loss "
+        f"{np.mean(hist[:50]):.3e} -> {np.mean(hist[-500:]):.3e}; held-out error ratios "
+        f"{[round(a / b, 3) for a, b in held]}")
+    m = make_mesh(cfg)
+    g = MatrixFree(m, cfg["p"], cfg["dt"])
+    g.MAKE_MATRICES_FREE()
+    g.MAKE_RHS_FREE(_lib.RHS_STAT, _lib.F_NULL, _lib.GD_NULL, _lib.GN_NULL)
+    E.point_source(g, [0.5, 0.5, 0.5], [0.0, 0.0, 1.0])
+    f0 = sc["f0"]
+    gfun = lambda t: float(E.ricker(t, f0, 2.0 / f0))  # noqa: E731
+    g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_DISPLACEMENT, _lib.SLOT_U0)
+    g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_DISPLACEMENT, _lib.SLOT_V0)
+    _lib.check(g.lib.lymph_first_step_g(g.ctx, gfun(0.0)), "first_step_g")
+    t0 = S.run_plain(g, sc["warm"] - 1, gfun, g.dt)
+    u0, un = g.get_state(_lib.SLOT_U0).copy(), g.get_state(_lib.SLOT_UN).copy()
+    graph = S.build_graph(m)
+    dofs = 3 * g.Np * g.n_poly
+    sync = lambda: g.get_state(_lib.SLOT_UN)[:1]  # noqa: E731  (host read: the device is idle after it)
+    sync()
+    a = time.perf_counter()
+    S.run_plain(g, steps, gfun, t0)
+    sync()
+    t_plain = time.perf_counter() - a
+    ref = g.get_state(_lib.SLOT_UN).copy()
+    zero = np.zeros_like(ref)
+
+    def rel_l2():
+        g.set_state(_lib.SLOT_UEX, ref)
+        e = g.COMPUTE_ERROR_L2_MATRIX_FREE()
+        g.set_state(_lib.SLOT_UEX, zero)
+        nrm = g.COMPUTE_ERROR_L2_MATRIX_FREE()
+        return math.sqrt(e / nrm)
+
+    runs = []
+    for mode, nn in (("taylor", None), ("network", net)):
+        for tol in sc["res_tols"]:
+            g.set_state(_lib.SLOT_U0, u0)
+            g.set_state(_lib.SLOT_UN, un)
+            sync()
+            a = time.perf_counter()
+            _, st = S.run_hybrid(g, nn, steps, gfun, t0, K=K, graph=graph, res_tol=tol)
+            sync()
+            el = time.perf_counter() - a
+            runs.append({"mode": mode, "res_tol": tol, "seconds": el, "speedup_vs_plain": t_plain / el,
+                         "value": dofs * steps / el, "rel_L2_vs_plain": rel_l2(), "blocks": st["blocks"],
+                         "accepted": st["accepted"], "plain_steps": st["plain_steps"],
+                         "judge_err_max": st["judge_err_max"]})
+            log(f"[bench] {mode} res_tol {tol:g}: {el:.2f}s (plain {t_plain:.2f}s) x{t_plain / el:.2f}, "
+                f"rel L2 {runs[-1]['rel_L2_vs_plain']:.2e}, accepted {st['accepted']}/{st['blocks']}")
+    launches = g.launch_count()
+    out = {"dofs": dofs, "n_poly": g.n_poly, "t_plain": t_plain, "runs": runs, "held_out": held,
+           "train": {"trajectories": sc["n_traj"], "iters": sc["iters"], "data_s": t_data, "train_s": t_train,
+                     "loss_first": float(np.mean(hist[:50])), "loss_last": float(np.mean(hist[-500:]))},
+           "launches": launches}
+    net.close()
+    g.close()
+    return out
+
+
 def rank_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -379,6 +459,24 @@ def main():
         return
 
     precision = 1 if args.precision == "mixed" else 0
+    if cfg.get("surrogate"):
+        if info["rank"] != 0:
+            return
+        with ClockSampler(info["gpu"]) as clk:
+            r = run_surrogate(cfg, args.steps)
+        best = max(r["runs"], key=lambda x: x["speedup_vs_plain"] if x["rel_L2_vs_plain"] < 1e-2 else 0.0)
+        line = {"metric": metric, "value": best["value"], "unit": "DOF-steps/s", "n_gpus": 1, "steps": args.steps,
+                "warmup": cfg["surrogate"]["warm"], "ms_per_step": 1e3 * best["seconds"] / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (network bf16/f32)",
+                "data": "synthetic (generated meshes; training runs of the solver itself)",
+                "config": {"workload": f"surrogate K=8 on the c2 mesh at p=3: {r['n_poly']} polyhedra, dt=2e-5, "
+                                       "50 Hz Ricker point source at the centre, 2000 steps after 600 plain",
+                           "dofs": r["dofs"], "l2_flush": "inputs larger than L2"},
+                "plain_value": r["dofs"] * args.steps / r["t_plain"], "runs": r["runs"],
+                "held_out_error_ratio_network_vs_taylor": [a / b for a, b in r["held_out"]],
+                "train": r["train"], "gpu_launches": r["launches"], "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+        return
     if cfg.get("ensemble"):
         r = run_ensemble(cfg, precision, args.steps, args.warmup, info)
         value = r["dofs"] * r["steps"] / (r["ms"] / 1e3)

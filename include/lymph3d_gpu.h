@@ -259,20 +259,39 @@ int lymph_mpnn_forward(lymph_mpnn* net, const float* x, float* y);
 int lymph_mpnn_loss_grad(lymph_mpnn* net, const float* x, const float* target, double* loss);
 int lymph_mpnn_adam(lymph_mpnn* net, float lr, float beta1, float beta2, float eps);
 int lymph_mpnn_launch_count(const lymph_mpnn* net, int64_t* count);
+/* Gated output head: the O = 6 B network outputs per node are coefficients
+ * alpha[j][b][i] and the effective output (2 nd columns, what forward
+ * returns and the loss compares) is
+ * yg[j][i*Np + m] = sum_b alpha[j][b][i] x[b*nd + i*Np + m], nd = 3 Np:
+ * a per-node, per-component combination of the first B feature blocks. */
+int lymph_mpnn_set_gate(lymph_mpnn* net, int32_t nd, int32_t B);
 
 /* One surrogate block: with V0 = u^{n-1}, U0 = u^n, UN = u^{n+1} in the
- * context, predicts u^{n+1+k} for k = K-3, K-2, K-1 as the
- * constant-second-difference extrapolation u1 + k d1 + k(k+1)/2 d2
- * (d1 = u1 - u0, d2 = u1 - 2u0 + um) plus the network's correction
- * sc (y3 phi3(k) + y4 phi4(k)) in the Newton basis phi3 = k(k+1)(k+2)/K^3,
- * phi4 = phi3 (k+3)/K, sc = (s3^2/s2) K^3/6 with s1..s3 the RMS of u1, d1,
- * d2 (use_net = 0: the extrapolation alone).  The features [u1/s1, d1/s2,
- * d2/s3, log10 s2/s1, log10 s3/s2, lambda, mu, rho] are built on the device;
- * the network's O = 2 * 3Np outputs are [y3 | y4].  Afterwards V0 and UEX
- * hold u^n, u^{n+1} (for a fallback), U0 and UN the predicted u^{n+K-2},
- * u^{n+K-1}, and the network object the predicted u^{n+K}.  K >= 4.
- * scales (nullable) receives s1, s2, s3. */
-int lymph_surrogate_predict(lymph_ctx* ctx, lymph_mpnn* net, int32_t K, int32_t use_net, double* scales);
+ * context, predicts u^{n+1+k} for k = K-3, K-2, K-1 as the cubic Taylor
+ * extrapolation u1 + k d1 + k(k+1)/2 d2 - k(k+1)(k+2)/6 a1
+ * (d1 = u1 - u0, d2 = u1 - 2u0 + um, a1 = dt^2 M^-1 (K d1 - gdiff F_dyn),
+ * one operator apply; gdiff = g(t_{n+1}) - g(t_n) of the source time
+ * function) plus the network's correction sc_P (y3 phi3(k) + y4 phi4(k)) in
+ * the Newton basis phi3 = k(k+1)(k+2)/K^3, phi4 = phi3 (k+3)/K, with
+ * sc_P = (r4^2/r3) K^4/24 from the polyhedron's own scales r_b (RMS of u1,
+ * d1, d2, a1 over its DOFs plus 1e-3 x the mesh-wide RMS); use_net = 0: the
+ * extrapolation alone.  The features, normalised per polyhedron,
+ * [u1/r1, d1/r2, d2/r3, a1/r4, log10 r2/r1, log10 r3/r2, log10 r4/r3,
+ * log10 r1/s1, lambda, mu, rho] are built on the device: F >= 4 * 3Np + 7;
+ * the network's effective output is [y3 | y4] (2 * 3Np per polyhedron).
+ * Afterwards V0 and UEX hold u^n, u^{n+1} (for a fallback), U0 and UN the
+ * predicted u^{n+K-2}, u^{n+K-1}, and the network object the predicted
+ * u^{n+K}.  K >= 4.  scales (nullable) receives the mesh-wide RMS s1..s4. */
+int lymph_surrogate_predict(lymph_ctx* ctx, lymph_mpnn* net, int32_t K, int32_t use_net, double gdiff,
+                            double* scales);
+
+/* The feature rows lymph_surrogate_predict would build from the same
+ * context state, copied to x (host, n_poly x F floats); scales (nullable, 4
+ * doubles) receives s1..s4, a1 (nullable, n_poly x 3Np doubles) the
+ * operator term, sig (nullable, n_poly x 4 doubles) the per-polyhedron
+ * scales r1..r4.  For training samples from solver runs. */
+int lymph_surrogate_features(lymph_ctx* ctx, lymph_mpnn* net, double gdiff, float* x, double* scales, double* a1,
+                             double* sig);
 
 /* After one plain step from the predicted pair (U0 = u^{n+K-1}, UN = the
  * stepped u^{n+K}): residual = |UN - predicted u^{n+K}| / |UN|. */

@@ -118,8 +118,10 @@ _SIGS = {
     "lymph_mpnn_loss_grad": (c_int, [c_void_p, POINTER(c_float), POINTER(c_float), P_F64]),
     "lymph_mpnn_adam": (c_int, [c_void_p, c_float, c_float, c_float, c_float]),
     "lymph_mpnn_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
-    "lymph_surrogate_predict": (c_int, [c_void_p, c_void_p, c_int32, c_int32, P_F64]),
+    "lymph_surrogate_predict": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_double, P_F64]),
     "lymph_surrogate_residual": (c_int, [c_void_p, c_void_p, P_F64]),
+    "lymph_mpnn_set_gate": (c_int, [c_void_p, c_int32, c_int32]),
+    "lymph_surrogate_features": (c_int, [c_void_p, c_void_p, c_double, POINTER(c_float), P_F64, P_F64, P_F64]),
     "lymph_surrogate_judge": (c_int, [c_void_p, c_void_p, c_int32, P_F64]),
     "lymph_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_device_bytes": (c_int, [c_void_p, POINTER(c_int64)]),

@@ -6,6 +6,10 @@
 //     h = relu(x W0 + b0)
 //     L times:  m = relu(h Wm + bm);  a = W m;  h += relu([h a g] Wu + bu)
 //     y = h Wo + bo
+// Optional gated head (lymph_mpnn_set_gate): y holds per-node coefficients
+// alpha[j][b][i] (j < 2 outputs, b < B basis vectors, i < 3 components) and
+// the effective output is  yg[j][i*Np + m] = sum_b alpha[j][b][i] x[b*nd + i*Np + m]
+// (nd = 3 Np): a learned per-node combination of the first B feature blocks.
 // Weight matrices are kept as FP32 masters for Adam and as BF16 copies that
 // every GEMM reads; activations and accumulation are FP32.  The concatenation
 // [h a g] is never formed: its GEMM is three GEMMs on row slices of Wu
@@ -14,12 +18,15 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "common.cuh"
+
+int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);  // out = M^-1 K u (step.cu)
 
 namespace {
 
@@ -171,6 +178,37 @@ __global__ void k_to_bf16(int64_t n, const float* __restrict__ a, __nv_bfloat16*
         b[i] = __float2bfloat16_rn(a[i]);
 }
 
+// Gated head: yg[P][j*nd + c] = sum_b y[P][(j*B + b)*3 + i] x[P][b*nd + c],
+// i = c / Np (the displacement component of DOF c).
+__global__ void k_gate(int N, int nd, int B, int F, const float* __restrict__ y, const float* __restrict__ x,
+                       float* yg) {
+    const int Np = nd / 3, O = 2 * B * 3;
+    const int64_t tot = (int64_t)N * 2 * nd;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t P = q / (2 * nd);
+        const int r = (int)(q % (2 * nd)), j = r / nd, c = r % nd, i = c / Np;
+        float v = 0.0f;
+        for (int b = 0; b < B; ++b) v += y[P * O + (j * B + b) * 3 + i] * x[P * F + b * nd + c];
+        yg[q] = v;
+    }
+}
+
+// Its adjoint: dy[P][(j*B + b)*3 + i] = sum_m dyg[P][j*nd + i*Np + m] x[P][b*nd + i*Np + m]
+__global__ void k_gate_back(int N, int nd, int B, int F, const float* __restrict__ dyg, const float* __restrict__ x,
+                            float* dy) {
+    const int Np = nd / 3, O = 2 * B * 3;
+    const int64_t tot = (int64_t)N * O;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t P = q / O;
+        const int o = (int)(q % O), i = o % 3, jb = o / 3, j = jb / B, b = jb % B;
+        const float* g = dyg + P * 2 * nd + j * nd + i * Np;
+        const float* xv = x + P * F + b * nd + i * Np;
+        float s = 0.0f;
+        for (int m = 0; m < Np; ++m) s += g[m] * xv[m];
+        dy[q] = s;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -189,6 +227,9 @@ struct lymph_mpnn {
     // activations for the current graph size
     int n_cap = 0;
     float *d_x = nullptr, *d_z0 = nullptr, *d_y = nullptr, *d_t = nullptr, *d_dy = nullptr, *d_gf = nullptr;
+    // gated head: gate_nd DOFs per node, gate_B basis blocks (0: plain head)
+    int gate_nd = 0, gate_B = 0;
+    float *d_yg = nullptr, *d_dyg = nullptr;
     std::vector<float*> d_h, d_zm, d_m_, d_a, d_zu;  // per layer
     float *d_dh = nullptr, *d_dz = nullptr, *d_dtmp = nullptr, *d_dm = nullptr;
     double* d_partial = nullptr;
@@ -196,6 +237,8 @@ struct lymph_mpnn {
     int64_t nv_cap = 0;
     double *d_d1 = nullptr, *d_d2 = nullptr, *d_ss = nullptr;
     double* d_u3 = nullptr;  // the predicted u^{n+K}, checked after the closing plain step
+    double* d_a1 = nullptr;  // dt^2 M^-1 (K d1 - gdiff F) (a feature)
+    double* d_sig = nullptr;  // per-polyhedron scales [n_poly][4] of the last features
     const lymph_ctx* have_u3 = nullptr;      // context of the last prediction
     const lymph_ctx* judge_saved = nullptr;  // context whose pair the judge keeps
     // graph (CSR weights, and transposed)
@@ -242,14 +285,16 @@ void aggregate(lymph_mpnn* n, bool transposed, int width, const float* in, float
 int ensure_capacity(lymph_mpnn* n, int N) {
     if (N <= n->n_cap) return LYMPH_OK;
     auto fr = [](float*& p) { if (p) cudaFree(p); p = nullptr; };
-    fr(n->d_x); fr(n->d_z0); fr(n->d_y); fr(n->d_t); fr(n->d_dy); fr(n->d_gf);
+    fr(n->d_x); fr(n->d_z0); fr(n->d_y); fr(n->d_t); fr(n->d_dy); fr(n->d_gf); fr(n->d_yg); fr(n->d_dyg);
     fr(n->d_dh); fr(n->d_dz); fr(n->d_dtmp); fr(n->d_dm);
     for (auto* v : {&n->d_h, &n->d_zm, &n->d_m_, &n->d_a, &n->d_zu})
         for (auto& p : *v) fr(p);
     const int H = n->H;
     auto al = [&](float*& p, int64_t cnt) { return cudaMalloc(&p, sizeof(float) * (size_t)cnt) == cudaSuccess; };
+    const int64_t Ot = n->gate_B ? 2 * n->gate_nd : n->O;  // width of the effective output and target
     bool ok = al(n->d_x, (int64_t)N * n->F) && al(n->d_z0, (int64_t)N * H) && al(n->d_y, (int64_t)N * n->O) &&
-              al(n->d_t, (int64_t)N * n->O) && al(n->d_dy, (int64_t)N * n->O) && al(n->d_gf, (int64_t)N * n->G) &&
+              al(n->d_t, (int64_t)N * Ot) && al(n->d_dy, (int64_t)N * n->O) && al(n->d_gf, (int64_t)N * n->G) &&
+              (!n->gate_B || (al(n->d_yg, (int64_t)N * Ot) && al(n->d_dyg, (int64_t)N * Ot))) &&
               al(n->d_dh, (int64_t)N * H) && al(n->d_dz, (int64_t)N * H) && al(n->d_dtmp, (int64_t)N * H) &&
               al(n->d_dm, (int64_t)N * H);
     n->d_h.assign(n->L + 1, nullptr);
@@ -291,7 +336,17 @@ void forward(lymph_mpnn* n) {
     }
     gemm<false, false, __nv_bfloat16>(n, N, O, H, n->d_h[n->L], H, B_(n, "Wo"), O, n->d_y, O, P_(n, "bo"), nullptr,
                                       EPI_STORE);
+    if (n->gate_B) {
+        const int64_t tot = (int64_t)N * 2 * n->gate_nd;
+        k_gate<<<(int)std::min<int64_t>((tot + 255) / 256, 4096), 256, 0, n->stream>>>(N, n->gate_nd, n->gate_B, n->F,
+                                                                                       n->d_y, n->d_x, n->d_yg);
+        n->launches++;
+    }
 }
+
+// effective output (what predictions and the loss use)
+const float* eff_out(const lymph_mpnn* n) { return n->gate_B ? n->d_yg : n->d_y; }
+int64_t eff_width(const lymph_mpnn* n) { return n->gate_B ? 2 * n->gate_nd : n->O; }
 
 // backward from d_dy; gradients into d_g
 void backward(lymph_mpnn* n) {
@@ -425,58 +480,135 @@ __global__ void k_sum3(int nblk, const double* __restrict__ part, double* out) {
     if (lane == 0) out[j] = s;
 }
 
-// Node features of the surrogate (one row per polyhedron, F columns):
-// [u1/s1, d1/s2, d2/s3, log10(s2/s1), log10(s3/s2), lambda, mu, rho, 0...]
-// with s = RMS of u1, d1, d2 over the whole mesh.
-__global__ void k_features(int n_poly, int nd, int F, const double* __restrict__ u1, const double* __restrict__ d1,
-                           const double* __restrict__ d2, const double* __restrict__ ss, int64_t n_all,
-                           const int32_t* __restrict__ pptr, const int32_t* __restrict__ ptets,
-                           const int32_t* __restrict__ tmat, const double* __restrict__ mat, float* x) {
-    const int P = blockIdx.x;
+// Node features of the surrogate (one row per polyhedron, F columns), all
+// normalised per polyhedron so that they do not depend on the mesh's size:
+// [u1/r1, d1/r2, d2/r3, a1/r4, log10(r2/r1), log10(r3/r2), log10(r4/r3),
+//  log10(r1/s1), lambda, mu, rho, 0...] with a1 = dt^2 M^-1 (K d1 - gdiff F)
+// (the third difference to leading order, up to sign), r_b = the
+// polyhedron's RMS of vector b plus 1e-3 x its mesh-wide RMS s_b (a floor
+// where the field is quiet).  sig[P][b] = r_b (the per-polyhedron scales of
+// the correction).
+constexpr int FEAT_THREADS = 128;  // >= 3 Np for p <= 4 (105)
+
+__global__ void __launch_bounds__(FEAT_THREADS) k_features(
+    int n_poly, int nd, int F, const double* __restrict__ u1, const double* __restrict__ d1,
+    const double* __restrict__ d2, const double* __restrict__ a1, const double* __restrict__ ss, int64_t n_all,
+    const int32_t* __restrict__ pptr, const int32_t* __restrict__ ptets, const int32_t* __restrict__ tmat,
+    const double* __restrict__ mat, float* x, double* sig) {
+    __shared__ double red[4][FEAT_THREADS];
+    __shared__ double r[4];
+    const int P = blockIdx.x, tid = threadIdx.x;
     if (P >= n_poly) return;
-    const double tiny = 1e-300;
-    const double s1 = sqrt(ss[0] / (double)n_all) + tiny, s2 = sqrt(ss[1] / (double)n_all) + tiny,
-                 s3 = sqrt(ss[2] / (double)n_all) + tiny;
-    float* row = x + (int64_t)P * F;
-    for (int c = threadIdx.x; c < F; c += blockDim.x) {
+    const int64_t q = (int64_t)P * nd;
+    const double* vec[4] = {u1, d1, d2, a1};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
         double v = 0.0;
-        const int64_t q = (int64_t)P * nd;
-        if (c < nd) v = u1[q + c] / s1;
-        else if (c < 2 * nd) v = d1[q + c - nd] / s2;
-        else if (c < 3 * nd) v = d2[q + c - 2 * nd] / s3;
-        else if (c == 3 * nd) v = log10(s2 / s1);
-        else if (c == 3 * nd + 1) v = log10(s3 / s2);
-        else if (c < 3 * nd + 5) v = mat[tmat[ptets[pptr[P]]] * 3 + (c - 3 * nd - 1) % 3];
+        for (int c = tid; c < nd; c += FEAT_THREADS) {
+            const double w = vec[b][q + c];
+            v += w * w;
+        }
+        red[b][tid] = v;
+    }
+    __syncthreads();
+    for (int w = FEAT_THREADS / 2; w > 0; w >>= 1) {
+        if (tid < w)
+            for (int b = 0; b < 4; ++b) red[b][tid] += red[b][tid + w];
+        __syncthreads();
+    }
+    if (tid < 4) {
+        const double glob = sqrt(ss[tid] / (double)n_all);
+        r[tid] = sqrt(red[tid][0] / (double)nd) + 1e-3 * glob + 1e-300;
+        sig[(int64_t)P * 4 + tid] = r[tid];
+    }
+    __syncthreads();
+    const double s1 = sqrt(ss[0] / (double)n_all) + 1e-300;
+    float* row = x + (int64_t)P * F;
+    for (int c = tid; c < F; c += FEAT_THREADS) {
+        double v = 0.0;
+        if (c < 4 * nd) v = vec[c / nd][q + c % nd] / r[c / nd];
+        else if (c == 4 * nd) v = log10(r[1] / r[0]);
+        else if (c == 4 * nd + 1) v = log10(r[2] / r[1]);
+        else if (c == 4 * nd + 2) v = log10(r[3] / r[2]);
+        else if (c == 4 * nd + 3) v = log10(r[0] / s1);
+        else if (c < 4 * nd + 7) v = mat[tmat[ptets[pptr[P]]] * 3 + (c - 4 * nd - 3) % 3];
         row[c] = (float)v;
     }
 }
 
-// Predicted states u^{n+1+k} = u1 + k d1 + k(k+1)/2 d2
+// y[q] = sum_c Minv_P[m, c] rhs[P, i, c] for q = (P, i, m): M^-1 applied to
+// the source's right-hand side (Minv column-major per polyhedron).
+__global__ void k_minv_rhs(int n_poly, int Np, const double* __restrict__ Minv, const double* __restrict__ rhs,
+                           double* y) {
+    const int64_t nv = (int64_t)n_poly * 3 * Np;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nv; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t P = q / (3 * Np);
+        const int r = (int)(q % (3 * Np)), i = r / Np, m = r % Np;
+        const double* Mi = Minv + P * Np * Np + m;
+        const double* b = rhs + P * 3 * Np + i * Np;
+        double x = 0.0;
+        for (int c = 0; c < Np; ++c) x += Mi[(int64_t)c * Np] * b[c];
+        y[q] = x;
+    }
+}
+
+// a1 = dt^2 (a1 - gdiff * MinvF): dt^2 M^-1 (K d1 - gdiff F), minus the
+// third difference of the leapfrog to leading order
+__global__ void k_accel_combine(int64_t n, double dt2, double gdiff, const double* __restrict__ minvf, double* a1) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a1[i] = dt2 * (a1[i] - gdiff * minvf[i]);
+}
+
+// Per-CTA partial sums of squares of one vector (into part[3 blk])
+__global__ void __launch_bounds__(256) k_one_sumsq(int64_t n, const double* __restrict__ a, double* part) {
+    __shared__ double red[256];
+    double s0 = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s0 += a[i] * a[i];
+    red[threadIdx.x] = s0;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = red[0];
+        part[3 * blockIdx.x + 1] = 0.0;
+        part[3 * blockIdx.x + 2] = 0.0;
+    }
+}
+
+// Predicted states u^{n+1+k} = u1 + k d1 + k(k+1)/2 d2 - k(k+1)(k+2)/6 a1
 //                             + sc (y3 phi3(k) + y4 phi4(k)),
-// phi3(k) = k(k+1)(k+2)/K^3, phi4(k) = k(k+1)(k+2)(k+3)/K^4 (the Newton basis
-// of the extrapolation's cubic and quartic error terms), sc = (s3^2/s2) K^3/6
-// (s3/s2 ~ omega dt, so the coefficients are of order one); y = [y3 | y4] per
-// row.  Written for k = K-3 (out_a), K-2 (out_b) and K-1 (out_c).
+// a1 = dt^2 M^-1 (K d1 - gdiff F) (the third difference, up to sign, to
+// leading order), phi3(k) = k(k+1)(k+2)/K^3, phi4(k) = phi3(k) (k+3)/K (the
+// Newton basis of the remaining cubic and quartic error terms),
+// sc = (r4^2/r3) K^4/24 per polyhedron (r: its scales from k_features;
+// r4/r3 ~ omega dt: coefficients of order one); y = [y3 | y4] per row.
+// Written for k = K-3 (out_a), K-2 (out_b), K-1 (out_c).
 __global__ void k_predict(int64_t n, int nd, int K, const double* __restrict__ u1, const double* __restrict__ d1,
-                          const double* __restrict__ d2, const double* __restrict__ ss, int64_t n_all,
-                          const float* __restrict__ y, int use_net, double* out_a, double* out_b, double* out_c) {
-    const double s2 = sqrt(ss[1] / (double)n_all) + 1e-300, s3 = sqrt(ss[2] / (double)n_all) + 1e-300;
+                          const double* __restrict__ d2, const double* __restrict__ a1,
+                          const double* __restrict__ sig, const float* __restrict__ y, int use_net,
+                          double* out_a, double* out_b, double* out_c) {
     const double Kd = (double)K;
-    const double sc = (s3 * s3 / s2) * Kd * Kd * Kd / 6.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t P = i / nd, c = i % nd;
-        double y3 = 0.0, y4 = 0.0;
+        double y3 = 0.0, y4 = 0.0, sc = 0.0;
         if (use_net) {
             y3 = (double)y[P * 2 * nd + c];
             y4 = (double)y[P * 2 * nd + nd + c];
+            const double r3 = sig[P * 4 + 2], r4 = sig[P * 4 + 3];
+            sc = (r4 * r4 / r3) * Kd * Kd * Kd * Kd / 24.0;
         }
         double* outs[3] = {out_a, out_b, out_c};
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             const double k = Kd - 3.0 + j;
-            const double p3 = k * (k + 1.0) * (k + 2.0) / (Kd * Kd * Kd);
+            const double c3 = k * (k + 1.0) * (k + 2.0);
+            const double p3 = c3 / (Kd * Kd * Kd);
             const double p4 = p3 * (k + 3.0) / Kd;
-            outs[j][i] = u1[i] + k * d1[i] + 0.5 * k * (k + 1.0) * d2[i] + sc * (y3 * p3 + y4 * p4);
+            outs[j][i] = u1[i] + k * d1[i] + 0.5 * k * (k + 1.0) * d2[i] - (c3 / 6.0) * a1[i] +
+                         sc * (y3 * p3 + y4 * p4);
         }
     }
 }
@@ -541,8 +673,9 @@ int lymph_mpnn_destroy(lymph_mpnn* n) {
     if (!n) return LYMPH_OK;
     if (n->stream) cudaStreamSynchronize(n->stream);
     for (void* p : {(void*)n->d_p, (void*)n->d_g, (void*)n->d_m, (void*)n->d_v, (void*)n->d_pb, (void*)n->d_partial,
-                    (void*)n->d_d1, (void*)n->d_d2, (void*)n->d_ss, (void*)n->d_u3,
+                    (void*)n->d_d1, (void*)n->d_d2, (void*)n->d_ss, (void*)n->d_u3, (void*)n->d_a1, (void*)n->d_sig,
                     (void*)n->d_x, (void*)n->d_z0, (void*)n->d_y, (void*)n->d_t, (void*)n->d_dy, (void*)n->d_gf,
+                    (void*)n->d_yg, (void*)n->d_dyg,
                     (void*)n->d_dh, (void*)n->d_dz, (void*)n->d_dtmp, (void*)n->d_dm, (void*)n->d_wp, (void*)n->d_wi,
                     (void*)n->d_tp, (void*)n->d_ti, (void*)n->d_wv, (void*)n->d_tv})
         if (p) cudaFree(p);
@@ -592,7 +725,8 @@ int lymph_mpnn_forward(lymph_mpnn* n, const float* x, float* y) {
     LYMPH_CUDA_TRY(cudaMemcpyAsync(n->d_x, x, sizeof(float) * (size_t)n->n_nodes * n->F, cudaMemcpyHostToDevice, n->stream));
     forward(n);
     LYMPH_CUDA_TRY(cudaGetLastError());
-    LYMPH_CUDA_TRY(cudaMemcpyAsync(y, n->d_y, sizeof(float) * (size_t)n->n_nodes * n->O, cudaMemcpyDeviceToHost, n->stream));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(y, eff_out(n), sizeof(float) * (size_t)n->n_nodes * eff_width(n),
+                                   cudaMemcpyDeviceToHost, n->stream));
     LYMPH_CUDA_TRY(cudaStreamSynchronize(n->stream));
     return LYMPH_OK;
 }
@@ -601,13 +735,21 @@ int lymph_mpnn_forward(lymph_mpnn* n, const float* x, float* y) {
 // (read them with lymph_mpnn_get_params).  loss may be NULL.
 int lymph_mpnn_loss_grad(lymph_mpnn* n, const float* x, const float* target, double* loss) {
     if (!n || !x || !target || n->n_nodes <= 0) return LYMPH_ERR_INVALID;
-    const int64_t ny = (int64_t)n->n_nodes * n->O;
+    const int64_t ny = (int64_t)n->n_nodes * eff_width(n);
     LYMPH_CUDA_TRY(cudaMemcpyAsync(n->d_x, x, sizeof(float) * (size_t)n->n_nodes * n->F, cudaMemcpyHostToDevice, n->stream));
     LYMPH_CUDA_TRY(cudaMemcpyAsync(n->d_t, target, sizeof(float) * (size_t)ny, cudaMemcpyHostToDevice, n->stream));
     forward(n);
     const int nb = 120;
-    k_mse<<<nb, 256, 0, n->stream>>>(ny, n->d_y, n->d_t, n->d_dy, n->d_partial);
-    n->launches++;
+    if (n->gate_B) {
+        k_mse<<<nb, 256, 0, n->stream>>>(ny, n->d_yg, n->d_t, n->d_dyg, n->d_partial);
+        const int64_t tot = (int64_t)n->n_nodes * n->O;
+        k_gate_back<<<(int)std::min<int64_t>((tot + 255) / 256, 4096), 256, 0, n->stream>>>(
+            n->n_nodes, n->gate_nd, n->gate_B, n->F, n->d_dyg, n->d_x, n->d_dy);
+        n->launches += 2;
+    } else {
+        k_mse<<<nb, 256, 0, n->stream>>>(ny, n->d_y, n->d_t, n->d_dy, n->d_partial);
+        n->launches++;
+    }
     backward(n);
     LYMPH_CUDA_TRY(cudaGetLastError());
     double part[nb];
@@ -618,6 +760,22 @@ int lymph_mpnn_loss_grad(lymph_mpnn* n, const float* x, const float* target, dou
         for (int i = 0; i < nb; ++i) s += part[i];
         *loss = s / (double)ny;
     }
+    return LYMPH_OK;
+}
+
+// Switches the output head to the gated form over the first B feature blocks
+// of nd DOFs each (nd = 3 Np): O must be 2 * B * 3 and F >= B * nd.  The
+// effective output (forward, loss target) then has 2 * nd columns.
+int lymph_mpnn_set_gate(lymph_mpnn* n, int32_t nd, int32_t B) {
+    if (!n || nd <= 0 || nd % 3 || B <= 0 || n->O != 2 * B * 3 || n->F < B * nd) {
+        lymph_set_error("lymph_mpnn_set_gate: need nd % 3 == 0, O == 6 B and F >= B nd");
+        return LYMPH_ERR_INVALID;
+    }
+    n->gate_nd = nd;
+    n->gate_B = B;
+    const int N = n->n_cap;
+    n->n_cap = 0;  // re-size the activations for the new output width
+    if (N > 0) LYMPH_TRY(ensure_capacity(n, N));
     return LYMPH_OK;
 }
 
@@ -639,54 +797,120 @@ int lymph_mpnn_launch_count(const lymph_mpnn* n, int64_t* count) {
     return LYMPH_OK;
 }
 
+}  // extern "C"
 
-// One surrogate block on a context whose slots hold V0 = u^{n-1},
-// U0 = u^n, UN = u^{n+1}: builds the features on the device, runs the
-// network (use_net = 0: the baseline extrapolation alone), saves u^n into V0
-// and u^{n+1} into UEX (for a fallback), and writes the predicted
-// u^{n+K-1}, u^{n+K} into U0, UN.  scales (nullable, 3 doubles) receives the
-// RMS of u1, d1, d2.
-int lymph_surrogate_predict(lymph_ctx* c, lymph_mpnn* n, int32_t K, int32_t use_net, double* scales) {
-    if (!c || !n || K < 4) return LYMPH_ERR_INVALID;
+namespace {
+
+// Shared front of a surrogate block on a context with V0 = u^{n-1},
+// U0 = u^n, UN = u^{n+1}: d1, d2, a1 = dt^2 M^-1 (K d1 - gdiff F_dyn) and
+// their sums of squares (ss[0..3]: u1, d1, d2, a1) into the network's
+// scratch; with_features also the feature rows in d_x.  gdiff is the source
+// time function's increment g(t_{n+1}) - g(t_n).
+int surrogate_front(lymph_ctx* c, lymph_mpnn* n, bool with_features, double gdiff, const char* who) {
     const int nd = c->nd;
-    if (use_net && (n->F < 3 * nd + 5 || n->O != 2 * nd)) {
-        lymph_set_error("lymph_surrogate_predict: network shape does not match the problem (F >= 3*3Np+5, O = 2*3Np)");
+    if (with_features && (n->F < 4 * nd + 7 || eff_width(n) != 2 * nd || (n->gate_B && n->gate_nd != nd))) {
+        lymph_set_error(std::string(who) + ": network shape does not match the problem (F >= 4*3Np+7, output 2*3Np)");
         return LYMPH_ERR_INVALID;
     }
-    if (use_net && n->n_nodes != c->n_poly) {
-        lymph_set_error("lymph_surrogate_predict: set the network's graph for this mesh first");
+    if (with_features && n->n_nodes != c->n_poly) {
+        lymph_set_error(std::string(who) + ": set the network's graph for this mesh first");
+        return LYMPH_ERR_ORDER;
+    }
+    if (!c->have_matrices) {
+        lymph_set_error(std::string(who) + ": call lymph_make_matrices first");
         return LYMPH_ERR_ORDER;
     }
     const int64_t nv = (int64_t)c->n_poly * nd;
     if (nv > n->nv_cap) {  // scratch grows once per (network, largest mesh) and is kept
-        for (double** p : {&n->d_d1, &n->d_d2, &n->d_ss, &n->d_u3})
+        for (double** p : {&n->d_d1, &n->d_d2, &n->d_ss, &n->d_u3, &n->d_a1, &n->d_sig})
             if (*p) { cudaFree(*p); *p = nullptr; }
         n->nv_cap = 0;
-        if (cudaMalloc(&n->d_d1, sizeof(double) * nv) != cudaSuccess ||
+        if (cudaMalloc(&n->d_sig, sizeof(double) * 4 * (size_t)c->n_poly) != cudaSuccess ||
+            cudaMalloc(&n->d_d1, sizeof(double) * nv) != cudaSuccess ||
             cudaMalloc(&n->d_d2, sizeof(double) * nv) != cudaSuccess ||
             cudaMalloc(&n->d_u3, sizeof(double) * nv) != cudaSuccess ||
+            cudaMalloc(&n->d_a1, sizeof(double) * nv) != cudaSuccess ||
             cudaMalloc(&n->d_ss, sizeof(double) * (6 * SS_BLOCKS + 6)) != cudaSuccess) {
-            lymph_set_error("lymph_surrogate_predict: out of memory");
+            lymph_set_error(std::string(who) + ": out of memory");
             return LYMPH_ERR_OOM;
         }
         n->nv_cap = nv;
     }
-    double *d1 = n->d_d1, *d2 = n->d_d2, *ss = n->d_ss, *part = n->d_ss + 6;
-    double* um = c->d_v0;
-    double* u0 = lymph_slot_ptr(c, LYMPH_SLOT_U0);
-    double* u1 = lymph_slot_ptr(c, LYMPH_SLOT_UN);
     cudaStream_t st = c->stream;
     // the network's own work is ordered before this block; its forward then
     // runs on the context's stream, so the block needs no host round trip
     LYMPH_CUDA_TRY(cudaStreamSynchronize(n->stream));
-    k_diffs_sumsq<<<SS_BLOCKS, 256, 0, st>>>(nv, um, u0, u1, d1, d2, part);
+    double *ss = n->d_ss, *part = n->d_ss + 6;
+    k_diffs_sumsq<<<SS_BLOCKS, 256, 0, st>>>(nv, c->d_v0, lymph_slot_ptr(c, LYMPH_SLOT_U0),
+                                             lymph_slot_ptr(c, LYMPH_SLOT_UN), n->d_d1, n->d_d2, part);
     k_sum3<<<1, 96, 0, st>>>(SS_BLOCKS, part, ss);
     c->launches += 2;
-    int rc = LYMPH_OK;
-    if (use_net) {
-        k_features<<<c->n_poly, 128, 0, st>>>(c->n_poly, nd, n->F, u1, d1, d2, ss, nv, c->d_poly_ptr, c->d_poly_tets,
-                                             c->d_tet_mat, c->d_mat, n->d_x);
+    LYMPH_TRY(lymph_dev_apply(c, n->d_d1, n->d_a1));
+    k_minv_rhs<<<1024, 256, 0, st>>>(c->n_poly, c->Np, c->d_Minv, c->d_rhs_dyn, n->d_u3);  // u3: free until k_predict
+    k_accel_combine<<<1024, 256, 0, st>>>(nv, c->dt * c->dt, gdiff, n->d_u3, n->d_a1);
+    k_one_sumsq<<<SS_BLOCKS, 256, 0, st>>>(nv, n->d_a1, part);
+    k_sum3<<<1, 96, 0, st>>>(SS_BLOCKS, part, ss + 3);  // ss[3] (ss[4], ss[5] get zeros)
+    c->launches += 4;
+    if (with_features) {
+        k_features<<<c->n_poly, FEAT_THREADS, 0, st>>>(c->n_poly, nd, n->F, lymph_slot_ptr(c, LYMPH_SLOT_UN),
+                                                      n->d_d1, n->d_d2, n->d_a1, ss, nv, c->d_poly_ptr,
+                                                      c->d_poly_tets, c->d_tet_mat, c->d_mat, n->d_x, n->d_sig);
         c->launches++;
+    }
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+int read_scales(lymph_ctx* c, lymph_mpnn* n, double* scales, int count) {
+    double t[4];
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(t, n->d_ss, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const double nv = (double)c->n_poly * c->nd;
+    for (int i = 0; i < count; ++i) scales[i] = std::sqrt(t[i] / nv);
+    return LYMPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// The features of a block, built on the device exactly as
+// lymph_surrogate_predict builds them, copied to x (host, n_poly x F
+// floats); scales (nullable, 4 doubles) receives the mesh-wide RMS s1..s4,
+// a1 (nullable, n_poly x 3Np doubles) the operator term and sig (nullable,
+// n_poly x 4 doubles) the per-polyhedron scales.  Used to make training
+// samples from solver runs.
+int lymph_surrogate_features(lymph_ctx* c, lymph_mpnn* n, double gdiff, float* x, double* scales, double* a1,
+                             double* sig) {
+    if (!c || !n || !x) return LYMPH_ERR_INVALID;
+    LYMPH_TRY(surrogate_front(c, n, true, gdiff, "lymph_surrogate_features"));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(x, n->d_x, sizeof(float) * (size_t)c->n_poly * n->F, cudaMemcpyDeviceToHost,
+                                   c->stream));
+    if (a1)
+        LYMPH_CUDA_TRY(cudaMemcpyAsync(a1, n->d_a1, sizeof(double) * (size_t)c->n_poly * c->nd,
+                                       cudaMemcpyDeviceToHost, c->stream));
+    if (sig)
+        LYMPH_CUDA_TRY(cudaMemcpyAsync(sig, n->d_sig, sizeof(double) * 4 * (size_t)c->n_poly, cudaMemcpyDeviceToHost,
+                                       c->stream));
+    if (scales) LYMPH_TRY(read_scales(c, n, scales, 4));
+    return lymph_sync_status(c, "lymph_surrogate_features");
+}
+
+// One surrogate block on a context whose slots hold V0 = u^{n-1},
+// U0 = u^n, UN = u^{n+1}: builds the features on the device, runs the
+// network (use_net = 0: the extrapolation alone), saves u^n into V0 and
+// u^{n+1} into UEX (for a fallback), and writes the predicted u^{n+K-2},
+// u^{n+K-1} into U0, UN and u^{n+K} into the network's scratch.  scales
+// (nullable, 4 doubles) receives the RMS of u1, d1, d2, a1.
+int lymph_surrogate_predict(lymph_ctx* c, lymph_mpnn* n, int32_t K, int32_t use_net, double gdiff, double* scales) {
+    if (!c || !n || K < 4) return LYMPH_ERR_INVALID;
+    LYMPH_TRY(surrogate_front(c, n, use_net != 0, gdiff, "lymph_surrogate_predict"));
+    const int nd = c->nd;
+    const int64_t nv = (int64_t)c->n_poly * nd;
+    cudaStream_t st = c->stream;
+    double* u0 = lymph_slot_ptr(c, LYMPH_SLOT_U0);
+    double* u1 = lymph_slot_ptr(c, LYMPH_SLOT_UN);
+    if (use_net) {
         cudaStream_t own = n->stream;
         n->stream = st;
         const int64_t before = n->launches;
@@ -694,21 +918,14 @@ int lymph_surrogate_predict(lymph_ctx* c, lymph_mpnn* n, int32_t K, int32_t use_
         c->launches += n->launches - before;
         n->stream = own;
     }
-    if (rc == LYMPH_OK) {
-        // keep u^n, u^{n+1} for a fallback, then overwrite U0/UN with the prediction
-        cudaMemcpyAsync(c->d_v0, u0, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(c->d_uex, u1, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st);
-        k_predict<<<1024, 256, 0, st>>>(nv, nd, K, c->d_uex, d1, d2, ss, nv, n->d_y, use_net, u0, u1, n->d_u3);
-        c->launches++;
-        if (scales) {
-            double t[3];
-            cudaMemcpyAsync(t, ss, sizeof(t), cudaMemcpyDeviceToHost, st);
-            cudaStreamSynchronize(st);
-            for (int i = 0; i < 3; ++i) scales[i] = std::sqrt(t[i] / (double)nv);
-        }
-        if (cudaStreamSynchronize(st) != cudaSuccess) rc = LYMPH_ERR_CUDA;
-    }
-    if (rc != LYMPH_OK) { lymph_set_error("lymph_surrogate_predict: CUDA error"); return rc; }
+    // keep u^n, u^{n+1} for a fallback, then overwrite U0/UN with the prediction
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(c->d_v0, u0, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(c->d_uex, u1, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st));
+    k_predict<<<1024, 256, 0, st>>>(nv, nd, K, c->d_uex, n->d_d1, n->d_d2, n->d_a1, n->d_sig, eff_out(n), use_net,
+                                    u0, u1, n->d_u3);
+    c->launches++;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    if (scales) LYMPH_TRY(read_scales(c, n, scales, 4));
     n->have_u3 = c;
     return lymph_sync_status(c, "lymph_surrogate_predict");
 }

@@ -43,7 +43,8 @@ G_FEATURES = 8
 
 
 def feature_width(nd: int) -> int:
-    return ((3 * nd + 5 + 15) // 16) * 16
+    """Feature columns for 3Np = nd: 4 nd + 7, rounded up to 16."""
+    return ((4 * nd + 7 + 15) // 16) * 16
 
 
 # ---------------------------------------------------------------------------
@@ -113,64 +114,69 @@ def poly_material(mesh: M.Mesh) -> np.ndarray:
     return mesh.mat[mesh.tet_mat[first]]
 
 
-def features(um, u0, u1, mat, F):
-    """The device's k_features in numpy (float64 arithmetic, float32 out)."""
+def features(um, u0, u1, a1, mat, F):
+    """The device's k_features in numpy (float64 arithmetic, float32 out);
+    a1 = dt^2 M^-1 (K d1 - gdiff F).  Returns (x, mesh-wide RMS s1..s4,
+    per-polyhedron scales r [N, 4], d1, d2)."""
     d1 = u1 - u0
     d2 = (u1 - 2.0 * u0) + um
+    vecs = (u1, d1, d2, a1)
     n = u1.size
-    s1 = math.sqrt(float(np.sum(u1 * u1)) / n) + 1e-300
-    s2 = math.sqrt(float(np.sum(d1 * d1)) / n) + 1e-300
-    s3 = math.sqrt(float(np.sum(d2 * d2)) / n) + 1e-300
     N, nd = u1.shape
+    s = [math.sqrt(float(np.sum(v * v)) / n) for v in vecs]
+    r = np.stack([np.sqrt(np.sum(v * v, axis=1) / nd) + 1e-3 * sg + 1e-300 for v, sg in zip(vecs, s)], axis=1)
     x = np.zeros((N, F))
-    x[:, :nd] = u1 / s1
-    x[:, nd:2 * nd] = d1 / s2
-    x[:, 2 * nd:3 * nd] = d2 / s3
-    x[:, 3 * nd] = math.log10(s2 / s1)
-    x[:, 3 * nd + 1] = math.log10(s3 / s2)
-    x[:, 3 * nd + 2:3 * nd + 5] = mat[:, [1, 2, 0]]
-    return x.astype(np.float32), (s1, s2, s3), d1, d2
+    for b, v in enumerate(vecs):
+        x[:, b * nd:(b + 1) * nd] = v / r[:, b:b + 1]
+    x[:, 4 * nd] = np.log10(r[:, 1] / r[:, 0])
+    x[:, 4 * nd + 1] = np.log10(r[:, 2] / r[:, 1])
+    x[:, 4 * nd + 2] = np.log10(r[:, 3] / r[:, 2])
+    x[:, 4 * nd + 3] = np.log10(r[:, 0] / (s[0] + 1e-300))
+    x[:, 4 * nd + 4:4 * nd + 7] = mat[:, [1, 2, 0]]
+    return x.astype(np.float32), tuple(s), r, d1, d2
 
 
-def baseline(u1, d1, d2, k):
-    """Constant-second-difference extrapolation of u^{n+1+k}."""
-    return u1 + k * d1 + 0.5 * k * (k + 1.0) * d2
+def baseline(u1, d1, d2, a1, k):
+    """Cubic Taylor extrapolation of u^{n+1+k}: u1 + k d1 + k(k+1)/2 d2
+    - k(k+1)(k+2)/6 a1, with a1 = dt^2 M^-1 (K d1 - gdiff F) ~ -d3."""
+    return u1 + k * d1 + 0.5 * k * (k + 1.0) * d2 - (k * (k + 1.0) * (k + 2.0) / 6.0) * a1
 
 
 def newton_phi(k, K):
-    """Newton basis of the extrapolation's cubic and quartic error terms."""
+    """Newton basis of the remaining cubic and quartic error terms."""
     p3 = k * (k + 1.0) * (k + 2.0) / float(K) ** 3
     return p3, p3 * (k + 3.0) / K
 
 
-def corr_scale(s2, s3, K):
-    """(s3^2 / s2) K^3 / 6: s3/s2 ~ omega dt, so the coefficients are O(1)."""
-    return (s3 * s3 / s2) * K ** 3 / 6.0
+def corr_scale(sig, K):
+    """Per-polyhedron (r4^2 / r3) K^4 / 24 as a column [N, 1]: r4/r3 ~ omega dt,
+    so the coefficients are O(1)."""
+    return ((sig[:, 3] ** 2 / sig[:, 2]) * K ** 4 / 24.0)[:, None]
 
 
 PRED_K = lambda K: (K - 3, K - 2, K - 1)  # noqa: E731  (offsets of the three predicted states)
 
 
-def targets(u1, d1, d2, s2, s3, K, later):
+def targets(u1, d1, d2, a1, sig, K, later):
     """Least-squares Newton coefficients [y3 | y4] of the extrapolation error
     over u^{n+1+k}, k = 1..K-1 (later[k-1] = u^{n+1+k})."""
     ks = np.arange(1, K, dtype=np.float64)
     Phi = np.stack(newton_phi(ks, K), axis=1)  # [K-1, 2]
     pinv = np.linalg.pinv(Phi)  # [2, K-1]
-    sc = corr_scale(s2, s3, K)
-    E = np.stack([(later[k - 1] - baseline(u1, d1, d2, k)) / sc for k in range(1, K)], axis=0)  # [K-1, N, nd]
+    sc = corr_scale(sig, K)
+    E = np.stack([(later[k - 1] - baseline(u1, d1, d2, a1, k)) / sc for k in range(1, K)], axis=0)
     y = np.tensordot(pinv, E, axes=(1, 0))  # [2, N, nd]
     return np.concatenate([y[0], y[1]], axis=1).astype(np.float32)
 
 
-def predict_states(u1, d1, d2, s2, s3, K, y):
+def predict_states(u1, d1, d2, a1, sig, K, y):
     """The three predicted states of a block from coefficients y = [y3 | y4]."""
     nd = u1.shape[1]
-    sc = corr_scale(s2, s3, K)
+    sc = corr_scale(sig, K)
     out = []
     for k in PRED_K(K):
         p3, p4 = newton_phi(float(k), K)
-        out.append(baseline(u1, d1, d2, k) + sc * (y[:, :nd] * p3 + y[:, nd:] * p4))
+        out.append(baseline(u1, d1, d2, a1, k) + sc * (y[:, :nd] * p3 + y[:, nd:] * p4))
     return out
 
 
@@ -178,15 +184,21 @@ def predict_states(u1, d1, d2, s2, s3, K, y):
 # network handle
 # ---------------------------------------------------------------------------
 class MPNN:
-    """The CUDA network (lymph_mpnn_*)."""
+    """The CUDA network (lymph_mpnn_*).  gate = (nd, B) switches to the gated
+    head: O = 6 B per-node coefficients over the first B feature blocks of nd
+    DOFs, effective output width 2 nd."""
 
-    def __init__(self, F: int, O: int, H: int = 256, L: int = 3, G: int = G_FEATURES, seed: int = 0):
+    def __init__(self, F: int, O: int, H: int = 256, L: int = 3, G: int = G_FEATURES, seed: int = 0, gate=None):
         self.lib = _lib.load()
         self.F, self.O, self.H, self.L, self.G = F, O, H, L, G
+        self.gate = gate
+        self.out_width = 2 * gate[0] if gate else O
         h = c_void_p()
         check(self.lib.lymph_mpnn_create(F, H, O, L, G, byref(h)), "lymph_mpnn_create")
         self.h = h
         self.n_par = self.lib.lymph_mpnn_num_params(h)
+        if gate:
+            check(self.lib.lymph_mpnn_set_gate(h, gate[0], gate[1]), "lymph_mpnn_set_gate")
         self.set_params(self.init_params(seed))
         self.graph_key = None
 
@@ -240,7 +252,7 @@ class MPNN:
 
     def forward(self, x):
         x = np.ascontiguousarray(x, np.float32)
-        y = np.empty((x.shape[0], self.O), np.float32)
+        y = np.empty((x.shape[0], self.out_width), np.float32)
         check(self.lib.lymph_mpnn_forward(self.h, ptr(x, c_float), ptr(y, c_float)), "lymph_mpnn_forward")
         return y
 
@@ -274,24 +286,42 @@ class MPNN:
 # ---------------------------------------------------------------------------
 # training data from the solver
 # ---------------------------------------------------------------------------
-def solver_samples(seed: int, K: int, F: int, p: int = 3, n: int = 5, steps: int | None = None, every: int = 32,
+def device_features(s: MatrixFree, net: MPNN, gdiff: float = 0.0):
+    """Feature rows of the block whose V0, U0, UN the context holds, built
+    on the device (lymph_surrogate_features); returns
+    (x, mesh-wide RMS (s1, s2, s3, s4), a1, per-polyhedron scales [N, 4])."""
+    x = np.empty((s.n_poly, net.F), np.float32)
+    a1 = np.empty((s.n_poly, s.nd), np.float64)
+    sig = np.empty((s.n_poly, 4), np.float64)
+    sc = (c_double * 4)()
+    check(s.lib.lymph_surrogate_features(s.ctx, net.h, gdiff, ptr(x, c_float), sc, ptr(a1, c_double),
+                                         ptr(sig, c_double)), "lymph_surrogate_features")
+    return x, tuple(sc), a1, sig
+
+
+def solver_samples(seed: int, K: int, net: MPNN, p: int = 3, n: int = 5, steps: int | None = None, every: int = 32,
                    start: int = 40, cfl: float | None = None, f_dt: float | None = None, lognormal: bool = True,
-                   keep_truth: bool = False):
+                   keep_truth: bool = False, t0_cycles: float = 2.0):
     """Training or evaluation samples from one solver run from rest on a small
     seeded mesh: homogeneous Dirichlet, BFS polyhedra of 4-16 tets,
-    lognormal lambda and mu, a Ricker point source (t0 = 1.2/f0) at a random
-    point and direction, dt = cfl x 2/sqrt(lambda_max) and f0 = f_dt / dt
-    (f_dt = source cycles per step; both drawn from the seed when None).
-    The run lasts `steps` (default 2.6/f_dt, the whole pulse); a sample is
-    taken every `every` steps.  Returns (samples, graph, material, meta)."""
+    lognormal lambda and mu, a Ricker point source centred at
+    t0 = t0_cycles / f0 (2 cycles: the source starts smoothly from zero) at a
+    random point and direction, dt = cfl x 2/sqrt(lambda_max) and
+    f0 = f_dt / dt (f_dt = source cycles per step; cfl and f_dt drawn from
+    the seed when None).  The run lasts `steps` (default: until the pulse
+    has passed); a sample is taken every `every` steps, its features built
+    on the device by the network handle `net` (its graph is set to this
+    mesh).  Returns (samples, graph, material, meta)."""
     rng = np.random.default_rng(seed)
     cfl = float(rng.uniform(0.04, 0.15)) if cfl is None else cfl
     f_dt = float(rng.uniform(0.7e-3, 2e-3)) if f_dt is None else f_dt
-    steps = int(2.6 / f_dt) if steps is None else steps
+    steps = int((t0_cycles + 1.5) / f_dt) if steps is None else steps
     base = M.cube(n, bc="dirichlet", agglomeration="bfs", seed=seed, group=(4, 16))
     mats = M.lognormal_materials(base.n_poly, seed=seed) if lognormal else None
     m = M.cube(n, bc="dirichlet", agglomeration="bfs", seed=seed, group=(4, 16), poly_materials=mats)
     mat = poly_material(m)
+    graph = build_graph(m)
+    net.set_graph(graph, ("samples", seed, n))
     s = MatrixFree(m, p, 1.0)
     samples = []
     try:
@@ -305,28 +335,34 @@ def solver_samples(seed: int, K: int, F: int, p: int = 3, n: int = 5, steps: int
         E.point_source(s, x0, d / np.linalg.norm(d))
         s.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_DISPLACEMENT, _lib.SLOT_U0)  # zero at t = 0
         s.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_DISPLACEMENT, _lib.SLOT_V0)
-        gfun = lambda t: float(E.ricker(t, f0))  # noqa: E731
+        gfun = lambda t: float(E.ricker(t, f0, t0_cycles / f0))  # noqa: E731
         check(s.lib.lymph_first_step_g(s.ctx, gfun(0.0)), "first_step_g")
-        t = s.dt
-        win = {}
-        for i in range(1, steps):  # UN holds u^i
+        t, t_prev = s.dt, 0.0
+        win, x, sc, a1, sig = {}, None, None, None, None
+        for i in range(1, steps):  # UN holds u^i at time t
             r = (i - (start - 1)) % every
             if i >= start - 1 and r <= K + 1:
                 win[r] = s.get_state(_lib.SLOT_UN).copy()
-                if r == K + 1:
+                if r == 1:  # V0 = u^{n-1} for the features after the next step
+                    check(s.lib.lymph_copy_state(s.ctx, _lib.SLOT_V0, _lib.SLOT_U0), "copy")
+                elif r == 2:
+                    x, sc, a1, sig = device_features(s, net, gfun(t) - gfun(t_prev))
+                elif r == K + 1:
                     um, u0, u1 = win[0], win[1], win[2]
-                    x, (s1, s2, s3), d1, d2 = features(um, u0, u1, mat, F)
-                    if s2 > 1e-280 and s3 > 1e-280:
+                    d1 = u1 - u0
+                    d2 = (u1 - 2.0 * u0) + um
+                    if sc[2] > 1e-280 and sc[3] > 1e-280:
                         later = [win[2 + k] for k in range(1, K)]
-                        tgt = targets(u1, d1, d2, s2, s3, K, later)
-                        aux = (u1, d1, d2, s2, s3, [win[2 + k] for k in PRED_K(K)]) if keep_truth else None
+                        tgt = targets(u1, d1, d2, a1, sig, K, later)
+                        aux = (u1, d1, d2, a1, sig, [win[2 + k] for k in PRED_K(K)]) if keep_truth else None
                         samples.append((x, tgt, aux))
                     win = {}
             check(s.lib.lymph_step_g(s.ctx, gfun(t)), "step_g")
+            t_prev = t
             t += s.dt
     finally:
         s.close()
-    return samples, build_graph(m), mat, {"cfl": cfl, "f_dt": f_dt, "f0": f0, "steps": steps, "n_poly": m.n_poly}
+    return samples, graph, mat, {"cfl": cfl, "f_dt": f_dt, "f0": f0, "steps": steps, "n_poly": m.n_poly}
 
 
 def train(net: MPNN, datasets, iters: int, lr: float = 1e-3, seed: int = 0, log_every: int = 0):
@@ -353,9 +389,9 @@ def prediction_error(net: MPNN | None, graph, key, samples, K: int):
     errs = []
     if net is not None:
         net.set_graph(graph, key)
-    for x, t, (u1, d1, d2, s2, s3, truth) in samples:
+    for x, t, (u1, d1, d2, a1, sig, truth) in samples:
         y = net.forward(x).astype(np.float64) if net is not None else np.zeros(t.shape)
-        pred = predict_states(u1, d1, d2, s2, s3, K, y)
+        pred = predict_states(u1, d1, d2, a1, sig, K, y)
         errs.append(float(np.linalg.norm(np.concatenate(pred) - np.concatenate(truth)) /
                           np.linalg.norm(np.concatenate(truth))))
     return float(np.mean(errs))
@@ -413,7 +449,8 @@ def run_hybrid(s: MatrixFree, net: MPNN | None, n_steps: int, gfun, t: float, K:
         t0 = t
         check(s.lib.lymph_copy_state(s.ctx, _lib.SLOT_V0, _lib.SLOT_U0), "copy")
         t1 = run_plain(s, 1, gfun, t0)  # u^{n+1}
-        check(s.lib.lymph_surrogate_predict(s.ctx, hnet, K, int(use_net), None), "surrogate_predict")
+        gdiff = gfun(t1) - gfun(t0)
+        check(s.lib.lymph_surrogate_predict(s.ctx, hnet, K, int(use_net), gdiff, None), "surrogate_predict")
         tpred = t1
         for _ in range(K - 2):
             tpred += s.dt  # time of the predicted u^{n+K-1}
@@ -463,6 +500,49 @@ def run_hybrid(s: MatrixFree, net: MPNN | None, n_steps: int, gfun, t: float, K:
 
 
 _DUMMY = None
+
+
+def training_sets(net: MPNN, p: int, n_traj: int, K: int = 8, seed0: int = 0, every: int = 32, sizes=(4, 5, 6)):
+    """Samples of n_traj solver runs (seeds seed0.., meshes n^3 x 6 with n
+    cycling through `sizes`; larger meshes are sampled every 2 x `every`)."""
+    sets = []
+    for sd in range(seed0, seed0 + n_traj):
+        n = sizes[sd % len(sizes)]
+        sm, gr, _, _ = solver_samples(sd, K, net, p=p, n=n, every=every if n <= 6 else 2 * every)
+        if sm:
+            sets.append((gr, sm, ("train", p, sd)))
+    return sets
+
+
+def held_out_errors(net: MPNN, p: int, seeds=(100, 101, 102, 103), K: int = 8, every: int = 64):
+    """(network, extrapolation-only) mean relative errors of the predicted
+    states on solver runs the network was not trained on."""
+    out = []
+    for sd in seeds:
+        sm, gr, _, _ = solver_samples(sd, K, net, p=p, n=4 + sd % 3, every=every, keep_truth=True)
+        key = ("held", p, sd)
+        out.append((prediction_error(net, gr, key, sm, K), prediction_error(None, gr, key, sm, K)))
+    return out
+
+
+def train_surrogate(p: int, n_traj: int = 200, iters: int = 20000, H: int = 256, L: int = 3, lr: float = 1e-3,
+                    K: int = 8, seed: int = 0, sizes=(4, 5, 6)):
+    """Builds the network for degree p and trains it on the GPU on n_traj
+    runs of the solver.  Returns (net, loss history, seconds for data,
+    seconds for training)."""
+    net = surrogate_net(p, H=H, L=L, seed=seed)
+    t0 = time.perf_counter()
+    sets = training_sets(net, p, n_traj, K, sizes=sizes)
+    t1 = time.perf_counter()
+    hist = train(net, sets, iters, lr=lr, seed=seed)
+    return net, hist, t1 - t0, time.perf_counter() - t1
+
+
+def surrogate_net(p: int, H: int = 256, L: int = 3, seed: int = 0) -> MPNN:
+    """The surrogate's network for degree p: gated head over the four
+    feature blocks [u1, d1, d2, a1] (24 outputs per polyhedron)."""
+    nd = 3 * (p + 1) * (p + 2) * (p + 3) // 6
+    return MPNN(feature_width(nd), 6 * 4, H=H, L=L, seed=seed, gate=(nd, 4))
 
 
 def _dummy_net():

@@ -51,3 +51,30 @@ def test_bf16_round_ties_to_even():
     assert got[2] == 1.0 + 4 * 2.0 ** -8      # tie -> even (rounds up)
     assert got[3] == -2.5
     assert got[4] == 1.0
+
+
+def test_gated_backward_matches_finite_differences():
+    rng = np.random.default_rng(3)
+    Np, B = 2, 2
+    nd = 3 * Np
+    F, H, L, G, N = B * nd + 3, 6, 1, 3, 10
+    O = 6 * B
+    params = R.init_params(F, H, O, L, G, seed=4)
+    for k in params:
+        if k.startswith("b"):
+            params[k] = rng.standard_normal(params[k].shape) * 0.1
+    graph = _graph(N, rng, G)
+    x = rng.standard_normal((N, F))
+    t = rng.standard_normal((N, 2 * nd))
+    assert R.finite_difference_check(params, x, graph, t, L, n_probe=8, eps=1e-4, gate=(nd, B)) <= 1e-5
+
+
+def test_gate_adjoint():
+    rng = np.random.default_rng(5)
+    nd, B, N = 9, 3, 4
+    x = rng.standard_normal((N, B * nd + 2))
+    y = rng.standard_normal((N, 6 * B))
+    g = rng.standard_normal((N, 2 * nd))
+    lhs = np.sum(R.gate_apply(y, x, nd, B) * g)
+    rhs = np.sum(y * R.gate_adjoint(g, x, nd, B))
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)
