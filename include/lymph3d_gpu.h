@@ -303,6 +303,13 @@ int lymph_surrogate_residual(lymph_ctx* ctx, lymph_mpnn* net, double* residual);
  * lymph_surrogate_predict (they share the scratch). */
 int lymph_surrogate_judge(lymph_ctx* ctx, lymph_mpnn* net, int32_t phase, double* rel);
 
+/* Nodal values of the field in `slot` at the four vertices of every
+ * tetrahedron, out (host) [n_tet][4][3]: the reference's u_nod_vet(DIM, 4,
+ * num_elem_loc) in the same memory order.  Replaces the evaluation loop of
+ * EXPORT_SOLUTION (solution_processing.f90:62-194); the VTK / VTU / PVD
+ * writers of export_file_formats.f90 are host code (export.py). */
+int lymph_nodal_values(lymph_ctx* ctx, int slot, double* out);
+
 /* Aliases with the names the project specification uses for the two error
  * routines (COMPUTE_ERROR_L2_FREE / COMPUTE_ERROR_DG_FREE). */
 int lymph_compute_error_l2_free(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
@@ -334,6 +341,19 @@ int lymph_get_poly_geometry(lymph_ctx* ctx, double* bbox, double* hk);
  * src/matrix_free.f90:602-664, modelled on FIND_ELEM_FROM_POINT,
  * src/find_tet.f90:82-124, for the point lookup). */
 int lymph_make_rhs_point(lymph_ctx* ctx, int which, int32_t tet, const double* x0, const double* dir);
+
+/* Double-couple seismic source, the loop over PolyData%val_sism_el of
+ * MAKE_RHS_FREE (matrix_free.f90:602-664) with MAKE_DOUBLE_COUPLE
+ * (assemble_element.f90:116-167) and moment_density
+ * (problem_data_and_properties.f90:317-335): ADDS to RHS `which`
+ * (LYMPH_RHS_STAT / _DYN) the load int_T M : grad(phi) over tetrahedron
+ * `tet` (find it with lymph_mesh_find_tet), M = (s n^T + n s^T) M0 / |T|,
+ * s the strike vector, n the fault normal.  Each call takes its own s, n
+ * and M0 (the reference reads the first source's for every source,
+ * matrix_free.f90:647-652).  Call after MAKE_RHS_FREE, which zeroes the
+ * vector; the reference adds the couple before the forcing terms, so the
+ * source polyhedron's entries differ from it by rounding. */
+int lymph_make_rhs_double_couple(lymph_ctx* ctx, int which, int32_t tet, const double* s, const double* n, double M0);
 
 /* Time step after creation (e.g. from a CFL bound). */
 int lymph_set_dt(lymph_ctx* ctx, double dt);

@@ -99,6 +99,7 @@ _SIGS = {
     "lymph_get_rhs": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_get_poly_geometry": (c_int, [c_void_p, P_F64, P_F64]),
     "lymph_make_rhs_point": (c_int, [c_void_p, c_int, c_int32, P_F64, P_F64]),
+    "lymph_make_rhs_double_couple": (c_int, [c_void_p, c_int, c_int32, P_F64, P_F64, c_double]),
     "lymph_set_dt": (c_int, [c_void_p, c_double]),
     "lymph_get_dt": (c_int, [c_void_p, P_F64]),
     "lymph_max_eigenvalue": (c_int, [c_void_p, c_int32, P_F64]),
@@ -120,6 +121,7 @@ _SIGS = {
     "lymph_mpnn_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_surrogate_predict": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_double, P_F64]),
     "lymph_surrogate_residual": (c_int, [c_void_p, c_void_p, P_F64]),
+    "lymph_nodal_values": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_mpnn_set_gate": (c_int, [c_void_p, c_int32, c_int32]),
     "lymph_surrogate_features": (c_int, [c_void_p, c_void_p, c_double, POINTER(c_float), P_F64, P_F64, P_F64]),
     "lymph_surrogate_judge": (c_int, [c_void_p, c_void_p, c_int32, P_F64]),

@@ -24,6 +24,7 @@ int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double s
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
 int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);
+int lymph_dev_double_couple(lymph_ctx* c, int t, int P, const double moment[9], double* out);
 int lymph_dev_power_iteration(lymph_ctx* c, double* x, double* y, double* d_ss, int iters);
 int lymph_dev_point_source(lymph_ctx* c, int P, const double x0[3], const double dir[3], double* out);
 int lymph_dev_bump(lymph_ctx* c);
@@ -698,6 +699,48 @@ int lymph_make_rhs_point(lymph_ctx* c, int which, int32_t tet, const double* x0,
     double* out = (which == LYMPH_RHS_STAT) ? c->d_rhs_stat : c->d_rhs_dyn;
     LYMPH_TRY(lymph_dev_point_source(c, P, x0, dir, out));
     LYMPH_TRY(lymph_sync_status(c, "lymph_make_rhs_point"));
+    if (which == LYMPH_RHS_STAT) c->have_rhs_stat = true; else c->have_rhs_dyn = true;
+    return LYMPH_OK;
+}
+
+// Double-couple seismic source (matrix_free.f90:602-664): adds to RHS
+// `which` the moment-tensor load of tetrahedron `tet` with strike vector s,
+// fault normal n and moment magnitude M0, moment density
+// (s n^T + n s^T) M0 / V, V the tetrahedron's volume (find_tet.f90:184-210).
+int lymph_make_rhs_double_couple(lymph_ctx* c, int which, int32_t tet, const double* s, const double* n, double M0) {
+    if (!c || !s || !n || (which != LYMPH_RHS_STAT && which != LYMPH_RHS_DYN) || !std::isfinite(M0))
+        return LYMPH_ERR_INVALID;
+    if (tet < 0 || tet >= c->n_tet) {
+        lymph_set_error("lymph_make_rhs_double_couple: tetrahedron out of range");
+        return LYMPH_ERR_INVALID;
+    }
+    if (!c->have_matrices) {
+        lymph_set_error("lymph_make_rhs_double_couple: call lymph_make_matrices first");
+        return LYMPH_ERR_ORDER;
+    }
+    int32_t P = 0, tv[4];
+    LYMPH_CUDA_TRY(cudaMemcpy(&P, c->d_tet_poly + tet, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    LYMPH_CUDA_TRY(cudaMemcpy(tv, c->d_tet_vert + (size_t)tet * 4, sizeof(tv), cudaMemcpyDeviceToHost));
+    double X[4][3];
+    for (int v = 0; v < 4; ++v)
+        LYMPH_CUDA_TRY(cudaMemcpy(X[v], c->d_coords + (size_t)tv[v] * 3, sizeof(double) * 3, cudaMemcpyDeviceToHost));
+    // volume = |det [x_v 1]| / 6 (find_tet.f90:208), expanded along the ones column
+    double a[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 3; ++k) a[r][k] = X[r + 1][k] - X[0][k];
+    const double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                       a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+    const double vol = std::fabs(det) / 6.0;
+    if (!(vol > 0.0)) {
+        lymph_set_error("lymph_make_rhs_double_couple: degenerate tetrahedron");
+        return LYMPH_EXIT_ELEM_ORIENT;
+    }
+    double moment[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) moment[i * 3 + j] = (s[i] * n[j] + s[j] * n[i]) * M0 / vol;
+    double* out = (which == LYMPH_RHS_STAT) ? c->d_rhs_stat : c->d_rhs_dyn;
+    LYMPH_TRY(lymph_dev_double_couple(c, tet, P, moment, out));
+    LYMPH_TRY(lymph_sync_status(c, "lymph_make_rhs_double_couple"));
     if (which == LYMPH_RHS_STAT) c->have_rhs_stat = true; else c->have_rhs_dyn = true;
     return LYMPH_OK;
 }

@@ -699,6 +699,36 @@ __global__ void k_point_source(int Np, int P, const double* __restrict__ bbox, c
     rhs[base + 2 * Np + m] = dz * ph;
 }
 
+// Double-couple source on tetrahedron t of polyhedron P (one block of Np
+// threads, thread m): rhs[P][(i, m)] += sum_q w_q |J| sum_j moment(i, j)
+// dphi_j(m, x_q), the body of MAKE_DOUBLE_COUPLE
+// (assemble_element.f90:116-167) with the moment density
+// (s n^T + n s^T) M0 / V of problem_data_and_properties.f90:317-335, in the
+// reference's order (q outer, j inner).
+__global__ void k_double_couple(int Np, int nq3, int t, int P, const double* __restrict__ fk,
+                                const double* __restrict__ jdet, const double* __restrict__ bbox,
+                                const RefTables* __restrict__ ref, const double* __restrict__ moment, double* rhs) {
+    const int m = threadIdx.x;
+    if (m >= Np) return;
+    const double* F = fk + (int64_t)t * 12;
+    const double aj = fabs(jdet[t]);
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < nq3; ++q) {
+        const double* nq = &ref->nodtet3[q * 4];
+        double pt[3];
+        for (int a = 0; a < 3; ++a) pt[a] = F[a * 4 + 0] * nq[0] + F[a * 4 + 1] * nq[1] + F[a * 4 + 2] * nq[2] + F[a * 4 + 3];
+        double ph, dp[3];
+        basis_eval(pt, &bbox[P * 6], &ref->blist[m * 3], &ph, dp);
+        for (int i = 0; i < 3; ++i) {
+            double reduct = 0.0;
+            for (int j = 0; j < 3; ++j) reduct = reduct + moment[i * 3 + j] * dp[j];
+            acc[i] = acc[i] + ref->weitet3[q] * aj * reduct;
+        }
+    }
+    const int64_t base = (int64_t)P * 3 * Np;
+    for (int i = 0; i < 3; ++i) rhs[base + i * Np + m] += acc[i];
+}
+
 template <int PD>
 int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {
     size_t smem = asm_smem<PD>();
@@ -785,6 +815,24 @@ int lymph_dev_point_source(lymph_ctx* c, int P, const double x0[3], const double
     k_point_source<<<1, 64, 0, c->stream>>>(c->Np, P, c->d_bbox, c->d_ref, x0[0], x0[1], x0[2], dir[0], dir[1], dir[2], out);
     c->launches++;
     LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+int lymph_dev_double_couple(lymph_ctx* c, int t, int P, const double moment[9], double* out) {
+    double* d_m = nullptr;
+    LYMPH_CUDA_TRY(cudaMalloc(&d_m, sizeof(double) * 9));
+    cudaError_t e = cudaMemcpyAsync(d_m, moment, sizeof(double) * 9, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        k_double_couple<<<1, 64, 0, c->stream>>>(c->Np, c->nq3, t, P, c->d_fk, c->d_jdet, c->d_bbox, c->d_ref, d_m, out);
+        c->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_m);
+    if (e != cudaSuccess) {
+        lymph_set_error(std::string("lymph_dev_double_couple: ") + cudaGetErrorString(e));
+        return LYMPH_ERR_CUDA;
+    }
     return LYMPH_OK;
 }
 

@@ -66,6 +66,23 @@ def point_source(s: MatrixFree, x0, direction, which: int = _lib.RHS_DYN) -> int
     return tet.value
 
 
+def double_couple(s: MatrixFree, x0, strike, normal, M0: float, which: int = _lib.RHS_DYN) -> int:
+    """Adds the double-couple load of moment (s n^T + n s^T) M0 / |T| on the
+    tetrahedron T that contains x0 (lymph_make_rhs_double_couple)."""
+    m = s.mesh
+    tv = np.ascontiguousarray(m.tet_vert, dtype=np.int32)
+    X = np.ascontiguousarray(m.coords, dtype=np.float64)
+    x = np.ascontiguousarray(x0, dtype=np.float64)
+    sv = np.ascontiguousarray(strike, dtype=np.float64)
+    nv = np.ascontiguousarray(normal, dtype=np.float64)
+    tet = c_int32()
+    check(s.lib.lymph_mesh_find_tet(m.n_tet, ptr(tv, c_int32), ptr(X, c_double), ptr(x, c_double), byref(tet)),
+          "lymph_mesh_find_tet")
+    check(s.lib.lymph_make_rhs_double_couple(s.ctx, which, tet.value, ptr(sv, c_double), ptr(nv, c_double), M0),
+          "lymph_make_rhs_double_couple")
+    return tet.value
+
+
 class Batch:
     """Problems advanced together; each keeps its own context."""
 

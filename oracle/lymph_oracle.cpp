@@ -1194,6 +1194,85 @@ int oracle_error_dg(void* h, int s_uh, int s_uex, double* out) {
 // Pattern / blocks in the same convention as lymph_get_pattern/lymph_get_blocks
 // except for the neighbour order within a row (here: first appearance in the
 // tet/face loop).  n_blocks_out gets the total count when row_ptr is NULL.
+// det4 (vet_mat_operations.f90:52-69), cofactor expansion along row 1.
+double det4(const double A[4][4]) {
+    return A[0][0] * (A[1][1] * (A[2][2] * A[3][3] - A[2][3] * A[3][2]) - A[1][2] * (A[2][1] * A[3][3] - A[2][3] * A[3][1]) +
+                      A[1][3] * (A[2][1] * A[3][2] - A[2][2] * A[3][1])) -
+           A[0][1] * (A[1][0] * (A[2][2] * A[3][3] - A[2][3] * A[3][2]) - A[1][2] * (A[2][0] * A[3][3] - A[2][3] * A[3][0]) +
+                      A[1][3] * (A[2][0] * A[3][2] - A[2][2] * A[3][0])) +
+           A[0][2] * (A[1][0] * (A[2][1] * A[3][3] - A[2][3] * A[3][1]) - A[1][1] * (A[2][0] * A[3][3] - A[2][3] * A[3][0]) +
+                      A[1][3] * (A[2][0] * A[3][1] - A[2][1] * A[3][0])) -
+           A[0][3] * (A[1][0] * (A[2][1] * A[3][2] - A[2][2] * A[3][1]) - A[1][1] * (A[2][0] * A[3][2] - A[2][2] * A[3][0]) +
+                      A[1][2] * (A[2][0] * A[3][1] - A[2][1] * A[3][0]));
+}
+
+// The double-couple load of MAKE_RHS_FREE (matrix_free.f90:602-664): volume
+// (find_tet.f90:184-210), moment_density (problem_data_and_properties.f90:
+// 317-335), MAKE_DOUBLE_COUPLE (assemble_element.f90:116-167), added to the
+// rows of the polyhedron of tetrahedron t in RHS `which`.
+int oracle_make_rhs_double_couple(void* h, int which, int t, const double* sv, const double* nv, double M0) {
+    Oracle& o = *(Oracle*)h;
+    if (t < 0 || t >= o.n_tet || (which != 0 && which != 1)) return LYMPH_ERR_INVALID;
+    if (!o.have_matrices) return LYMPH_ERR_ORDER;
+    double A[4][4];
+    for (int v = 0; v < 4; ++v) {
+        for (int k = 0; k < 3; ++k) A[v][k] = o.coords[(size_t)o.tet_vert[t * 4 + v] * 3 + k];
+        A[v][3] = 1.0;
+    }
+    const double vol = std::fabs(det4(A)) / 6.0;
+    double moment[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) moment[i][j] = sv[i] * nv[j] + sv[j] * nv[i];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) moment[i][j] = moment[i][j] * M0 / vol;
+    const int P = o.tet_poly[t], Np = o.Np;
+    std::vector<double> phi, dphi;
+    basis_tet(o, t, P, phi, dphi);
+    std::vector<double> couple(3 * Np, 0.0);
+    const double aj = std::fabs(o.jdet[t]);
+    for (int q = 0; q < o.Q.nq3; ++q)
+        for (int m = 0; m < Np; ++m)
+            for (int i = 0; i < 3; ++i) {
+                double reduct = 0.0;
+                for (int j = 0; j < 3; ++j) reduct = reduct + moment[i][j] * dphi[q * 3 * Np + j * Np + m];
+                couple[i * Np + m] = couple[i * Np + m] + o.Q.weitet3[q] * aj * reduct;
+            }
+    std::vector<double>& rhs = which == 0 ? o.rhs_stat : o.rhs_dyn;
+    if (rhs.empty()) rhs.assign((size_t)o.n_poly * o.nd, 0.0);
+    for (int r = 0; r < 3 * Np; ++r) rhs[(size_t)P * o.nd + r] += couple[r];
+    return 0;
+}
+
+// EXPORT_SOLUTION's evaluation loop (solution_processing.f90:62-194):
+// out[t][v][k] = sum_i u(i, (k-1) Npoly + P) LegendreP_x LegendreP_y
+// LegendreP_z at the v-th vertex of tetrahedron t, summed in the reference's
+// order (temp = temp + u * valx * valy * valz, i = 1..Np).
+int oracle_nodal_values(void* h, int slot, double* out) {
+    Oracle& o = *(Oracle*)h;
+    if (slot < 0 || slot > 3) return LYMPH_ERR_INVALID;
+    const std::vector<double>& u = o.slot[slot];
+    if (o.bbox.empty() || u.empty()) return LYMPH_ERR_ORDER;
+    const int Np = o.Np, nd = o.nd;
+    for (int k = 0; k < 3; ++k)
+        for (int t = 0; t < o.n_tet; ++t) {
+            const int P = o.tet_poly[t];
+            double bb[3][2];
+            get_bb(o, P, bb);
+            for (int v = 0; v < 4; ++v) {
+                const double* x = &o.coords[(size_t)o.tet_vert[t * 4 + v] * 3];
+                double temp = 0.0;
+                for (int i = 0; i < Np; ++i) {
+                    const double vx = legendre(x[0], o.blist[i * 3 + 0], bb[0][0], bb[0][1]);
+                    const double vy = legendre(x[1], o.blist[i * 3 + 1], bb[1][0], bb[1][1]);
+                    const double vz = legendre(x[2], o.blist[i * 3 + 2], bb[2][0], bb[2][1]);
+                    temp = temp + u[(size_t)P * nd + k * Np + i] * vx * vy * vz;
+                }
+                out[((size_t)t * 4 + v) * 3 + k] = temp;
+            }
+        }
+    return 0;
+}
+
 int oracle_get_pattern(void* h, int32_t* row_ptr, int32_t* col, int64_t* n_blocks_out) {
     Oracle& o = *(Oracle*)h;
     int64_t nb = 0;

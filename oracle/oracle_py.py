@@ -48,6 +48,8 @@ def load():
             "oracle_step": (c_int, [c_void_p, c_double]),
             "oracle_run_steps": (c_int, [c_void_p, c_double, c_int64, P_F64, POINTER(c_int64)]),
             "oracle_get_state": (c_int, [c_void_p, c_int, P_F64]),
+            "oracle_nodal_values": (c_int, [c_void_p, c_int, P_F64]),
+            "oracle_make_rhs_double_couple": (c_int, [c_void_p, c_int, c_int, P_F64, P_F64, c_double]),
             "oracle_set_state": (c_int, [c_void_p, c_int, P_F64]),
             "oracle_error_l2": (c_int, [c_void_p, c_int, c_int, P_F64]),
             "oracle_error_dg": (c_int, [c_void_p, c_int, c_int, P_F64]),
@@ -95,6 +97,7 @@ class Oracle:
         self.Np = (degree + 1) * (degree + 2) * (degree + 3) // 6
         self.nd = 3 * self.Np
         self.n_poly = mesh.n_poly
+        self.n_tet = mesh.n_tet
 
     def close(self):
         if getattr(self, "h", None):
@@ -131,6 +134,20 @@ class Oracle:
         n = c_int64()
         self._chk(self.lib.oracle_run_steps(self.h, stop_time, max_steps, byref(tt), byref(n)), "run_steps")
         return tt.value, n.value
+
+    def make_rhs_double_couple(self, which, tet, strike, normal, M0):
+        sv = np.ascontiguousarray(strike, np.float64)
+        nv = np.ascontiguousarray(normal, np.float64)
+        self._chk(self.lib.oracle_make_rhs_double_couple(self.h, which, tet, _p(sv), _p(nv), M0),
+                  "make_rhs_double_couple")
+
+    def nodal_values(self, slot):
+        """EXPORT_SOLUTION's vertex evaluation: [n_tet, 4, 3]."""
+        out = np.empty((self.n_tet, 4, 3))
+        rc = self.lib.oracle_nodal_values(self.h, slot, _p(out))
+        if rc:
+            raise RuntimeError(f"oracle_nodal_values: {rc}")
+        return out
 
     def get_state(self, slot):
         out = np.empty((self.n_poly, self.nd))
