@@ -223,7 +223,7 @@ def prepare(cfg, precision):
 
 
 def step_bytes(g, precision):
-    es = 4 if precision == 1 else 8
+    es = {0: 8, 1: 4}[precision]
     nd, Np = g.nd, g.Np
     return g.n_blocks * nd * nd * es + g.n_poly * (3 * nd * 8 + 2 * Np * Np * 8 + 2 * nd * 8)
 
@@ -237,6 +237,10 @@ def errors(g, t):
     from lymph3d_apsc_gb300 import _lib, time_function
     g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_UEX, _lib.SLOT_UEX, time_function(t))
     return math.sqrt(g.COMPUTE_ERROR_L2_MATRIX_FREE()), math.sqrt(g.COMPUTE_ERROR_DG_MATRIX_FREE())
+
+
+ERROR_STEPS = 1000
+DTYPES = {0: "f64", 1: "f32-blocks/f64"}
 
 
 def run_gpu(cfg, precision, steps, warmup, rank_info, want_e2e=True):
@@ -256,10 +260,16 @@ def run_gpu(cfg, precision, steps, warmup, rank_info, want_e2e=True):
     out = {"dofs": dofs, "steps": n, "ms": ms, "kernel_ms_avg": mk / n2, "launches": launches,
            "clocks": clk.summary(), "n_blocks": g.n_blocks, "n_poly": g.n_poly, "n_tet": m.n_tet, "Np": g.Np,
            "bytes": step_bytes(g, precision), "flops": step_flops(g), "t": t}
+    # errors after ERROR_STEPS steps in all (the configurations' 1000-step
+    # runs), the same step count for every precision
+    done = 1 + nw + n + n2
+    if done < ERROR_STEPS:
+        t, _, _, _ = g.run_steps(t, 1e30, ERROR_STEPS - done)
+        done = ERROR_STEPS
+    out["err_L2"], out["err_DG"] = errors(g, t)
+    out["error_steps"], out["error_t"] = done, t
     if want_e2e:
         out["e2e"] = run_e2e(g, t, steps)
-        t = out["e2e"]["t"]
-    out["err_L2"], out["err_DG"] = errors(g, t)
     g.close()
     return out
 
@@ -458,7 +468,7 @@ def main():
         print(json.dumps(line), flush=True)
         return
 
-    precision = 1 if args.precision == "mixed" else 0
+    precision = {"fp64": 0, "mixed": 1}[args.precision]
     if cfg.get("surrogate"):
         if info["rank"] != 0:
             return
@@ -485,7 +495,7 @@ def main():
             degrees[m["p"]] = degrees.get(m["p"], 0) + 1
         line = {"metric": metric, "value": value, "unit": "DOF-steps/s", "n_gpus": 1, "steps": r["steps"],
                 "warmup": args.warmup, "ms_per_step": r["ms"] / r["steps"], "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f32-blocks/f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[precision],
                 "data": "synthetic (64 generated cube meshes, Ricker point sources)",
                 "config": {"workload": "64-problem ensemble: n^3x6 tets with n~U{8..32}, BFS groups 4-16, p~U{1..4}, "
                                        "Ricker f0~U[5,20] Hz, x0~U[0.2,0.8]^3, own CFL dt (0.8 x 2/sqrt(lambda_max))",
@@ -501,17 +511,17 @@ def main():
     value = total_dof_steps / (r["ms"] / 1e3)
     peak, peak_kind = measured_peaks()
     achieved = r["bytes"] / (r["kernel_ms_avg"] / 1e3) / 1e9
-    traffic = step_traffic_per_launch(args.config + ("_mixed" if precision else ""), r["n_blocks"])
+    traffic = step_traffic_per_launch(args.config + {0: "", 1: "_mixed"}[precision], r["n_blocks"])
     line = {
         "metric": metric, "value": value, "unit": "DOF-steps/s", "n_gpus": info["world"], "steps": r["steps"],
         "warmup": args.warmup, "ms_per_step": r["ms"] / r["steps"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == 0 else "f32-blocks/f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[precision],
         "data": "synthetic (generated cube mesh, manufactured solution; no public dataset)",
         "config": {"workload": workload, "n_tet": r["n_tet"], "n_poly": r["n_poly"], "dofs": r["dofs"],
                    "n_blocks": r["n_blocks"], "precision": args.precision,
                    "l2_flush": "inputs larger than L2 (operator blocks %.1f GB per step)" % (r["bytes"] / 1e9),
                    "parallelism": "replicas" if info["world"] > 1 else "single GPU"},
-        "err_L2": r["err_L2"], "err_DG": r["err_DG"],
+        "err_L2": r["err_L2"], "err_DG": r["err_DG"], "error_after_steps": r["error_steps"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_launch": r["bytes"], "kernel_ms": r["kernel_ms_avg"],
@@ -529,13 +539,16 @@ def main():
         line["cpu_baseline"] = {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",
                                 "sample": cb["sample"]}
     if info["rank"] == 0 and precision == 0 and not args.no_mixed:
-        rm = run_gpu(cfg, 1, args.steps, args.warmup, {**info, "barrier": lambda: None, "max": lambda x: x},
-                     want_e2e=False)
-        vm = rm["dofs"] * rm["steps"] / (rm["ms"] / 1e3)
-        line["mixed"] = {"value": vm, "speedup_vs_fp64": vm / value * info["world"], "err_L2": rm["err_L2"],
+        for key, prec in (("mixed", 1),):
+            rm = run_gpu(cfg, prec, args.steps, args.warmup, {**info, "barrier": lambda: None, "max": lambda x: x},
+                         want_e2e=False)
+            vm = rm["dofs"] * rm["steps"] / (rm["ms"] / 1e3)
+            line[key] = {"value": vm, "speedup_vs_fp64": vm / value * info["world"], "err_L2": rm["err_L2"],
                          "err_DG": rm["err_DG"], "err_L2_ratio_vs_fp64": rm["err_L2"] / r["err_L2"],
-                         "kernel_ms": rm["kernel_ms_avg"],
-                         "achieved_gbs": rm["bytes"] / (rm["kernel_ms_avg"] / 1e3) / 1e9}
+                         "err_DG_ratio_vs_fp64": rm["err_DG"] / r["err_DG"],
+                         "error_after_steps": rm["error_steps"], "kernel_ms": rm["kernel_ms_avg"],
+                         "achieved_gbs": rm["bytes"] / (rm["kernel_ms_avg"] / 1e3) / 1e9,
+                         "bytes_per_launch": rm["bytes"]}
     if info["rank"] == 0:
         print(json.dumps(line), flush=True)
     if info.get("dist"):

@@ -61,6 +61,15 @@ int g_perturb_ulps = 0;
 // The spread between the two orders is the algorithm's own rounding floor.
 int g_reverse_sums = 0;
 
+// Third instrument (0 = off, else the number of column slices S the CUDA step
+// kernel uses at this degree): the operator apply, right-hand side, M^-1
+// product and update in the CUDA step kernel's order -- row r summed as S
+// column slices (columns s, s+S, ...) with two fused-multiply-add
+// accumulators each (even and odd j), over the blocks in stored order, the
+// slices added in order; M^-1 with two accumulators (even and odd columns);
+// the contractions a*b + c of those expressions as fused multiply-adds.
+int g_device_order = 0;
+
 // Third instrument: when set, the time steps apply M^-1 as an explicit
 // inverse (columns solved once with solve_LU) instead of the two triangular
 // solves, the way the device kernel applies it.
@@ -962,7 +971,66 @@ int modal_project(Oracle& o, int fun_id, std::vector<double>& out) {
 // Shared body of FIRST_TIME_STEP_MATRIX_FREE (matrix_free.f90:1100-1227) and
 // TIME_STEP_MATRIX_FREE (:1230-1385): tmp = K u (self + neighbour blocks),
 // tmp = -tmp + rhs_stat + rhs_dyn g(t), per-component solve_LU(R^T, R).
+// The explicit inverse of M_P, column k = solve_LU(R, e_k).
+void explicit_inverse(const Oracle& o, int P, std::vector<double>& inv) {
+    const int Np = o.Np;
+    inv.assign((size_t)Np * Np, 0.0);
+    std::vector<double> e(Np), col(Np);
+    for (int k = 0; k < Np; ++k) {
+        for (int m = 0; m < Np; ++m) e[m] = (m == k) ? 1.0 : 0.0;
+        solve_LU_RT_R(&o.R[(size_t)P * Np * Np], e.data(), Np, col.data());
+        for (int m = 0; m < Np; ++m) inv[(size_t)m * Np + k] = col[m];
+    }
+}
+
+// The CUDA step kernel's evaluation order (g_device_order = S): returns
+// x = M^-1 (f - K u) for polyhedron P.
+void apply_and_solve_device_order(const Oracle& o, const std::vector<double>& u, double t, int P,
+                                  std::vector<double>& out) {
+    const int nd = o.nd, Np = o.Np, S = g_device_order;
+    const int cpt = (nd + S - 1) / S;
+    const double g = time_function(t);
+    const size_t nb = o.nbr[P].size();
+    // the device's row order: the self block, then the neighbours by index
+    std::vector<size_t> order(nb);
+    for (size_t bi = 0; bi < nb; ++bi) order[bi] = bi;
+    std::sort(order.begin() + 1, order.end(), [&](size_t a, size_t b) { return o.nbr[P][a] < o.nbr[P][b]; });
+    std::vector<double> b(nd);
+    for (int r = 0; r < nd; ++r) {
+        double y = 0.0;
+        for (int sl = 0; sl < S; ++sl) {
+            double acc0 = 0.0, acc1 = 0.0;
+            for (size_t oi = 0; oi < nb; ++oi) {
+                const size_t bi = order[oi];
+                const double* Kb = &o.K[P][bi * nd * nd];
+                const double* uq = &u[(size_t)o.nbr[P][bi] * nd];
+                for (int j = 0; j < cpt; ++j) {
+                    const int c = sl + j * S;
+                    if (c >= nd) continue;
+                    if (j & 1) acc1 = std::fma(Kb[r * nd + c], uq[c], acc1);
+                    else acc0 = std::fma(Kb[r * nd + c], uq[c], acc0);
+                }
+            }
+            y += acc0 + acc1;
+        }
+        b[r] = std::fma(o.rhs_dyn[(size_t)P * nd + r], g, -y + o.rhs_stat[(size_t)P * nd + r]);
+    }
+    std::vector<double> inv;
+    explicit_inverse(o, P, inv);
+    out.assign(nd, 0.0);
+    for (int i = 0; i < 3; ++i)
+        for (int m = 0; m < Np; ++m) {
+            double x0 = 0.0, x1 = 0.0;
+            for (int c = 0; c < Np; c += 2) {
+                x0 = std::fma(inv[(size_t)m * Np + c], b[i * Np + c], x0);
+                if (c + 1 < Np) x1 = std::fma(inv[(size_t)m * Np + c + 1], b[i * Np + c + 1], x1);
+            }
+            out[i * Np + m] = x0 + x1;
+        }
+}
+
 void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, int P, std::vector<double>& out) {
+    if (g_device_order) { apply_and_solve_device_order(o, u, t, P, out); return; }
     int nd = o.nd, Np = o.Np;
     std::vector<double> tmp(nd, 0.0), v(Np), x(Np);
     double g = time_function(t);
@@ -984,12 +1052,8 @@ void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, in
     for (int r = 0; r < nd; ++r) tmp[r] = -tmp[r] + o.rhs_stat[(size_t)P * nd + r] + o.rhs_dyn[(size_t)P * nd + r] * g;
     out.assign(nd, 0.0);
     if (g_explicit_inverse) {
-        std::vector<double> inv((size_t)Np * Np), e(Np), col(Np);
-        for (int k = 0; k < Np; ++k) {
-            for (int m = 0; m < Np; ++m) e[m] = (m == k) ? 1.0 : 0.0;
-            solve_LU_RT_R(&o.R[(size_t)P * Np * Np], e.data(), Np, col.data());
-            for (int m = 0; m < Np; ++m) inv[(size_t)m * Np + k] = col[m];
-        }
+        std::vector<double> inv;
+        explicit_inverse(o, P, inv);
         for (int i = 0; i < 3; ++i)
             for (int m = 0; m < Np; ++m) {
                 double x = 0.0;
@@ -1019,6 +1083,8 @@ void oracle_set_data_perturbation(int ulps) { g_perturb_ulps = ulps; }
 void oracle_set_reverse_sums(int on) { g_reverse_sums = on; }
 
 void oracle_set_explicit_inverse(int on) { g_explicit_inverse = on; }
+
+void oracle_set_device_order(int slices) { g_device_order = slices > 0 ? slices : 0; }
 
 int oracle_num_threads(void) {
 #ifdef _OPENMP
@@ -1088,8 +1154,13 @@ int oracle_first_step(void* h, double t) {
     for (int P = 0; P < o.n_poly; ++P) {
         std::vector<double> x;
         apply_and_solve(o, o.slot[LYMPH_SLOT_U0], t, P, x);
-        for (int r = 0; r < nd; ++r)
-            un[(size_t)P * nd + r] = half_dt2 * x[r] + o.slot[LYMPH_SLOT_U0][(size_t)P * nd + r] + o.dt * o.slot[LYMPH_SLOT_V0][(size_t)P * nd + r];
+        for (int r = 0; r < nd; ++r) {
+            const size_t q = (size_t)P * nd + r;
+            if (g_device_order)
+                un[q] = std::fma(o.dt, o.slot[LYMPH_SLOT_V0][q], std::fma(half_dt2, x[r], o.slot[LYMPH_SLOT_U0][q]));
+            else
+                un[q] = half_dt2 * x[r] + o.slot[LYMPH_SLOT_U0][q] + o.dt * o.slot[LYMPH_SLOT_V0][q];
+        }
     }
     o.slot[LYMPH_SLOT_UN] = un;
     return 0;
@@ -1105,8 +1176,13 @@ int oracle_step(void* h, double t) {
     for (int P = 0; P < o.n_poly; ++P) {
         std::vector<double> x;
         apply_and_solve(o, o.slot[LYMPH_SLOT_UN], t, P, x);
-        for (int r = 0; r < nd; ++r)
-            us[(size_t)P * nd + r] = dt2 * x[r] + 2.0 * o.slot[LYMPH_SLOT_UN][(size_t)P * nd + r] - o.slot[LYMPH_SLOT_U0][(size_t)P * nd + r];
+        for (int r = 0; r < nd; ++r) {
+            const size_t q = (size_t)P * nd + r;
+            if (g_device_order)
+                us[q] = std::fma(dt2, x[r], 2.0 * o.slot[LYMPH_SLOT_UN][q]) - o.slot[LYMPH_SLOT_U0][q];
+            else
+                us[q] = dt2 * x[r] + 2.0 * o.slot[LYMPH_SLOT_UN][q] - o.slot[LYMPH_SLOT_U0][q];
+        }
     }
     o.slot[LYMPH_SLOT_U0].swap(o.slot[LYMPH_SLOT_UN]);
     o.slot[LYMPH_SLOT_UN].swap(us);
