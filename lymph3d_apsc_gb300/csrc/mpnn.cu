@@ -153,11 +153,6 @@ __global__ void k_mse(int64_t n, const float* __restrict__ y, const float* __res
     if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
-__global__ void k_add(int64_t n, const float* __restrict__ a, float* b) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        b[i] += a[i];
-}
-
 // Adam on FP32 masters; weight matrices are re-rounded to their BF16 copies.
 __global__ void k_adam(int64_t n, float* p, const float* __restrict__ g, float* m, float* v, __nv_bfloat16* pb,
                        float lr, float b1, float b2, float eps, float c1, float c2) {
