@@ -57,7 +57,11 @@ CONFIGS = {
     # 1..4, Ricker point sources, homogeneous Dirichlet, own CFL dt), one
     # persistent launch per step
     "c3": dict(n=None, agglomeration="bfs", group=(4, 16), seed=2, p=None, material=(1.0, 1.0, 1.0), lognormal=False,
-               dt=None, sample_n=None, ensemble=64),
+               dt=None, sample_n=None, ensemble=64, n_range=(8, 32)),
+    # the same construction with 256 small problems (cubes 3^3..8^3 x 6): the
+    # regime where one launch per step for all problems pays
+    "c3s": dict(n=None, agglomeration="bfs", group=(4, 16), seed=3, p=None, material=(1.0, 1.0, 1.0), lognormal=False,
+                dt=None, sample_n=None, ensemble=256, n_range=(3, 8)),
     # 48k polyhedra, p = 4, lognormal lambda/mu per polyhedron
     "c2": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=4, material=(1.0, 1.0, 1.0), lognormal=True,
                dt=2e-5, sample_n=8),
@@ -311,7 +315,7 @@ def run_ensemble(cfg, precision, steps, warmup, info):
     from lymph3d_apsc_gb300 import ensemble as E
     t0 = time.perf_counter()
     solvers, meta = E.make_ensemble(n_problems=cfg["ensemble"], seed=cfg["seed"], group=cfg["group"],
-                                    precision=precision)
+                                    precision=precision, n_range=cfg["n_range"])
     t1 = time.perf_counter()
     b = E.Batch(solvers)
     grid, order = b.autotune(trial_steps=2)
@@ -496,8 +500,9 @@ def main():
         line = {"metric": metric, "value": value, "unit": "DOF-steps/s", "n_gpus": 1, "steps": r["steps"],
                 "warmup": args.warmup, "ms_per_step": r["ms"] / r["steps"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[precision],
-                "data": "synthetic (64 generated cube meshes, Ricker point sources)",
-                "config": {"workload": "64-problem ensemble: n^3x6 tets with n~U{8..32}, BFS groups 4-16, p~U{1..4}, "
+                "data": f"synthetic ({cfg['ensemble']} generated cube meshes, Ricker point sources)",
+                "config": {"workload": f"{cfg['ensemble']}-problem ensemble: n^3x6 tets with "
+                                       f"n~U{{{cfg['n_range'][0]}..{cfg['n_range'][1]}}}, BFS groups 4-16, p~U{{1..4}}, "
                                        "Ricker f0~U[5,20] Hz, x0~U[0.2,0.8]^3, own CFL dt (0.8 x 2/sqrt(lambda_max))",
                            "problems": len(r["meta"]), "degrees": degrees, "dofs": r["dofs"],
                            "autotuned_grid": r["grid"], "autotuned_order": ["largest-first", "problem-major"][r["order"]]},
