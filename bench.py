@@ -28,6 +28,7 @@ on one GPU per problem; see the design notes), value = sum over ranks.
 from __future__ import annotations
 
 import argparse
+from ctypes import c_double
 import json
 import math
 
@@ -65,6 +66,10 @@ CONFIGS = {
     # 48k polyhedra, p = 4, lognormal lambda/mu per polyhedron
     "c2": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=4, material=(1.0, 1.0, 1.0), lognormal=True,
                dt=2e-5, sample_n=8),
+    # the surrogate network's forward on the c2 mesh (46,767 polyhedra, p = 3
+    # features, H = 256, 3 layers, gated head): its GEMMs on tcgen05 tensor cores
+    "c4f": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 1.0, 1.0), lognormal=True,
+                dt=2e-5, sample_n=None, mpnn_forward=dict(H=256, L=3, reps=50)),
     # learned surrogate: trained on 200 seeded solver runs (p = 3, 4^3..10^3
     # meshes, Ricker sources from rest, lognormal materials), evaluated on the
     # c2 mesh at p = 3, dt = 2e-5, a 50 Hz Ricker point source at the centre,
@@ -415,6 +420,37 @@ def run_surrogate(cfg, steps):
     return out
 
 
+def run_mpnn_forward(cfg, info):
+    """Config c4f: device time of the network forward at the evaluation
+    mesh's size (synthetic features, random weights: the cost does not depend
+    on the values), on the tensor cores and, for comparison, on the SIMT pipe."""
+    import numpy as np
+    from lymph3d_apsc_gb300 import _lib
+    from lymph3d_apsc_gb300 import surrogate as S
+    mf = cfg["mpnn_forward"]
+    m = make_mesh(cfg)
+    graph = S.build_graph(m)
+    N = m.n_poly
+    out = {"n_nodes": N}
+    for label, simt in (("tensor_cores", "0"), ("simt", "1")):
+        os.environ["LYMPH_MPNN_SIMT"] = simt
+        net = S.surrogate_net(cfg["p"], H=mf["H"], L=mf["L"])
+        net.set_graph(graph)
+        x = np.random.default_rng(0).standard_normal((N, net.F)).astype(np.float32)
+        net.forward(x)
+        ms = c_double()
+        with ClockSampler(info["gpu"]) as clk:
+            _lib.check(net.lib.lymph_mpnn_time_forward(net.h, mf["reps"], ms), "time_forward")
+        out[label] = {"ms": ms.value, "tensor_cores": bool(net.lib.lymph_mpnn_uses_tensor_cores(net.h)),
+                      "clocks": clk.summary()}
+        F, H, L, G, O = net.F, net.H, net.L, net.G, net.O
+        out["flops"] = 2.0 * N * (F * H + L * (H * H + (2 * H + G) * H) + H * O)
+        out["launches_per_forward"] = 1 + 2 * L + 1
+        net.close()
+    os.environ.pop("LYMPH_MPNN_SIMT", None)
+    return out
+
+
 def rank_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -473,6 +509,30 @@ def main():
         return
 
     precision = {"fp64": 0, "mixed": 1}[args.precision]
+    if cfg.get("mpnn_forward"):
+        if info["rank"] != 0:
+            return
+        r = run_mpnn_forward(cfg, info)
+        tc = r["tensor_cores"]
+        tfl = r["flops"] / (tc["ms"] / 1e3) / 1e12
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        bf16 = peaks.get("bf16_tflops", 1900.0)
+        line = {"metric": "network forward TFLOP/s (2 N (F H + L (H^2 + (2H+G) H) + H O) per forward)",
+                "value": tfl, "unit": "TFLOP/s", "n_gpus": 1, "steps": cfg["mpnn_forward"]["reps"], "warmup": 1,
+                "ms_per_step": tc["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "tf32 hi+lo split (activations), bf16 weights, f32 accumulate",
+                "data": "synthetic features on the c2 mesh graph, random weights",
+                "config": {"workload": f"MPNN forward, {r['n_nodes']} nodes, H=256, L=3, gated head, p=3 features",
+                           "l2_flush": "activations 48 MB per layer, weights L2-resident (read by every CTA)"},
+                "roofline": {"bound": "tensor", "achieved": tfl, "peak": bf16 / 2.0, "unit": "TFLOP/s",
+                             "frac": tfl / (bf16 / 2.0), "traffic": None,
+                             "peak_source": "measured bf16 / 2 (TF32 rate)",
+                             "tensor_issue_tflops": 2.0 * tfl},
+                "simt_ms": r["simt"]["ms"], "speedup_vs_simt": r["simt"]["ms"] / tc["ms"],
+                "uses_tensor_cores": tc["tensor_cores"], "gpu_launches": r["launches_per_forward"] * cfg["mpnn_forward"]["reps"],
+                "clocks": tc["clocks"]}
+        print(json.dumps(line), flush=True)
+        return
     if cfg.get("surrogate"):
         if info["rank"] != 0:
             return

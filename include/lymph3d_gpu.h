@@ -259,6 +259,14 @@ int lymph_mpnn_forward(lymph_mpnn* net, const float* x, float* y);
 int lymph_mpnn_loss_grad(lymph_mpnn* net, const float* x, const float* target, double* loss);
 int lymph_mpnn_adam(lymph_mpnn* net, float lr, float beta1, float beta2, float eps);
 int lymph_mpnn_launch_count(const lymph_mpnn* net, int64_t* count);
+/* Average device time of `reps` forwards on the features already on the
+ * device (after a lymph_mpnn_forward), CUDA events on the network's stream. */
+int lymph_mpnn_time_forward(lymph_mpnn* net, int32_t reps, double* ms);
+/* 1 when the forward GEMMs run on the tensor cores (tcgen05, TF32 hi/lo split
+ * of the activations, FP32 accumulation in tensor memory): H and O <= 256
+ * and F, H, G multiples of 4; 0 when they run on the FP32 SIMT pipe (also
+ * with LYMPH_MPNN_SIMT=1 in the environment at creation). */
+int lymph_mpnn_uses_tensor_cores(const lymph_mpnn* net);
 /* Gated output head: the O = 6 B network outputs per node are coefficients
  * alpha[j][b][i] and the effective output (2 nd columns, what forward
  * returns and the loss compares) is

@@ -123,6 +123,8 @@ _SIGS = {
     "lymph_surrogate_residual": (c_int, [c_void_p, c_void_p, P_F64]),
     "lymph_nodal_values": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_mpnn_set_gate": (c_int, [c_void_p, c_int32, c_int32]),
+    "lymph_mpnn_time_forward": (c_int, [c_void_p, c_int32, P_F64]),
+    "lymph_mpnn_uses_tensor_cores": (c_int, [c_void_p]),
     "lymph_surrogate_features": (c_int, [c_void_p, c_void_p, c_double, POINTER(c_float), P_F64, P_F64, P_F64]),
     "lymph_surrogate_judge": (c_int, [c_void_p, c_void_p, c_int32, P_F64]),
     "lymph_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),

@@ -20,11 +20,13 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "common.cuh"
+#include "umma_gemm.cuh"
 
 int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);  // out = M^-1 K u (step.cu)
 
@@ -116,6 +118,26 @@ __global__ void k_aggregate(int n, int width, const int32_t* __restrict__ ptr, c
         float s = 0.0f;
         for (int k = ptr[i]; k < ptr[i + 1]; ++k) s += val[k] * in[(int64_t)idx[k] * width + c];
         out[(int64_t)i * width + c] = s;
+    }
+}
+
+// The same with one warp per node and 16-byte loads (width a multiple of 4):
+// each neighbour row is read as one coalesced segment; the sum over the
+// neighbours runs in the CSR order, as in k_aggregate.
+__global__ void __launch_bounds__(256) k_aggregate_v4(int n, int width, const int32_t* __restrict__ ptr,
+                                                      const int32_t* __restrict__ idx, const float* __restrict__ val,
+                                                      const float* __restrict__ in, float* out) {
+    const int i = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (i >= n) return;
+    const int k0 = ptr[i], k1 = ptr[i + 1];
+    for (int c = 4 * lane; c < width; c += 128) {
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = k0; k < k1; ++k) {
+            const float w = val[k];
+            const float4 v = *(const float4*)(in + (int64_t)idx[k] * width + c);
+            s.x += w * v.x; s.y += w * v.y; s.z += w * v.z; s.w += w * v.w;
+        }
+        *(float4*)(out + (int64_t)i * width + c) = s;
     }
 }
 
@@ -241,6 +263,13 @@ struct lymph_mpnn {
     int32_t *d_wp = nullptr, *d_wi = nullptr, *d_tp = nullptr, *d_ti = nullptr;
     float *d_wv = nullptr, *d_tv = nullptr;
     int64_t launches = 0;
+    // tensor-core forward: per weight matrix W [K][N] (BF16), an FP32 copy of
+    // W^T padded to Npad = round16(N) rows (the K-major B operand)
+    float* d_wt = nullptr;
+    std::vector<int64_t> wt_off;  // per entry of par (matrices only), -1 otherwise
+    bool wt_dirty = true;
+    bool use_umma = true;         // LYMPH_MPNN_SIMT=1 selects the SIMT GEMMs for the forward too
+    int* d_status = nullptr;      // bit 0: a tensor-core wait ran out
 };
 
 namespace {
@@ -261,6 +290,82 @@ float* P_(lymph_mpnn* n, const char* w, int l = 0) { return n->d_p + n->par[pidx
 float* G_(lymph_mpnn* n, const char* w, int l = 0) { return n->d_g + n->par[pidx(n, w, l)].off; }
 const __nv_bfloat16* B_(lymph_mpnn* n, const char* w, int l = 0) { return n->d_pb + n->par[pidx(n, w, l)].off; }
 
+int round16(int x) { return (x + 15) / 16 * 16; }
+
+// Bt[n][k] = W[k][n] for n < N, 0 for N <= n < Npad
+__global__ void k_transpose_w(int K, int N, int Npad, const __nv_bfloat16* __restrict__ W, float* Bt) {
+    const int64_t tot = (int64_t)Npad * K;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
+        const int n = (int)(i / K), k = (int)(i % K);
+        Bt[i] = n < N ? __bfloat162float(W[(int64_t)k * N + n]) : 0.0f;
+    }
+}
+
+// Refreshes the transposed FP32 weight copies after the BF16 weights changed.
+void refresh_wt(lymph_mpnn* n) {
+    if (!n->wt_dirty) return;
+    for (size_t i = 0; i < n->par.size(); ++i) {
+        if (n->wt_off[i] < 0) continue;
+        const auto& P = n->par[i];
+        const int K = (int)P.rows, N = (int)P.cols;
+        k_transpose_w<<<256, 256, 0, n->stream>>>(K, N, round16(N), n->d_pb + P.off, n->d_wt + n->wt_off[i]);
+        n->launches++;
+    }
+    n->wt_dirty = false;
+}
+
+// Can the tensor-core kernel take this GEMM?  (N <= 256, every K and leading
+// dimension a multiple of 4 for its 16-byte loads.)
+bool umma_ok(const lymph_mpnn* n, int N, std::initializer_list<int> dims) {
+    if (!n->use_umma || N > 256 || N <= 0) return false;
+    for (int d : dims)
+        if (d % 4) return false;
+    return true;
+}
+
+// C = sum_s A_s W_s (+ bias) with the epilogue, on the tensor cores; the
+// weight matrix is parameter `pi`, whose rows are the concatenated K of the
+// segments.
+void umma_gemm(lymph_mpnn* n, int pi, int M, const umma::Seg* segs, int nseg, const float* bias, float* C, int ldc,
+               float* Z, const float* R, int epi) {
+    const auto& P = n->par[pi];
+    umma::Args a;
+    for (int s = 0; s < nseg; ++s) a.seg[s] = segs[s];
+    a.nseg = nseg;
+    a.M = M;
+    a.N = (int)P.cols;
+    a.Npad = round16((int)P.cols);
+    a.Bt = n->d_wt + n->wt_off[pi];
+    a.Ktot = (int)P.rows;
+    a.bias = bias;
+    a.C = C;
+    a.ldc = ldc;
+    a.Z = Z;
+    a.R = R;
+    a.epi = epi;
+    a.status = n->d_status;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(umma::k_umma_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)umma::SMEM_ALLOC);
+        attr_set = true;
+    }
+    const dim3 grid((M + umma::BM - 1) / umma::BM, (a.Npad + umma::BN - 1) / umma::BN);
+    umma::k_umma_gemm<<<grid, umma::THREADS, umma::SMEM_ALLOC, n->stream>>>(a);
+    n->launches++;
+}
+
+int read_status(lymph_mpnn* n, const char* who) {
+    int st = 0;
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(&st, n->d_status, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(n->stream));
+    if (st) {
+        cudaMemsetAsync(n->d_status, 0, sizeof(int), n->stream);
+        lymph_set_error(std::string(who) + ": a tensor-core wait ran out (the kernel returned without its result)");
+        return LYMPH_ERR_TIMEOUT;
+    }
+    return LYMPH_OK;
+}
+
 template <bool TA, bool TB, typename BT>
 void gemm(lymph_mpnn* n, int M, int N, int K, const float* A, int lda, const BT* B, int ldb, float* C, int ldc,
           const float* bias, float* Z, int epi) {
@@ -271,9 +376,13 @@ void gemm(lymph_mpnn* n, int M, int N, int K, const float* A, int lda, const BT*
 }
 
 void aggregate(lymph_mpnn* n, bool transposed, int width, const float* in, float* out) {
-    k_aggregate<<<n->n_nodes, 128, 0, n->stream>>>(n->n_nodes, width, transposed ? n->d_tp : n->d_wp,
-                                                   transposed ? n->d_ti : n->d_wi, transposed ? n->d_tv : n->d_wv, in,
-                                                   out);
+    const int32_t* p = transposed ? n->d_tp : n->d_wp;
+    const int32_t* ix = transposed ? n->d_ti : n->d_wi;
+    const float* v = transposed ? n->d_tv : n->d_wv;
+    if (width % 4 == 0)  // rows of 16-byte multiples from cudaMalloc'd buffers: 16-byte aligned
+        k_aggregate_v4<<<(n->n_nodes + 7) / 8, 256, 0, n->stream>>>(n->n_nodes, width, p, ix, v, in, out);
+    else
+        k_aggregate<<<n->n_nodes, 128, 0, n->stream>>>(n->n_nodes, width, p, ix, v, in, out);
     n->launches++;
 }
 
@@ -312,25 +421,48 @@ int ensure_capacity(lymph_mpnn* n, int N) {
 // forward on the current graph; x in d_x, g in d_gf, output in d_y
 void forward(lymph_mpnn* n) {
     const int N = n->n_nodes, H = n->H, F = n->F, G = n->G, O = n->O;
-    gemm<false, false, __nv_bfloat16>(n, N, H, F, n->d_x, F, B_(n, "W0"), H, n->d_h[0], H, P_(n, "b0"), n->d_z0, EPI_RELU);
-    for (int l = 0; l < n->L; ++l) {
-        float* h = n->d_h[l];
-        float* h1 = n->d_h[l + 1];
-        cudaMemcpyAsync(h1, h, sizeof(float) * (size_t)N * H, cudaMemcpyDeviceToDevice, n->stream);
-        gemm<false, false, __nv_bfloat16>(n, N, H, H, h, H, B_(n, "Wm", l), H, n->d_m_[l], H, P_(n, "bm", l),
-                                          n->d_zm[l], EPI_RELU);
-        aggregate(n, false, H, n->d_m_[l], n->d_a[l]);
-        const __nv_bfloat16* Wu = B_(n, "Wu", l);
-        // zu = h Wu[0:H] + a Wu[H:2H] + g Wu[2H:] + bu ; h1 = h + relu(zu)
-        gemm<false, false, __nv_bfloat16>(n, N, H, H, h, H, Wu, H, n->d_zu[l], H, P_(n, "bu", l), nullptr, EPI_STORE);
-        gemm<false, false, __nv_bfloat16>(n, N, H, H, n->d_a[l], H, Wu + (int64_t)H * H, H, n->d_zu[l], H, nullptr,
-                                          nullptr, EPI_ADD);
-        // last slice: finishes zu and adds relu(zu) into h1 in its epilogue
-        gemm<false, false, __nv_bfloat16>(n, N, H, G, n->d_gf, G, Wu + (int64_t)2 * H * H, H, h1, H, nullptr,
-                                          n->d_zu[l], EPI_ACC_RELU_ADD);
+    const bool tc = umma_ok(n, H, {F, H, G}) && umma_ok(n, O, {H});
+    if (tc) {
+        // tensor cores: h0 = relu(x W0 + b0); per layer m = relu(h Wm + bm),
+        // a = W m, h1 = h + relu([h a g] Wu + bu); y = h Wo + bo
+        refresh_wt(n);
+        umma::Seg s0[1] = {{n->d_x, F, F}};
+        umma_gemm(n, (int)pidx(n, "W0", 0), N, s0, 1, P_(n, "b0"), n->d_h[0], H, n->d_z0, nullptr, umma::EPI_RELU);
+        for (int l = 0; l < n->L; ++l) {
+            float* h = n->d_h[l];
+            umma::Seg sm[1] = {{h, H, H}};
+            umma_gemm(n, (int)pidx(n, "Wm", l), N, sm, 1, P_(n, "bm", l), n->d_m_[l], H, n->d_zm[l], nullptr,
+                      umma::EPI_RELU);
+            aggregate(n, false, H, n->d_m_[l], n->d_a[l]);
+            umma::Seg su[3] = {{h, H, H}, {n->d_a[l], H, H}, {n->d_gf, G, G}};
+            umma_gemm(n, (int)pidx(n, "Wu", l), N, su, 3, P_(n, "bu", l), n->d_h[l + 1], H, n->d_zu[l], h,
+                      umma::EPI_RES_RELU);
+        }
+        umma::Seg so[1] = {{n->d_h[n->L], H, H}};
+        umma_gemm(n, (int)pidx(n, "Wo", 0), N, so, 1, P_(n, "bo"), n->d_y, O, nullptr, nullptr, umma::EPI_STORE);
+    } else {
+        gemm<false, false, __nv_bfloat16>(n, N, H, F, n->d_x, F, B_(n, "W0"), H, n->d_h[0], H, P_(n, "b0"), n->d_z0,
+                                          EPI_RELU);
+        for (int l = 0; l < n->L; ++l) {
+            float* h = n->d_h[l];
+            float* h1 = n->d_h[l + 1];
+            cudaMemcpyAsync(h1, h, sizeof(float) * (size_t)N * H, cudaMemcpyDeviceToDevice, n->stream);
+            gemm<false, false, __nv_bfloat16>(n, N, H, H, h, H, B_(n, "Wm", l), H, n->d_m_[l], H, P_(n, "bm", l),
+                                              n->d_zm[l], EPI_RELU);
+            aggregate(n, false, H, n->d_m_[l], n->d_a[l]);
+            const __nv_bfloat16* Wu = B_(n, "Wu", l);
+            // zu = h Wu[0:H] + a Wu[H:2H] + g Wu[2H:] + bu ; h1 = h + relu(zu)
+            gemm<false, false, __nv_bfloat16>(n, N, H, H, h, H, Wu, H, n->d_zu[l], H, P_(n, "bu", l), nullptr,
+                                              EPI_STORE);
+            gemm<false, false, __nv_bfloat16>(n, N, H, H, n->d_a[l], H, Wu + (int64_t)H * H, H, n->d_zu[l], H,
+                                              nullptr, nullptr, EPI_ADD);
+            // last slice: finishes zu and adds relu(zu) into h1 in its epilogue
+            gemm<false, false, __nv_bfloat16>(n, N, H, G, n->d_gf, G, Wu + (int64_t)2 * H * H, H, h1, H, nullptr,
+                                              n->d_zu[l], EPI_ACC_RELU_ADD);
+        }
+        gemm<false, false, __nv_bfloat16>(n, N, O, H, n->d_h[n->L], H, B_(n, "Wo"), O, n->d_y, O, P_(n, "bo"),
+                                          nullptr, EPI_STORE);
     }
-    gemm<false, false, __nv_bfloat16>(n, N, O, H, n->d_h[n->L], H, B_(n, "Wo"), O, n->d_y, O, P_(n, "bo"), nullptr,
-                                      EPI_STORE);
     if (n->gate_B) {
         const int64_t tot = (int64_t)N * 2 * n->gate_nd;
         k_gate<<<(int)std::min<int64_t>((tot + 255) / 256, 4096), 256, 0, n->stream>>>(N, n->gate_nd, n->gate_B, n->F,
@@ -647,11 +779,19 @@ int lymph_mpnn_create(int32_t F, int32_t H, int32_t O, int32_t L, int32_t G, lym
     add(F, H, true); add(1, H, false);
     for (int l = 0; l < L; ++l) { add(H, H, true); add(1, H, false); add(2 * H + G, H, true); add(1, H, false); }
     add(H, O, true); add(1, O, false);
+    int64_t n_wt = 0;
+    for (const auto& P : n->par) {
+        n->wt_off.push_back(P.matrix ? n_wt : -1);
+        if (P.matrix) n_wt += (int64_t)round16((int)P.cols) * P.rows;
+    }
+    const char* simt = std::getenv("LYMPH_MPNN_SIMT");
+    n->use_umma = !(simt && simt[0] == '1');
     if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) { delete n; lymph_set_error("lymph_mpnn_create: stream"); return LYMPH_ERR_CUDA; }
     size_t b = sizeof(float) * (size_t)n->n_par;
     if (cudaMalloc(&n->d_p, b) != cudaSuccess || cudaMalloc(&n->d_g, b) != cudaSuccess || cudaMalloc(&n->d_m, b) != cudaSuccess ||
         cudaMalloc(&n->d_v, b) != cudaSuccess || cudaMalloc(&n->d_pb, sizeof(__nv_bfloat16) * (size_t)n->n_par) != cudaSuccess ||
-        cudaMalloc(&n->d_partial, sizeof(double) * 1024) != cudaSuccess) {
+        cudaMalloc(&n->d_partial, sizeof(double) * 1024) != cudaSuccess ||
+        cudaMalloc(&n->d_wt, sizeof(float) * (size_t)n_wt) != cudaSuccess || cudaMalloc(&n->d_status, sizeof(int)) != cudaSuccess) {
         lymph_mpnn_destroy(n);
         lymph_set_error("lymph_mpnn_create: out of memory");
         return LYMPH_ERR_OOM;
@@ -660,6 +800,7 @@ int lymph_mpnn_create(int32_t F, int32_t H, int32_t O, int32_t L, int32_t G, lym
     cudaMemsetAsync(n->d_g, 0, b, n->stream);
     cudaMemsetAsync(n->d_m, 0, b, n->stream);
     cudaMemsetAsync(n->d_v, 0, b, n->stream);
+    cudaMemsetAsync(n->d_status, 0, sizeof(int), n->stream);
     *out = n;
     return LYMPH_OK;
 }
@@ -668,6 +809,7 @@ int lymph_mpnn_destroy(lymph_mpnn* n) {
     if (!n) return LYMPH_OK;
     if (n->stream) cudaStreamSynchronize(n->stream);
     for (void* p : {(void*)n->d_p, (void*)n->d_g, (void*)n->d_m, (void*)n->d_v, (void*)n->d_pb, (void*)n->d_partial,
+                    (void*)n->d_wt, (void*)n->d_status,
                     (void*)n->d_d1, (void*)n->d_d2, (void*)n->d_ss, (void*)n->d_u3, (void*)n->d_a1, (void*)n->d_sig,
                     (void*)n->d_x, (void*)n->d_z0, (void*)n->d_y, (void*)n->d_t, (void*)n->d_dy, (void*)n->d_gf,
                     (void*)n->d_yg, (void*)n->d_dyg,
@@ -690,6 +832,7 @@ int lymph_mpnn_set_params(lymph_mpnn* n, const float* params) {
     if (!n || !params) return LYMPH_ERR_INVALID;
     LYMPH_CUDA_TRY(cudaMemcpyAsync(n->d_p, params, sizeof(float) * (size_t)n->n_par, cudaMemcpyHostToDevice, n->stream));
     k_to_bf16<<<256, 256, 0, n->stream>>>(n->n_par, n->d_p, n->d_pb);
+    n->wt_dirty = true;
     LYMPH_CUDA_TRY(cudaMemsetAsync(n->d_m, 0, sizeof(float) * (size_t)n->n_par, n->stream));
     LYMPH_CUDA_TRY(cudaMemsetAsync(n->d_v, 0, sizeof(float) * (size_t)n->n_par, n->stream));
     n->adam_t = 0;
@@ -723,7 +866,7 @@ int lymph_mpnn_forward(lymph_mpnn* n, const float* x, float* y) {
     LYMPH_CUDA_TRY(cudaMemcpyAsync(y, eff_out(n), sizeof(float) * (size_t)n->n_nodes * eff_width(n),
                                    cudaMemcpyDeviceToHost, n->stream));
     LYMPH_CUDA_TRY(cudaStreamSynchronize(n->stream));
-    return LYMPH_OK;
+    return read_status(n, "lymph_mpnn_forward");
 }
 
 // Forward, MSE loss against target, backward: gradients stay on the device
@@ -755,7 +898,7 @@ int lymph_mpnn_loss_grad(lymph_mpnn* n, const float* x, const float* target, dou
         for (int i = 0; i < nb; ++i) s += part[i];
         *loss = s / (double)ny;
     }
-    return LYMPH_OK;
+    return read_status(n, "lymph_mpnn_loss_grad");
 }
 
 // Switches the output head to the gated form over the first B feature blocks
@@ -774,12 +917,43 @@ int lymph_mpnn_set_gate(lymph_mpnn* n, int32_t nd, int32_t B) {
     return LYMPH_OK;
 }
 
+// Device time of the forward on the features already on the device (from
+// the last lymph_mpnn_forward / _loss_grad): `reps` forwards between two CUDA
+// events on the network's stream; *ms = the average.
+int lymph_mpnn_time_forward(lymph_mpnn* n, int32_t reps, double* ms) {
+    if (!n || reps < 1 || !ms || n->n_nodes <= 0) return LYMPH_ERR_INVALID;
+    cudaEvent_t e0, e1;
+    LYMPH_CUDA_TRY(cudaEventCreate(&e0));
+    LYMPH_CUDA_TRY(cudaEventCreate(&e1));
+    forward(n);  // weight copies refreshed outside the timed region
+    cudaEventRecord(e0, n->stream);
+    for (int r = 0; r < reps; ++r) forward(n);
+    cudaEventRecord(e1, n->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        lymph_set_error(std::string("lymph_mpnn_time_forward: ") + cudaGetErrorString(e));
+        return LYMPH_ERR_CUDA;
+    }
+    *ms = (double)t / reps;
+    return read_status(n, "lymph_mpnn_time_forward");
+}
+
+// 1 when the forward GEMMs of this network run on the tensor cores.
+int lymph_mpnn_uses_tensor_cores(const lymph_mpnn* n) {
+    return n && umma_ok(n, n->H, {n->F, n->H, n->G}) && umma_ok(n, n->O, {n->H}) ? 1 : 0;
+}
+
 // One Adam step with the gradients of the last lymph_mpnn_loss_grad.
 int lymph_mpnn_adam(lymph_mpnn* n, float lr, float beta1, float beta2, float eps) {
     if (!n) return LYMPH_ERR_INVALID;
     n->adam_t++;
     const float c1 = 1.0f - powf(beta1, (float)n->adam_t), c2 = 1.0f - powf(beta2, (float)n->adam_t);
     k_adam<<<1024, 256, 0, n->stream>>>(n->n_par, n->d_p, n->d_g, n->d_m, n->d_v, n->d_pb, lr, beta1, beta2, eps, c1, c2);
+    n->wt_dirty = true;
     n->launches++;
     LYMPH_CUDA_TRY(cudaGetLastError());
     LYMPH_CUDA_TRY(cudaStreamSynchronize(n->stream));
@@ -922,7 +1096,8 @@ int lymph_surrogate_predict(lymph_ctx* c, lymph_mpnn* n, int32_t K, int32_t use_
     LYMPH_CUDA_TRY(cudaGetLastError());
     if (scales) LYMPH_TRY(read_scales(c, n, scales, 4));
     n->have_u3 = c;
-    return lymph_sync_status(c, "lymph_surrogate_predict");
+    LYMPH_TRY(lymph_sync_status(c, "lymph_surrogate_predict"));
+    return use_net ? read_status(n, "lymph_surrogate_predict") : LYMPH_OK;
 }
 
 // After the closing plain step of a block (U0 = the predicted u^{n+K-1},

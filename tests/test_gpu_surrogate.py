@@ -53,42 +53,58 @@ def _random_graph(n, rng, G):
     return (np.array(ptr, np.int32), np.array(idx, np.int32), np.array(val, np.float32), g.astype(np.float32))
 
 
-def _net_and_ref(F=21, H=48, O=10, L=2, G=8, N=150, seed=0, gate=None):
-    rng = np.random.default_rng(seed)
+def _net_and_ref(F=21, H=32, O=10, L=2, G=8, N=64, seed=0, gate=None):
+    """A network, its parameters in the oracle's form, a random graph and
+    inputs.  Draws are repeated until no pre-activation of the oracle's
+    forward lies within 1e-5 of its tensor's largest magnitude from the ReLU
+    kink (ten times the device's FP32 rounding there), so that rounding
+    cannot flip a ReLU mask (a flipped mask changes a gradient by an O(1)
+    amount in one entry)."""
     net = S.MPNN(F, O, H=H, L=L, G=G, seed=seed, gate=gate)
-    flat = net.init_params(seed)
-    d = net.unpack(flat)
-    for k, v in d.items():  # non-zero biases and a visible output layer
-        if k.startswith("b"):
-            v[...] = rng.standard_normal(v.shape) * 0.1
-    flat = np.concatenate([d[k].ravel() for k, _ in net.shapes()]).astype(np.float32)
-    flat[-O - H * O:-O] *= 10.0
+    for attempt in range(200):
+        rng = np.random.default_rng(seed + 1000 * attempt)
+        flat = net.init_params(seed + 1000 * attempt)
+        d = net.unpack(flat)
+        for k, v in d.items():  # non-zero biases and a visible output layer
+            if k.startswith("b"):
+                v[...] = rng.standard_normal(v.shape) * 0.1
+        flat = np.concatenate([d[k].ravel() for k, _ in net.shapes()]).astype(np.float32)
+        flat[-O - H * O:-O] *= 10.0
+        graph = _random_graph(N, rng, G)
+        ref = {}
+        for k, v in net.unpack(flat).items():
+            ref[k] = R.bf16_round(v) if k.startswith("W") else v.astype(np.float64)
+        g64 = tuple(np.asarray(a, np.float64) if a.dtype.kind == "f" else a for a in graph)
+        x = rng.standard_normal((N, F)).astype(np.float32)
+        _, cache = R.forward(ref, x.astype(np.float64), g64, L, keep=True, gate=gate)
+        zs = [cache["z0"]] + [z for l in range(L) for z in (cache[l][1], cache[l][4])]
+        if all(np.abs(z).min() > 1e-5 * np.abs(z).max() for z in zs):
+            break
+    else:
+        raise AssertionError("no draw without near-kink pre-activations")
     net.set_params(flat)
-    graph = _random_graph(N, rng, G)
     net.set_graph(graph)
-    ref = {}
-    for k, v in net.unpack(flat).items():
-        ref[k] = R.bf16_round(v) if k.startswith("W") else v.astype(np.float64)
-    g64 = tuple(np.asarray(a, np.float64) if a.dtype.kind == "f" else a for a in graph)
-    x = rng.standard_normal((N, F)).astype(np.float32)
     return net, flat, ref, g64, x
 
 
-GATED = dict(F=30, O=12, gate=(9, 2))  # Np = 3, two basis blocks of 9 DOFs
+GATED = dict(F=32, O=12, gate=(9, 2))  # Np = 3, two basis blocks of 9 DOFs
 
 
-@pytest.mark.parametrize("gated", [False, True])
-def test_forward_matches_oracle(require_gpu, gated):
-    net, _, ref, graph, x = _net_and_ref(**(GATED if gated else {}))
+# F = 21 (not a multiple of 4) runs the SIMT forward GEMMs, F = 24 the
+# tensor-core ones (tcgen05, TF32 hi/lo split of the activations)
+@pytest.mark.parametrize("F,gated", [(21, False), (24, False), (32, True)])
+def test_forward_matches_oracle(require_gpu, F, gated):
+    net, _, ref, graph, x = _net_and_ref(F=F, **({k: v for k, v in GATED.items() if k != "F"} if gated else {}))
     y = net.forward(x)
     y_ref = R.forward(ref, x.astype(np.float64), graph, net.L, gate=net.gate)
     assert rel(y, y_ref) <= 2e-5
     net.close()
 
 
-@pytest.mark.parametrize("L,gated", [(0, False), (1, False), (3, False), (2, True)])
-def test_gradients_match_oracle(require_gpu, L, gated):
-    net, _, ref, graph, x = _net_and_ref(L=L, seed=L + 1, **(GATED if gated else {}))
+@pytest.mark.parametrize("L,gated,F", [(0, False, 21), (1, False, 24), (3, False, 24), (2, True, 32)])
+def test_gradients_match_oracle(require_gpu, L, gated, F):
+    net, _, ref, graph, x = _net_and_ref(L=L, seed=L + 1, F=F, **({k: v for k, v in GATED.items() if k != "F"}
+                                                                     if gated else {}))
     t = np.random.default_rng(9).standard_normal((x.shape[0], net.out_width)).astype(np.float32)
     loss = net.loss_grad(x, t)
     loss_ref, g_ref = R.loss_and_grad(ref, x.astype(np.float64), graph, t.astype(np.float64), L, gate=net.gate)
@@ -98,6 +114,27 @@ def test_gradients_match_oracle(require_gpu, L, gated):
     for k in g_ref:
         assert rel(gd[k], g_ref[k]) <= 2e-5, k
     net.close()
+
+
+def test_tensor_core_forward_equals_simt_on_a_large_graph(require_gpu, monkeypatch):
+    """1,000 nodes (8 row tiles, a partial last one), H = 256, three layers:
+    the tcgen05 forward and the SIMT forward agree to FP32 rounding (the
+    activations' lo part keeps 10 of its 13 bits: ~2^-21 per operand)."""
+    rng = np.random.default_rng(11)
+    F, H, O, L, N = 64, 256, 24, 3, 1000
+    graph = _random_graph(N, rng, 8)
+    x = rng.standard_normal((N, F)).astype(np.float32)
+    outs = []
+    for simt in ("0", "1"):
+        monkeypatch.setenv("LYMPH_MPNN_SIMT", simt)
+        net = S.MPNN(F, O, H=H, L=L, seed=7)
+        flat = net.init_params(7)
+        flat[-O - H * O:-O] *= 10.0
+        net.set_params(flat)
+        net.set_graph(graph)
+        outs.append(net.forward(x).astype(np.float64))
+        net.close()
+    assert rel(outs[0], outs[1]) <= 2e-5
 
 
 def test_adam_step_matches_formula(require_gpu):
