@@ -151,6 +151,14 @@ class ClockSampler:
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def fp64_peak():
+    """FP64 FMA rate measured on this device (the step kernel's real bound)."""
+    from lymph3d_apsc_gb300 import _lib
+    v = c_double()
+    _lib.check(_lib.load().lymph_fp64_peak(20000, v), "lymph_fp64_peak")
+    return v.value
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -590,10 +598,13 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
                      "bytes_per_launch": r["bytes"], "kernel_ms": r["kernel_ms_avg"],
-                     "fp64_tflops": r["flops"] / (r["kernel_ms_avg"] / 1e3) / 1e12},
+                     "fp64_tflops": r["flops"] / (r["kernel_ms_avg"] / 1e3) / 1e12,
+                     "fp64_peak_tflops": fp64_peak(), "fp64_peak_source": "measured (FMA chains, lymph_fp64_peak)"},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
     }
+    rf = line["roofline"]
+    rf["fp64_frac"] = rf["fp64_tflops"] / rf["fp64_peak_tflops"]
     if "e2e" in r:
         e = r["e2e"]
         line["e2e"] = {"value": info["sum"](e["value"]), "unit": "DOF-steps/s",

@@ -399,6 +399,11 @@ int lymph_launch_count(const lymph_ctx* ctx, int64_t* count);
 /* Device bytes the context holds (operator blocks, state, geometry). */
 int lymph_device_bytes(const lymph_ctx* ctx, int64_t* bytes);
 
+/* Measured FP64 FMA throughput of the current device, TFLOP/s (independent
+ * FMA chains in registers, CUDA events): the roofline denominator of the
+ * FP64 step kernel, which the FP64 pipe bounds.  No reference counterpart. */
+int lymph_fp64_peak(int32_t iters, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

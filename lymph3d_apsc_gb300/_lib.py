@@ -129,6 +129,7 @@ _SIGS = {
     "lymph_surrogate_judge": (c_int, [c_void_p, c_void_p, c_int32, P_F64]),
     "lymph_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_device_bytes": (c_int, [c_void_p, POINTER(c_int64)]),
+    "lymph_fp64_peak": (c_int, [c_int32, P_F64]),
     # mesh utilities (lymph3d_mesh.h)
     "lymph_mesh_cube_sizes": (c_int, [c_int32, c_int32, c_int32, P_I32, P_I32]),
     "lymph_mesh_cube": (c_int, [c_int32, c_int32, c_int32, P_F64, P_I32, P_I32]),
