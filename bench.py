@@ -76,7 +76,8 @@ CONFIGS = {
     # 2000 steps after 600 plain ones, K = 8
     "c4": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 1.0, 1.0), lognormal=True,
                dt=2e-5, sample_n=None, surrogate=dict(n_traj=200, iters=20000, K=8, f0=50.0, warm=600,
-                                                      res_tols=(1e-6, 1e-5), sizes=(4, 5, 6, 8, 10))),
+                                                      res_tols=(1e-6, 1e-5), sizes=(4, 5, 6, 8, 10),
+                                                      stated_rel_l2=3e-4)),
 }
 
 
@@ -549,7 +550,11 @@ def main():
             return
         with ClockSampler(info["gpu"]) as clk:
             r = run_surrogate(cfg, args.steps)
-        best = max(r["runs"], key=lambda x: x["speedup_vs_plain"] if x["rel_L2_vs_plain"] < 1e-2 else 0.0)
+        # the headline: the fastest run whose final state is within the stated
+        # relative L2 distance of the plain run's
+        bar = cfg["surrogate"]["stated_rel_l2"]
+        ok_runs = [x for x in r["runs"] if x["rel_L2_vs_plain"] <= bar]
+        best = max(ok_runs or r["runs"], key=lambda x: x["speedup_vs_plain"] if ok_runs else -x["rel_L2_vs_plain"])
         line = {"metric": metric, "value": best["value"], "unit": "DOF-steps/s", "n_gpus": 1, "steps": args.steps,
                 "warmup": cfg["surrogate"]["warm"], "ms_per_step": 1e3 * best["seconds"] / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (network bf16/f32)",
@@ -557,7 +562,9 @@ def main():
                 "config": {"workload": f"surrogate K=8 on the c2 mesh at p=3: {r['n_poly']} polyhedra, dt=2e-5, "
                                        "50 Hz Ricker point source at the centre, 2000 steps after 600 plain",
                            "dofs": r["dofs"], "l2_flush": "inputs larger than L2"},
-                "plain_value": r["dofs"] * args.steps / r["t_plain"], "runs": r["runs"],
+                "plain_value": r["dofs"] * args.steps / r["t_plain"], "stated_rel_L2_vs_plain": bar,
+                "headline_run": {k: best[k] for k in ("mode", "res_tol", "speedup_vs_plain", "rel_L2_vs_plain")},
+                "runs": r["runs"],
                 "held_out_error_ratio_network_vs_taylor": [a / b for a, b in r["held_out"]],
                 "train": r["train"], "gpu_launches": r["launches"], "clocks": clk.summary()}
         print(json.dumps(line), flush=True)

@@ -285,7 +285,7 @@ int lymph_mpnn_set_gate(lymph_mpnn* net, int32_t nd, int32_t B);
  * d1, d2, a1 over its DOFs plus 1e-3 x the mesh-wide RMS); use_net = 0: the
  * extrapolation alone.  The features, normalised per polyhedron,
  * [u1/r1, d1/r2, d2/r3, a1/r4, log10 r2/r1, log10 r3/r2, log10 r4/r3,
- * log10 r1/s1, lambda, mu, rho] are built on the device: F >= 4 * 3Np + 7;
+ * lambda, mu, rho] are built on the device: F >= 4 * 3Np + 6;
  * the network's effective output is [y3 | y4] (2 * 3Np per polyhedron).
  * Afterwards V0 and UEX hold u^n, u^{n+1} (for a fallback), U0 and UN the
  * predicted u^{n+K-2}, u^{n+K-1}, and the network object the predicted

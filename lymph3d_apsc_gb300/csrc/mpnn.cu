@@ -610,7 +610,7 @@ __global__ void k_sum3(int nblk, const double* __restrict__ part, double* out) {
 // Node features of the surrogate (one row per polyhedron, F columns), all
 // normalised per polyhedron so that they do not depend on the mesh's size:
 // [u1/r1, d1/r2, d2/r3, a1/r4, log10(r2/r1), log10(r3/r2), log10(r4/r3),
-//  log10(r1/s1), lambda, mu, rho, 0...] with a1 = dt^2 M^-1 (K d1 - gdiff F)
+//  lambda, mu, rho, 0...] with a1 = dt^2 M^-1 (K d1 - gdiff F)
 // (the third difference to leading order, up to sign), r_b = the
 // polyhedron's RMS of vector b plus 1e-3 x its mesh-wide RMS s_b (a floor
 // where the field is quiet).  sig[P][b] = r_b (the per-polyhedron scales of
@@ -649,7 +649,6 @@ __global__ void __launch_bounds__(FEAT_THREADS) k_features(
         sig[(int64_t)P * 4 + tid] = r[tid];
     }
     __syncthreads();
-    const double s1 = sqrt(ss[0] / (double)n_all) + 1e-300;
     float* row = x + (int64_t)P * F;
     for (int c = tid; c < F; c += FEAT_THREADS) {
         double v = 0.0;
@@ -657,8 +656,7 @@ __global__ void __launch_bounds__(FEAT_THREADS) k_features(
         else if (c == 4 * nd) v = log10(r[1] / r[0]);
         else if (c == 4 * nd + 1) v = log10(r[2] / r[1]);
         else if (c == 4 * nd + 2) v = log10(r[3] / r[2]);
-        else if (c == 4 * nd + 3) v = log10(r[0] / s1);
-        else if (c < 4 * nd + 7) v = mat[tmat[ptets[pptr[P]]] * 3 + (c - 4 * nd - 3) % 3];
+        else if (c < 4 * nd + 6) v = mat[tmat[ptets[pptr[P]]] * 3 + (c - 4 * nd - 2) % 3];
         row[c] = (float)v;
     }
 }
@@ -977,8 +975,8 @@ namespace {
 // time function's increment g(t_{n+1}) - g(t_n).
 int surrogate_front(lymph_ctx* c, lymph_mpnn* n, bool with_features, double gdiff, const char* who) {
     const int nd = c->nd;
-    if (with_features && (n->F < 4 * nd + 7 || eff_width(n) != 2 * nd || (n->gate_B && n->gate_nd != nd))) {
-        lymph_set_error(std::string(who) + ": network shape does not match the problem (F >= 4*3Np+7, output 2*3Np)");
+    if (with_features && (n->F < 4 * nd + 6 || eff_width(n) != 2 * nd || (n->gate_B && n->gate_nd != nd))) {
+        lymph_set_error(std::string(who) + ": network shape does not match the problem (F >= 4*3Np+6, output 2*3Np)");
         return LYMPH_ERR_INVALID;
     }
     if (with_features && n->n_nodes != c->n_poly) {

@@ -43,8 +43,8 @@ G_FEATURES = 8
 
 
 def feature_width(nd: int) -> int:
-    """Feature columns for 3Np = nd: 4 nd + 7, rounded up to 16."""
-    return ((4 * nd + 7 + 15) // 16) * 16
+    """Feature columns for 3Np = nd: 4 nd + 6, rounded up to 16."""
+    return ((4 * nd + 6 + 15) // 16) * 16
 
 
 # ---------------------------------------------------------------------------
@@ -131,8 +131,7 @@ def features(um, u0, u1, a1, mat, F):
     x[:, 4 * nd] = np.log10(r[:, 1] / r[:, 0])
     x[:, 4 * nd + 1] = np.log10(r[:, 2] / r[:, 1])
     x[:, 4 * nd + 2] = np.log10(r[:, 3] / r[:, 2])
-    x[:, 4 * nd + 3] = np.log10(r[:, 0] / (s[0] + 1e-300))
-    x[:, 4 * nd + 4:4 * nd + 7] = mat[:, [1, 2, 0]]
+    x[:, 4 * nd + 3:4 * nd + 6] = mat[:, [1, 2, 0]]
     return x.astype(np.float32), tuple(s), r, d1, d2
 
 
