@@ -11,10 +11,15 @@
 // the effective output is  yg[j][i*Np + m] = sum_b alpha[j][b][i] x[b*nd + i*Np + m]
 // (nd = 3 Np): a learned per-node combination of the first B feature blocks.
 // Weight matrices are kept as FP32 masters for Adam and as BF16 copies that
-// every GEMM reads; activations and accumulation are FP32.  The concatenation
-// [h a g] is never formed: its GEMM is three GEMMs on row slices of Wu
-// accumulating into one output.  Aggregation is a CSR gather (fixed order);
-// its adjoint uses the transposed CSR, so training is deterministic.
+// every GEMM reads; activations and accumulation are FP32.  The forward GEMMs
+// run on the tcgen05 tensor cores (umma_gemm.cuh: the activations split into
+// TF32 hi and lo parts, the BF16 weights exact in TF32, FP32 accumulation in
+// tensor memory) whenever the shapes suit it, else on the FP32 SIMT kernel
+// k_gemm, which also runs the backward.  The concatenation [h a g] is never
+// formed: the tensor-core GEMM reads it as three K segments, the SIMT path as
+// three GEMMs on row slices of Wu accumulating into one output.  Aggregation
+// is a CSR gather (fixed order); its adjoint uses the transposed CSR, so
+// training is deterministic.
 
 #include <cuda_bf16.h>
 
