@@ -444,8 +444,9 @@ def run_mpnn_forward(cfg, info):
     graph = S.build_graph(m)
     N = m.n_poly
     out = {"n_nodes": N}
-    for label, simt in (("tensor_cores", "0"), ("simt", "1")):
+    for label, simt, ws in (("tensor_cores", "0", "1"), ("tensor_cores_cpasync", "0", "0"), ("simt", "1", "1")):
         os.environ["LYMPH_MPNN_SIMT"] = simt
+        os.environ["LYMPH_UMMA_WS"] = ws
         net = S.surrogate_net(cfg["p"], H=mf["H"], L=mf["L"])
         net.set_graph(graph)
         x = np.random.default_rng(0).standard_normal((N, net.F)).astype(np.float32)
@@ -460,6 +461,7 @@ def run_mpnn_forward(cfg, info):
         out["launches_per_forward"] = 1 + 2 * L + 1
         net.close()
     os.environ.pop("LYMPH_MPNN_SIMT", None)
+    os.environ.pop("LYMPH_UMMA_WS", None)
     return out
 
 
@@ -541,6 +543,7 @@ def main():
                              "peak_source": "measured bf16 / 2 (TF32 rate)",
                              "tensor_issue_tflops": 2.0 * tfl},
                 "simt_ms": r["simt"]["ms"], "speedup_vs_simt": r["simt"]["ms"] / tc["ms"],
+                "cpasync_kernel_ms": r["tensor_cores_cpasync"]["ms"],
                 "uses_tensor_cores": tc["tensor_cores"], "gpu_launches": r["launches_per_forward"] * cfg["mpnn_forward"]["reps"],
                 "clocks": tc["clocks"]}
         print(json.dumps(line), flush=True)

@@ -32,6 +32,7 @@
 
 #include "common.cuh"
 #include "umma_gemm.cuh"
+#include "umma_ws.cuh"
 
 int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);  // out = M^-1 K u (step.cu)
 
@@ -274,6 +275,7 @@ struct lymph_mpnn {
     std::vector<int64_t> wt_off;  // per entry of par (matrices only), -1 otherwise
     bool wt_dirty = true;
     bool use_umma = true;         // LYMPH_MPNN_SIMT=1 selects the SIMT GEMMs for the forward too
+    bool use_ws = true;           // LYMPH_UMMA_WS=0 selects the cp.async tensor-core kernel over the TMA one
     int* d_status = nullptr;      // bit 0: a tensor-core wait ran out
 };
 
@@ -328,20 +330,80 @@ bool umma_ok(const lymph_mpnn* n, int N, std::initializer_list<int> dims) {
     return true;
 }
 
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver (looked up once; null when absent)
+EncodeTiled encode_tiled() {
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiled)p;
+    }
+    return fn;
+}
+
+// A 2-D FP32 tensor map [rows][cols] (row stride ld floats), box 32 x box_rows,
+// 128-byte swizzle, zero fill outside the tensor.
+bool make_map(CUtensorMap* m, const float* base, int cols, int rows, int ld, int box_rows) {
+    EncodeTiled enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)umma::BK, (cuuint32_t)box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // C = sum_s A_s W_s (+ bias) with the epilogue, on the tensor cores; the
 // weight matrix is parameter `pi`, whose rows are the concatenated K of the
-// segments.
+// segments.  The warp-specialised TMA kernel runs when its tensor maps can
+// be made (and LYMPH_UMMA_WS is not 0), else the cp.async kernel.
 void umma_gemm(lymph_mpnn* n, int pi, int M, const umma::Seg* segs, int nseg, const float* bias, float* C, int ldc,
                float* Z, const float* R, int epi) {
     const auto& P = n->par[pi];
+    const int N = (int)P.cols, Npad = round16(N), Ktot = (int)P.rows;
+    const float* Bt = n->d_wt + n->wt_off[pi];
+    if (n->use_ws) {
+        umma::WsArgs w;
+        std::memset(&w, 0, sizeof(w));
+        bool ok = make_map(&w.mapB, Bt, Ktot, Npad, Ktot, Npad < umma::WS_BN ? Npad : umma::WS_BN);
+        for (int s = 0; s < nseg && ok; ++s) {
+            ok = make_map(&w.mapA[s], segs[s].A, segs[s].K, M, segs[s].lda, umma::BM);
+            w.segK[s] = segs[s].K;
+        }
+        if (ok) {
+            w.nseg = nseg; w.M = M; w.N = N; w.Npad = Npad; w.Ktot = Ktot;
+            w.bias = bias; w.C = C; w.ldc = ldc; w.Z = Z; w.R = R; w.epi = epi; w.status = n->d_status;
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(umma::k_umma_gemm_ws, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)umma::WS_SMEM);
+                attr = true;
+            }
+            const dim3 grid((M + umma::BM - 1) / umma::BM, (Npad + umma::WS_BN - 1) / umma::WS_BN);
+            umma::k_umma_gemm_ws<<<grid, umma::WS_THREADS, umma::WS_SMEM, n->stream>>>(w);
+            n->launches++;
+            return;
+        }
+    }
     umma::Args a;
     for (int s = 0; s < nseg; ++s) a.seg[s] = segs[s];
     a.nseg = nseg;
     a.M = M;
-    a.N = (int)P.cols;
-    a.Npad = round16((int)P.cols);
-    a.Bt = n->d_wt + n->wt_off[pi];
-    a.Ktot = (int)P.rows;
+    a.N = N;
+    a.Npad = Npad;
+    a.Bt = Bt;
+    a.Ktot = Ktot;
     a.bias = bias;
     a.C = C;
     a.ldc = ldc;
@@ -789,6 +851,8 @@ int lymph_mpnn_create(int32_t F, int32_t H, int32_t O, int32_t L, int32_t G, lym
     }
     const char* simt = std::getenv("LYMPH_MPNN_SIMT");
     n->use_umma = !(simt && simt[0] == '1');
+    const char* ws = std::getenv("LYMPH_UMMA_WS");
+    n->use_ws = !(ws && ws[0] == '0');
     if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) { delete n; lymph_set_error("lymph_mpnn_create: stream"); return LYMPH_ERR_CUDA; }
     size_t b = sizeof(float) * (size_t)n->n_par;
     if (cudaMalloc(&n->d_p, b) != cudaSuccess || cudaMalloc(&n->d_g, b) != cudaSuccess || cudaMalloc(&n->d_m, b) != cudaSuccess ||

@@ -116,15 +116,18 @@ def test_gradients_match_oracle(require_gpu, L, gated, F):
     net.close()
 
 
-def test_tensor_core_forward_equals_simt_on_a_large_graph(require_gpu, monkeypatch):
+@pytest.mark.parametrize("ws", ["1", "0"])
+def test_tensor_core_forward_equals_simt_on_a_large_graph(require_gpu, monkeypatch, ws):
     """1,000 nodes (8 row tiles, a partial last one), H = 256, three layers:
-    the tcgen05 forward and the SIMT forward agree to FP32 rounding (the
+    the tcgen05 forward (the TMA warp-specialised kernel, ws = 1, and the
+    cp.async kernel, ws = 0) and the SIMT forward agree to FP32 rounding (the
     activations' lo part keeps 10 of its 13 bits: ~2^-21 per operand)."""
     rng = np.random.default_rng(11)
     F, H, O, L, N = 64, 256, 24, 3, 1000
     graph = _random_graph(N, rng, 8)
     x = rng.standard_normal((N, F)).astype(np.float32)
     outs = []
+    monkeypatch.setenv("LYMPH_UMMA_WS", ws)
     for simt in ("0", "1"):
         monkeypatch.setenv("LYMPH_MPNN_SIMT", simt)
         net = S.MPNN(F, O, H=H, L=L, seed=7)
