@@ -407,13 +407,14 @@ def run_surrogate(cfg, steps):
         return math.sqrt(e / nrm)
 
     runs = []
-    for mode, nn in (("taylor", None), ("network", net)):
-        for tol in sc["res_tols"]:
+    for mode, nn, a32 in (("taylor", None, False), ("network", net, False), ("taylor_fp32_apply", None, True),
+                          ("network_fp32_apply", net, True)):
+        for tol in (sc["res_tols"] if not a32 else sc["res_tols"][:1]):
             g.set_state(_lib.SLOT_U0, u0)
             g.set_state(_lib.SLOT_UN, un)
             sync()
             a = time.perf_counter()
-            _, st = S.run_hybrid(g, nn, steps, gfun, t0, K=K, graph=graph, res_tol=tol)
+            _, st = S.run_hybrid(g, nn, steps, gfun, t0, K=K, graph=graph, res_tol=tol, apply_fp32=a32)
             sync()
             el = time.perf_counter() - a
             runs.append({"mode": mode, "res_tol": tol, "seconds": el, "speedup_vs_plain": t_plain / el,

@@ -301,6 +301,11 @@ int lymph_surrogate_predict(lymph_ctx* ctx, lymph_mpnn* net, int32_t K, int32_t 
 int lymph_surrogate_features(lymph_ctx* ctx, lymph_mpnn* net, double gdiff, float* x, double* scales, double* a1,
                              double* sig);
 
+/* The blocks of the surrogate block's operator apply (a1): on = 1 uses an
+ * FP32 copy of an FP64 context's blocks (made on first use; faster, a1 then
+ * carries FP32 rounding, ~1e-5 relative), on = 0 (default) the context's own. */
+int lymph_surrogate_apply_fp32(lymph_ctx* ctx, int32_t on);
+
 /* After one plain step from the predicted pair (U0 = u^{n+K-1}, UN = the
  * stepped u^{n+K}): residual = |UN - predicted u^{n+K}| / |UN|. */
 int lymph_surrogate_residual(lymph_ctx* ctx, lymph_mpnn* net, double* residual);

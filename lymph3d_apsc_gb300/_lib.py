@@ -121,6 +121,7 @@ _SIGS = {
     "lymph_mpnn_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_surrogate_predict": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_double, P_F64]),
     "lymph_surrogate_residual": (c_int, [c_void_p, c_void_p, P_F64]),
+    "lymph_surrogate_apply_fp32": (c_int, [c_void_p, c_int32]),
     "lymph_nodal_values": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_mpnn_set_gate": (c_int, [c_void_p, c_int32, c_int32]),
     "lymph_mpnn_time_forward": (c_int, [c_void_p, c_int32, P_F64]),

@@ -187,7 +187,7 @@ int lymph_destroy(lymph_ctx* c) {
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     void* ptrs[] = {c->d_coords, c->d_tet_vert, c->d_tet_poly, c->d_tet_mat, c->d_neigh, c->d_fun_tag, c->d_mat,
                     c->d_ref, c->d_fk, c->d_jdet, c->d_normal, c->d_area, c->d_bbox, c->d_hk, c->d_poly_ptr,
-                    c->d_poly_tets, c->d_row_ptr, c->d_col, c->d_blk_row, c->d_bf_ptr, c->d_bf, c->d_K, c->d_M,
+                    c->d_poly_tets, c->d_row_ptr, c->d_col, c->d_blk_row, c->d_bf_ptr, c->d_bf, c->d_K, c->d_K32, c->d_M,
                     c->d_Mm, c->d_R, c->d_Rm, c->d_RT, c->d_RmT, c->d_Minv, c->d_rhs_stat, c->d_rhs_dyn, c->d_buf[0], c->d_buf[1],
                     c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status};
     for (void* p : ptrs) dfree(p);
@@ -375,6 +375,7 @@ int lymph_make_matrices(lymph_ctx* c) {
         LYMPH_TRY(dalloc(c, &c->d_RmT, nm));
         LYMPH_TRY(dalloc(c, &c->d_Minv, nm));
     }
+    c->k32_valid = false;  // an FP32 copy made from earlier blocks is stale
     LYMPH_TRY(lymph_dev_assemble(c, LYMPH_BLOCKS_K, c->d_K, c->precision == LYMPH_MIXED, true));
     LYMPH_TRY(lymph_dev_cholesky(c));
     LYMPH_TRY(lymph_sync_status(c, "lymph_make_matrices"));

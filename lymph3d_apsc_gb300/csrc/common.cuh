@@ -84,6 +84,9 @@ struct lymph_ctx {
     int32_t* d_bf = nullptr;
     // operator
     void* d_K = nullptr;            // [n_blocks][nd][nd] column-major per block (FP64 or FP32)
+    float* d_K32 = nullptr;         // FP32 copy of FP64 blocks for the surrogate's operator apply (on demand)
+    bool k32_valid = false;
+    bool surrogate_apply_fp32 = false;  // lymph_surrogate_apply_fp32
     double *d_M = nullptr, *d_Mm = nullptr, *d_R = nullptr, *d_Rm = nullptr, *d_RT = nullptr, *d_RmT = nullptr;
     double* d_Minv = nullptr;       // [n_poly][Np][Np] column-major inverse of M_loc
     double *d_rhs_stat = nullptr, *d_rhs_dyn = nullptr;

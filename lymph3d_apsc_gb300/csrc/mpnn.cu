@@ -35,6 +35,8 @@
 #include "umma_ws.cuh"
 
 int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);  // out = M^-1 K u (step.cu)
+int lymph_dev_apply_fp32(lymph_ctx* c, const float* K32, const double* u, double* out);
+const float* lymph_dev_blocks_f32(lymph_ctx* c);
 
 namespace {
 
@@ -1081,7 +1083,12 @@ int surrogate_front(lymph_ctx* c, lymph_mpnn* n, bool with_features, double gdif
                                              lymph_slot_ptr(c, LYMPH_SLOT_UN), n->d_d1, n->d_d2, part);
     k_sum3<<<1, 96, 0, st>>>(SS_BLOCKS, part, ss);
     c->launches += 2;
-    LYMPH_TRY(lymph_dev_apply(c, n->d_d1, n->d_a1));
+    // the predictor term, optionally with an FP32 copy of the blocks
+    // (lymph_surrogate_apply_fp32): half the bytes streamed and no FP64 pipe,
+    // at the price of FP32 rounding in a1 (~1e-5 relative after M^-1)
+    const float* k32 = c->surrogate_apply_fp32 ? lymph_dev_blocks_f32(c) : nullptr;
+    if (k32) LYMPH_TRY(lymph_dev_apply_fp32(c, k32, n->d_d1, n->d_a1));
+    else LYMPH_TRY(lymph_dev_apply(c, n->d_d1, n->d_a1));
     k_minv_rhs<<<1024, 256, 0, st>>>(c->n_poly, c->Np, c->d_Minv, c->d_rhs_dyn, n->d_u3);  // u3: free until k_predict
     k_accel_combine<<<1024, 256, 0, st>>>(nv, c->dt * c->dt, gdiff, n->d_u3, n->d_a1);
     k_one_sumsq<<<SS_BLOCKS, 256, 0, st>>>(nv, n->d_a1, part);
@@ -1109,6 +1116,16 @@ int read_scales(lymph_ctx* c, lymph_mpnn* n, double* scales, int count) {
 }  // namespace
 
 extern "C" {
+
+// Selects the blocks of the surrogate's operator apply (the a1 term): on = 1
+// uses an FP32 copy of an FP64 context's blocks (made on first use, 4 bytes
+// per block entry of device memory; the FP64 blocks when it does not fit),
+// on = 0 (the default) the context's own blocks.
+int lymph_surrogate_apply_fp32(lymph_ctx* c, int32_t on) {
+    if (!c) return LYMPH_ERR_INVALID;
+    c->surrogate_apply_fp32 = on != 0;
+    return LYMPH_OK;
+}
 
 // The features of a block, built on the device exactly as
 // lymph_surrogate_predict builds them, copied to x (host, n_poly x F

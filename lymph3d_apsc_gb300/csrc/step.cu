@@ -155,6 +155,45 @@ int lymph_dev_apply(lymph_ctx* c, const double* u, double* out) {
     return launch_step_mode<MODE_APPLY>(c, A, c->precision == LYMPH_MIXED);
 }
 
+// out = M^-1 K u with the FP32 copy K32 of an FP64 context's blocks (the
+// surrogate's predictor term, whose own error is far above FP32 rounding).
+int lymph_dev_apply_fp32(lymph_ctx* c, const float* K32, const double* u, double* out) {
+    StepArgs A = base_args(c);
+    A.K = K32;
+    A.un = u;
+    A.u0 = u;
+    A.out = out;
+    return launch_step_p<float, MODE_APPLY>(c, A);
+}
+
+// dst[i] = (float)src[i]
+__global__ void k_blocks_to_f32(int64_t n, const double* __restrict__ src, float* dst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+// The FP32 copy of an FP64 context's blocks, made on first use (null when the
+// context is FP32 already or the copy does not fit in device memory).
+const float* lymph_dev_blocks_f32(lymph_ctx* c) {
+    if (c->precision != LYMPH_FP64 || !c->have_matrices) return nullptr;
+    const int64_t nK = c->n_blocks * (int64_t)c->nd * c->nd;
+    if (!c->d_K32) {
+        if (cudaMalloc(&c->d_K32, sizeof(float) * (size_t)nK) != cudaSuccess) {
+            cudaGetLastError();  // clear the allocation failure: the caller falls back to the FP64 blocks
+            c->d_K32 = nullptr;
+            return nullptr;
+        }
+        c->device_bytes += (int64_t)sizeof(float) * nK;
+        c->k32_valid = false;
+    }
+    if (!c->k32_valid) {
+        k_blocks_to_f32<<<4096, 256, 0, c->stream>>>(nK, (const double*)c->d_K, c->d_K32);
+        c->launches++;
+        c->k32_valid = true;
+    }
+    return c->d_K32;
+}
+
 // `iters` power iterations x <- M^-1 K x / |M^-1 K x| entirely on the
 // device; x must hold a nonzero start vector, y is scratch; *d_ss receives
 // |M^-1 K x|^2 of the last iteration (x normalised before it).

@@ -415,15 +415,18 @@ def run_plain(s: MatrixFree, n_steps: int, gfun, t: float) -> float:
 
 
 def run_hybrid(s: MatrixFree, net: MPNN | None, n_steps: int, gfun, t: float, K: int = 8, check_every: int = 64,
-               drift_tol: float = 1e-4, res_tol: float = 1e-4, graph=None, g_scale: float = 1.0):
+               drift_tol: float = 1e-4, res_tol: float = 1e-4, graph=None, g_scale: float = 1.0,
+               apply_fp32: bool = False):
     """Advances n_steps with surrogate blocks of K steps (net = None: the
     extrapolation alone).  The context holds (u^{n-1}, u^n) with u^n at time
     t on entry and on exit.  A block is forced when a source value inside it
-    exceeds 1e-9 x g_scale; its energy is then not checked.  Returns
-    (t, stats)."""
+    exceeds 1e-9 x g_scale; its energy is then not checked.  apply_fp32
+    computes the predictor's operator term with an FP32 copy of the blocks.
+    Returns (t, stats)."""
     use_net = net is not None
     if use_net:
         net.set_graph(graph, ("hybrid", id(s)))
+    check(s.lib.lymph_surrogate_apply_fp32(s.ctx, int(apply_fp32)), "lymph_surrogate_apply_fp32")
     hnet = net.h if use_net else _dummy_net().h
     stats = {"blocks": 0, "accepted": 0, "rejected": 0, "rejected_residual": 0, "rejected_energy": 0,
              "judged": 0, "judge_err_max": 0.0, "plain_steps": 0, "energy_evals": 0, "residual_max": 0.0,
