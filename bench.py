@@ -244,9 +244,34 @@ def prepare(cfg, precision):
 
 
 def step_bytes(g, precision):
-    es = {0: 8, 1: 4}[precision]
+    """Algorithmic bytes of one step: the operator blocks once, plus per
+    polyhedron u^{n-1}, u^n, u^{n+1}, the two right-hand sides and M^-1.  The
+    matrix-free neighbour path stores only the self blocks; its per-triangle
+    geometry (80 bytes per triangle side) is counted with them."""
     nd, Np = g.nd, g.Np
-    return g.n_blocks * nd * nd * es + g.n_poly * (3 * nd * 8 + 2 * Np * Np * 8 + 2 * nd * 8)
+    per_poly = g.n_poly * (3 * nd * 8 + 2 * Np * Np * 8 + 2 * nd * 8)
+    if precision == 2:
+        return g.n_poly * nd * nd * 4 + mf_triangles(g) * 80 + per_poly
+    es = {0: 8, 1: 4}[precision]
+    return g.n_blocks * nd * nd * es + per_poly
+
+
+def mf_triangles(g):
+    """Triangle sides of the neighbour blocks (each shared triangle twice)."""
+    m = g.mesh
+    e2 = m.neigh.ravel()
+    t = np.repeat(np.arange(m.n_tet), 4)
+    ok = e2 >= 0
+    return int((m.tet_poly[t[ok]] != m.tet_poly[e2[ok]]).sum())
+
+
+def mf_flops(g):
+    """FP32 FLOPs of one matrix-free neighbour apply: per quadrature point of
+    every triangle side, the field and gradient of Q (12 Np FMA), the test
+    against P's basis (12 Np FMA) and the two bases' tensor products (2 x 7 Np
+    multiplies), plus the self block's 2 (3Np)^2."""
+    nq2 = (g.degree + 1) ** 2
+    return mf_triangles(g) * nq2 * 62.0 * g.Np + 2.0 * g.n_poly * g.nd * g.nd
 
 
 def step_flops(g):
@@ -261,7 +286,7 @@ def errors(g, t):
 
 
 ERROR_STEPS = 1000
-DTYPES = {0: "f64", 1: "f32-blocks/f64"}
+DTYPES = {0: "f64", 1: "f32-blocks/f64", 2: "f32 self blocks + matrix-free f32 face terms/f64"}
 
 
 def run_gpu(cfg, precision, steps, warmup, rank_info, want_e2e=True):
@@ -281,6 +306,8 @@ def run_gpu(cfg, precision, steps, warmup, rank_info, want_e2e=True):
     out = {"dofs": dofs, "steps": n, "ms": ms, "kernel_ms_avg": mk / n2, "launches": launches,
            "clocks": clk.summary(), "n_blocks": g.n_blocks, "n_poly": g.n_poly, "n_tet": m.n_tet, "Np": g.Np,
            "bytes": step_bytes(g, precision), "flops": step_flops(g), "t": t}
+    if precision == 2:
+        out["mf_flops"] = mf_flops(g)
     # errors after ERROR_STEPS steps in all (the configurations' 1000-step
     # runs), the same step count for every precision
     done = 1 + nw + n + n2
@@ -496,7 +523,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_mf"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison run")
     args = ap.parse_args()
@@ -523,7 +550,7 @@ def main():
         print(json.dumps(line), flush=True)
         return
 
-    precision = {"fp64": 0, "mixed": 1}[args.precision]
+    precision = {"fp64": 0, "mixed": 1, "mixed_mf": 2}[args.precision]
     if cfg.get("mpnn_forward"):
         if info["rank"] != 0:
             return
@@ -598,7 +625,7 @@ def main():
     value = total_dof_steps / (r["ms"] / 1e3)
     peak, peak_kind = measured_peaks()
     achieved = r["bytes"] / (r["kernel_ms_avg"] / 1e3) / 1e9
-    traffic = step_traffic_per_launch(args.config + {0: "", 1: "_mixed"}[precision], r["n_blocks"])
+    traffic = step_traffic_per_launch(args.config + {0: "", 1: "_mixed", 2: "_mixed_mf"}[precision], r["n_blocks"])
     line = {
         "metric": metric, "value": value, "unit": "DOF-steps/s", "n_gpus": info["world"], "steps": r["steps"],
         "warmup": args.warmup, "ms_per_step": r["ms"] / r["steps"], "higher_is_better": True,
@@ -631,7 +658,7 @@ def main():
         line["cpu_baseline"] = {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",
                                 "sample": cb["sample"]}
     if info["rank"] == 0 and precision == 0 and not args.no_mixed:
-        for key, prec in (("mixed", 1),):
+        for key, prec in (("mixed", 1), ("mixed_mf", 2)):
             rm = run_gpu(cfg, prec, args.steps, args.warmup, {**info, "barrier": lambda: None, "max": lambda x: x},
                          want_e2e=False)
             vm = rm["dofs"] * rm["steps"] / (rm["ms"] / 1e3)
@@ -641,6 +668,9 @@ def main():
                          "error_after_steps": rm["error_steps"], "kernel_ms": rm["kernel_ms_avg"],
                          "achieved_gbs": rm["bytes"] / (rm["kernel_ms_avg"] / 1e3) / 1e9,
                          "bytes_per_launch": rm["bytes"]}
+            if "mf_flops" in rm:
+                line[key]["fp32_tflops"] = rm["mf_flops"] / (rm["kernel_ms_avg"] / 1e3) / 1e12
+                line[key]["flops_per_launch"] = rm["mf_flops"]
     if info["rank"] == 0:
         print(json.dumps(line), flush=True)
     if info.get("dist"):

@@ -59,6 +59,14 @@ extern "C" {
 #define LYMPH_MIXED  1   /* operator blocks and their mat-vec in FP32, FP32
                             accumulation; geometry, assembly, mass inverse,
                             time update and error norms in FP64 */
+#define LYMPH_MIXED_MF 2  /* FP32 self blocks; the neighbour terms evaluated
+                            matrix-free in FP32 at every step from the face
+                            quadrature (Q's field and gradient at P's
+                            quadrature points, tested against P's basis), so no
+                            neighbour block is stored or read; FP32
+                            accumulation, FP64 combine, mass inverse, update
+                            and error norms.  Not accepted by
+                            lymph_batch_create. */
 
 /* ---- state slots (the driver's arrays, src/Lymph3D.f90:237-239) --------- */
 #define LYMPH_SLOT_U0   0   /* u0_loc: u^{n-1} (u^0 before the first step)   */
@@ -126,7 +134,7 @@ typedef struct lymph_mesh_desc {
 
 typedef struct lymph_params {
     int32_t degree;     /* polynomial degree p, 1..6 (Elem_loc%Degree)        */
-    int32_t precision;  /* LYMPH_FP64 or LYMPH_MIXED                          */
+    int32_t precision;  /* LYMPH_FP64, LYMPH_MIXED or LYMPH_MIXED_MF          */
     double  alpha;      /* penalty constant (set_properties: 10)              */
     double  theta;      /* -1 SIPG, 0 IIPG, 1 NIPG (set_properties: -1)       */
     double  dt;         /* time step (Poly.input TIMESTEP)                    */

@@ -34,6 +34,7 @@ MESH_UNMATCHED = -9
 
 FP64 = 0
 MIXED = 1
+MIXED_MF = 2  # FP32 self blocks, neighbour terms matrix-free from face quadrature
 
 SLOT_U0, SLOT_UN, SLOT_V0, SLOT_UEX = 0, 1, 2, 3
 LAYOUT_POLY_MAJOR, LAYOUT_FORTRAN = 0, 1

@@ -19,6 +19,9 @@
 // kernels (setup.cu, step.cu)
 int lymph_dev_geometry(lymph_ctx* c);
 int lymph_dev_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass);
+int lymph_dev_assemble_list(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass, const int64_t* list,
+                            int64_t n_list, int64_t out_stride);
+int lymph_mf_setup(lymph_ctx* c, const RefTables& R);
 int lymph_dev_cholesky(lymph_ctx* c);
 int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scale, double* out);
 int lymph_dev_step(lymph_ctx* c, bool bump);
@@ -171,6 +174,7 @@ int lymph_sync_status(lymph_ctx* c, const char* where) {
     if (st & ST_NOT_SPD) { lymph_set_error(w + ": Matrix is not positive definite!"); return LYMPH_EXIT_SINGULARMTX; }
     if (st & ST_DEGENERATE) { lymph_set_error(w + ": degenerate tetrahedron or face"); return LYMPH_EXIT_SETUP; }
     if (st & ST_NONFINITE) { lymph_set_error(w + ": non-finite value in the state"); return LYMPH_EXIT_INSTAB; }
+    if (st & ST_TIMEOUT) { lymph_set_error(w + ": a bounded wait on an asynchronous copy expired"); return LYMPH_ERR_TIMEOUT; }
     lymph_set_error(w + ": device status " + std::to_string(st));
     return LYMPH_ERR_CUDA;
 }
@@ -189,7 +193,8 @@ int lymph_destroy(lymph_ctx* c) {
                     c->d_ref, c->d_fk, c->d_jdet, c->d_normal, c->d_area, c->d_bbox, c->d_hk, c->d_poly_ptr,
                     c->d_poly_tets, c->d_row_ptr, c->d_col, c->d_blk_row, c->d_bf_ptr, c->d_bf, c->d_K, c->d_K32, c->d_M,
                     c->d_Mm, c->d_R, c->d_Rm, c->d_RT, c->d_RmT, c->d_Minv, c->d_rhs_stat, c->d_rhs_dyn, c->d_buf[0], c->d_buf[1],
-                    c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status};
+                    c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status,
+                    c->d_mf_tri, c->d_mf_poly};
     for (void* p : ptrs) dfree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -207,7 +212,7 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
         lymph_set_error("lymph_create: degree must be 1..4 on the device");
         return LYMPH_ERR_INVALID;
     }
-    if (prm->precision != LYMPH_FP64 && prm->precision != LYMPH_MIXED) {
+    if (prm->precision != LYMPH_FP64 && prm->precision != LYMPH_MIXED && prm->precision != LYMPH_MIXED_MF) {
         lymph_set_error("lymph_create: unknown precision");
         return LYMPH_ERR_INVALID;
     }
@@ -353,8 +358,56 @@ int lymph_sizes(const lymph_ctx* c, int32_t* Np, int32_t* n_poly, int64_t* n_blo
     return LYMPH_OK;
 }
 
+// Matrix-free neighbour terms: the FP32 self blocks (assembled alone, into
+// consecutive slots) and the per-triangle / per-polyhedron FP32 tables.
+static int make_mf_matrices(lymph_ctx* c) {
+    const int np = c->n_poly, nd = c->nd;
+    const size_t nK = (size_t)np * nd * nd;
+    if (!c->d_K) {
+        void* pK = nullptr;
+        if (cudaMalloc(&pK, nK * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            lymph_set_error("lymph_make_matrices: cannot allocate " + std::to_string(nK * sizeof(float)) +
+                            " bytes of self blocks");
+            return LYMPH_ERR_OOM;
+        }
+        c->d_K = pK;
+        c->device_bytes += (int64_t)(nK * sizeof(float));
+    }
+    std::vector<int64_t> self(np);
+    for (int P = 0; P < np; ++P) self[P] = c->h_row_ptr[P];
+    int64_t* d_list = nullptr;
+    LYMPH_CUDA_TRY(cudaMalloc(&d_list, sizeof(int64_t) * (size_t)np));
+    int rc = cudaMemcpy(d_list, self.data(), sizeof(int64_t) * (size_t)np, cudaMemcpyHostToDevice) == cudaSuccess
+                 ? LYMPH_OK : LYMPH_ERR_CUDA;
+    if (rc == LYMPH_OK) rc = lymph_dev_assemble_list(c, LYMPH_BLOCKS_K, c->d_K, 1, true, d_list, np, (int64_t)nd * nd);
+    if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+    cudaFree(d_list);
+    LYMPH_TRY(rc);
+    RefTables R;
+    if (!build_ref_tables(c->p, R)) { lymph_set_error("lymph_make_matrices: no quadrature for this degree"); return LYMPH_ERR_INVALID; }
+    return lymph_mf_setup(c, R);
+}
+
 int lymph_make_matrices(lymph_ctx* c) {
     if (!c) return LYMPH_ERR_INVALID;
+    if (c->precision == LYMPH_MIXED_MF) {
+        if (!c->d_M) {
+            size_t nm = (size_t)c->n_poly * c->Np * c->Np;
+            LYMPH_TRY(dalloc(c, &c->d_M, nm));
+            LYMPH_TRY(dalloc(c, &c->d_Mm, nm));
+            LYMPH_TRY(dalloc(c, &c->d_R, nm));
+            LYMPH_TRY(dalloc(c, &c->d_RT, nm));
+            LYMPH_TRY(dalloc(c, &c->d_Rm, nm));
+            LYMPH_TRY(dalloc(c, &c->d_RmT, nm));
+            LYMPH_TRY(dalloc(c, &c->d_Minv, nm));
+        }
+        LYMPH_TRY(make_mf_matrices(c));
+        LYMPH_TRY(lymph_dev_cholesky(c));
+        LYMPH_TRY(lymph_sync_status(c, "lymph_make_matrices"));
+        c->have_matrices = true;
+        return LYMPH_OK;
+    }
     size_t es = (c->precision == LYMPH_MIXED) ? sizeof(float) : sizeof(double);
     size_t nK = (size_t)c->n_blocks * c->nd * c->nd;
     if (!c->d_K) {
@@ -507,6 +560,7 @@ int lymph_run_steps(lymph_ctx* c, double stop_time, int64_t max_steps, double* t
                     lymph_dev_step(c, true);
                     c->cur ^= 1;
                 }
+                c->graph_launches = c->launches - l0;
                 c->launches = l0;
                 cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
                 c->cur = cur0;
@@ -521,7 +575,7 @@ int lymph_run_steps(lymph_ctx* c, double stop_time, int64_t max_steps, double* t
             // the parity is the same after every launch
             for (; i + R <= n; i += R) {
                 LYMPH_CUDA_TRY(cudaGraphLaunch(c->graph_exec, c->stream));
-                c->launches += 2 * R;
+                c->launches += c->graph_launches;
             }
         }
         for (; i < n; ++i) {
@@ -637,7 +691,17 @@ int lymph_get_blocks(lymph_ctx* c, int which, double* vals) {
     const int nd = c->nd;
     size_t nK = (size_t)c->n_blocks * nd * nd;
     std::vector<double> tmp(nK);
-    if (which == LYMPH_BLOCKS_K && c->precision == LYMPH_MIXED) {
+    if (which == LYMPH_BLOCKS_K && c->precision == LYMPH_MIXED_MF) {
+        // the operator the matrix-free path evaluates: the FP64 assembly of
+        // every block (the neighbour blocks are not stored in this mode)
+        double* A = nullptr;
+        if (cudaMalloc(&A, nK * sizeof(double)) != cudaSuccess) { lymph_set_error("lymph_get_blocks: out of memory"); return LYMPH_ERR_OOM; }
+        int rc = lymph_dev_assemble(c, LYMPH_BLOCKS_K, A, 0, false);
+        if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+        if (rc == LYMPH_OK && cudaMemcpy(tmp.data(), A, nK * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+        cudaFree(A);
+        LYMPH_TRY(rc);
+    } else if (which == LYMPH_BLOCKS_K && c->precision == LYMPH_MIXED) {
         std::vector<float> tf(nK);
         LYMPH_CUDA_TRY(cudaMemcpy(tf.data(), c->d_K, nK * sizeof(float), cudaMemcpyDeviceToHost));
         for (size_t i = 0; i < nK; ++i) tmp[i] = tf[i];

@@ -259,6 +259,7 @@ int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out) {
         if (!ctxs[i]) { lymph_set_error("lymph_batch_create: null context"); return LYMPH_ERR_INVALID; }
         if (!ctxs[i]->have_matrices) { lymph_set_error("lymph_batch_create: every context needs lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
         if (ctxs[i]->precision != ctxs[0]->precision) { lymph_set_error("lymph_batch_create: mixed precisions in one batch"); return LYMPH_ERR_INVALID; }
+        if (ctxs[i]->precision == LYMPH_MIXED_MF) { lymph_set_error("lymph_batch_create: matrix-free neighbour terms are not batched (use LYMPH_FP64 or LYMPH_MIXED)"); return LYMPH_ERR_INVALID; }
     }
     lymph_batch* b = new lymph_batch();
     b->ctx.assign(ctxs, ctxs + n);

@@ -36,6 +36,7 @@ enum : int {
     ST_NONFINITE = 2,    // NaN/Inf in a state vector
     ST_BAD_INDEX = 4,    // an index failed its bounds check
     ST_DEGENERATE = 8,   // zero-volume tetrahedron / zero-area face
+    ST_TIMEOUT = 16,     // a bounded wait on an asynchronous copy expired
 };
 
 constexpr int MAX_DEGREE = 4;     // device path supports p = 1..4 (Np <= 35)
@@ -89,6 +90,13 @@ struct lymph_ctx {
     bool surrogate_apply_fp32 = false;  // lymph_surrogate_apply_fp32
     double *d_M = nullptr, *d_Mm = nullptr, *d_R = nullptr, *d_Rm = nullptr, *d_RT = nullptr, *d_RmT = nullptr;
     double* d_Minv = nullptr;       // [n_poly][Np][Np] column-major inverse of M_loc
+    // matrix-free neighbour terms (LYMPH_MIXED_MF): d_K holds the n_poly FP32
+    // self blocks; d_mf_tri the FP32 geometry of every neighbour-block
+    // triangle (parallel to d_bf), d_mf_poly the Legendre map of every
+    // bounding box, mf_quad the triangle quadrature (xi, eta, w)
+    void* d_mf_tri = nullptr;
+    void* d_mf_poly = nullptr;
+    float mf_quad[3 * 25] = {};
     double *d_rhs_stat = nullptr, *d_rhs_dyn = nullptr;
     // state: two rotating step buffers + V0 + UEX
     double* d_buf[2] = {nullptr, nullptr};
@@ -106,6 +114,7 @@ struct lymph_ctx {
     int64_t device_bytes = 0;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_steps = 0;
+    int64_t graph_launches = 0;     // kernel launches one graph launch stands for
     int graph_parity = -1;
 };
 

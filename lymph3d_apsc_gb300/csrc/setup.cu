@@ -146,7 +146,9 @@ struct AsmArgs {
     double alpha, theta;
     int which;        // LYMPH_BLOCKS_K or LYMPH_BLOCKS_ADG
     int out_fp32;     // store FP32 blocks
-    void* out;        // [n_blocks][ND][ND] column-major
+    void* out;        // [n][out_stride] blocks, each [ND][ND] column-major
+    const int64_t* list;  // blocks to assemble (null: all, in order); output slot = position in the list
+    int64_t out_stride;   // elements from one output block to the next (>= ND*ND)
     double* M;        // [n_poly][NP][NP] rho-weighted mass (self blocks only; may be null)
     double* Mm;       // unweighted (modal) mass
     int64_t block0;   // first block of this launch
@@ -163,7 +165,8 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
     double* acc = sm;                   // [ND][ND] row-major
     double* tab = acc + ND * ND;        // tabulation area
     const int tid = threadIdx.x;
-    const int64_t k = A.block0 + blockIdx.x;
+    const int64_t slot = A.block0 + blockIdx.x;
+    const int64_t k = A.list ? A.list[slot] : slot;
     const int P = A.blk_row[k];
     const int Qc = A.col[k];
     const bool self = (Qc == P);
@@ -362,7 +365,7 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
     }
     __syncthreads();
     // write the block column-major (entry (r,c) at c*ND + r)
-    const int64_t base = k * (int64_t)ND * ND;
+    const int64_t base = slot * A.out_stride;
     if (A.out_fp32) {
         float* o = (float*)A.out;
         for (int i = tid; i < ND * ND; i += ASM_THREADS) {
@@ -730,7 +733,8 @@ __global__ void k_double_couple(int Np, int nq3, int t, int P, const double* __r
 }
 
 template <int PD>
-int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {
+int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass, const int64_t* list,
+                    int64_t n_list, int64_t out_stride) {
     size_t smem = asm_smem<PD>();
     LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_assemble<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     AsmArgs A;
@@ -740,10 +744,12 @@ int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write
     A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.alpha = c->alpha; A.theta = c->theta;
     A.which = which; A.out_fp32 = out_fp32; A.out = out;
     A.M = write_mass ? c->d_M : nullptr; A.Mm = write_mass ? c->d_Mm : nullptr;
+    A.list = list; A.out_stride = out_stride;
+    const int64_t n = list ? n_list : c->n_blocks;
     const int64_t chunk = 1 << 20;
-    for (int64_t b0 = 0; b0 < c->n_blocks; b0 += chunk) {
+    for (int64_t b0 = 0; b0 < n; b0 += chunk) {
         A.block0 = b0;
-        int64_t nb = c->n_blocks - b0 < chunk ? c->n_blocks - b0 : chunk;
+        int64_t nb = n - b0 < chunk ? n - b0 : chunk;
         k_assemble<PD><<<(unsigned)nb, ASM_THREADS, smem, c->stream>>>(A);
         c->launches++;
         LYMPH_CUDA_TRY(cudaGetLastError());
@@ -788,14 +794,21 @@ int lymph_dev_geometry(lymph_ctx* c) {
     return LYMPH_OK;
 }
 
-int lymph_dev_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {
+// Blocks list[0..n_list) (all blocks in order when list is null) into
+// consecutive output slots out_stride elements apart.
+int lymph_dev_assemble_list(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass, const int64_t* list,
+                            int64_t n_list, int64_t out_stride) {
     switch (c->p) {
-        case 1: return launch_assemble<1>(c, which, out, out_fp32, write_mass);
-        case 2: return launch_assemble<2>(c, which, out, out_fp32, write_mass);
-        case 3: return launch_assemble<3>(c, which, out, out_fp32, write_mass);
-        case 4: return launch_assemble<4>(c, which, out, out_fp32, write_mass);
+        case 1: return launch_assemble<1>(c, which, out, out_fp32, write_mass, list, n_list, out_stride);
+        case 2: return launch_assemble<2>(c, which, out, out_fp32, write_mass, list, n_list, out_stride);
+        case 3: return launch_assemble<3>(c, which, out, out_fp32, write_mass, list, n_list, out_stride);
+        case 4: return launch_assemble<4>(c, which, out, out_fp32, write_mass, list, n_list, out_stride);
         default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
     }
+}
+
+int lymph_dev_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {
+    return lymph_dev_assemble_list(c, which, out, out_fp32, write_mass, nullptr, 0, (int64_t)c->nd * c->nd);
 }
 
 int lymph_dev_cholesky(lymph_ctx* c) {

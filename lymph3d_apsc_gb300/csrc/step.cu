@@ -114,6 +114,20 @@ int launch_step_mode(lymph_ctx* c, const StepArgs& A, bool fp32) {
     return fp32 ? launch_step_p<float, MODE>(c, A) : launch_step_p<double, MODE>(c, A);
 }
 
+}  // namespace
+
+int lymph_dev_mf(lymph_ctx* c, int mode, const stepk::StepArgs& A);
+
+namespace {
+
+// The operator pass of a step mode in the context's precision: the fused
+// block-CSR kernel (FP64 or FP32 blocks) or the matrix-free neighbour kernel.
+template <int MODE>
+int launch_ctx(lymph_ctx* c, const StepArgs& A) {
+    if (c->precision == LYMPH_MIXED_MF) return lymph_dev_mf(c, MODE, A);
+    return launch_step_mode<MODE>(c, A, c->precision == LYMPH_MIXED);
+}
+
 StepArgs base_args(lymph_ctx* c) {
     StepArgs A;
     A.row_ptr = c->d_row_ptr; A.col = c->d_col; A.K = c->d_K; A.Minv = c->d_Minv;
@@ -132,7 +146,7 @@ int lymph_dev_step(lymph_ctx* c, bool bump) {
     A.u0 = c->d_buf[c->cur ^ 1];
     A.un = c->d_buf[c->cur];
     A.out = c->d_buf[c->cur ^ 1];
-    LYMPH_TRY(launch_step_mode<MODE_STEP>(c, A, c->precision == LYMPH_MIXED));
+    LYMPH_TRY(launch_ctx<MODE_STEP>(c, A));
     if (bump) {
         k_bump<<<1, 1, 0, c->stream>>>(c->d_step_idx);
         c->launches++;
@@ -152,7 +166,7 @@ int lymph_dev_apply(lymph_ctx* c, const double* u, double* out) {
     A.un = u;
     A.u0 = u;
     A.out = out;
-    return launch_step_mode<MODE_APPLY>(c, A, c->precision == LYMPH_MIXED);
+    return launch_ctx<MODE_APPLY>(c, A);
 }
 
 // out = M^-1 K u with the FP32 copy K32 of an FP64 context's blocks (the
@@ -220,7 +234,7 @@ int lymph_dev_first_step(lymph_ctx* c) {
     A.u0 = c->d_buf[c->cur ^ 1];
     A.un = c->d_v0;
     A.out = c->d_buf[c->cur];
-    return launch_step_mode<MODE_FIRST>(c, A, c->precision == LYMPH_MIXED);
+    return launch_ctx<MODE_FIRST>(c, A);
 }
 
 // du . (A du) per polyhedron with FP64 A_dg blocks in `blocks`, then the sum.
@@ -244,7 +258,7 @@ int lymph_dev_energy(lymph_ctx* c, const double* ua, const double* ub, double* d
     StepArgs A = base_args(c);
     A.u0 = ua;
     A.un = ub;
-    LYMPH_TRY(launch_step_mode<MODE_BILIN>(c, A, c->precision == LYMPH_MIXED));
+    LYMPH_TRY(launch_ctx<MODE_BILIN>(c, A));
     k_sum<<<1, 1024, 0, c->stream>>>(c->n_poly, c->d_partial, d_out + 1);
     c->launches += 3;
     LYMPH_CUDA_TRY(cudaGetLastError());

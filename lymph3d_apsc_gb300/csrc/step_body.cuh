@@ -58,14 +58,73 @@ template <int PD, typename KT> struct SmemSize {
     static constexpr size_t bytes = b_offset + sizeof(double) * ND;
 };
 
-// The block row of polyhedron P is one contiguous column-major
-// [ND x nb*ND] matrix (its blocks are adjacent in memory), multiplied by the
-// gathered coefficients of the column polyhedra.  The mass-matrix inverse is
+// The end of one polyhedron's step once thread tid < ND holds y = (K u)_tid
+// of row tid in FP64: the right-hand side, the mass-matrix inverse and the
+// leapfrog update (or the bilinear/DG partial sum).  The mass-matrix inverse is
 // applied in FP64 as a dense Np x Np product per component (precomputed from
 // the Cholesky factor), which replaces the reference's two triangular solves
-// per component with a parallel product of the same value.  Every thread of
-// the CTA must call this (it synchronises); threads beyond the degree's
-// shape only help with the gather.
+// per component with a parallel product of the same value.  s_b holds ND
+// doubles, 16-byte aligned.  Every thread of the CTA must call this (it
+// synchronises).
+template <int PD, int MODE>
+__device__ __forceinline__ void finish_poly(const StepArgs& A, int P, double y, double* s_b) {
+    constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND;
+    const int tid = threadIdx.x;
+    if (MODE == MODE_DG || MODE == MODE_BILIN) {
+        if (tid < ND) s_b[tid] = y;
+        __syncthreads();
+        if (tid == 0) {
+            double e = 0.0;
+            for (int rr = 0; rr < ND; ++rr) {
+                const int64_t q = (int64_t)P * ND + rr;
+                e = e + (MODE == MODE_DG ? (A.u0[q] - A.un[q]) : A.un[q]) * s_b[rr];
+            }
+            A.partial[P] = e;
+        }
+        return;
+    }
+    if (tid < ND) {
+        const int64_t q = (int64_t)P * ND + tid;
+        if (MODE == MODE_APPLY) {
+            s_b[tid] = y;
+        } else {
+            const double g = A.gvals[*A.step_idx];
+            s_b[tid] = -y + A.rhs_stat[q] + A.rhs_dyn[q] * g;
+        }
+    }
+    __syncthreads();
+    if (tid < ND) {
+        const int i = tid / NP, m = tid % NP;
+        const double* Mi = A.Minv + (int64_t)P * NP * NP + m;
+        const double* bi = s_b + i * NP;
+        double x0 = 0.0, x1 = 0.0;
+#pragma unroll
+        for (int c = 0; c < NP; c += 2) {
+            x0 += Mi[c * NP] * bi[c];
+            if (c + 1 < NP) x1 += Mi[(c + 1) * NP] * bi[c + 1];
+        }
+        const double x = x0 + x1;
+        const int64_t q = (int64_t)P * ND + tid;
+        double v;
+        if (MODE == MODE_STEP) {
+            const double dt2 = A.dt * A.dt;
+            v = dt2 * x + 2.0 * A.un[q] - A.u0[q];
+        } else if (MODE == MODE_FIRST) {
+            const double half_dt2 = 0.5 * (A.dt * A.dt);
+            v = half_dt2 * x + A.u0[q] + A.dt * A.un[q];
+        } else {
+            v = x;
+        }
+        if (!isfinite(v)) atomicOr(A.status, ST_NONFINITE);
+        A.out[q] = v;
+    }
+}
+
+// The block row of polyhedron P is one contiguous column-major
+// [ND x nb*ND] matrix (its blocks are adjacent in memory), multiplied by the
+// gathered coefficients of the column polyhedra, then finish_poly.  Every
+// thread of the CTA must call this (it synchronises); threads beyond the
+// degree's shape only help with the gather.
 template <int PD, typename KT, int MODE>
 __device__ __forceinline__ void step_poly(const StepArgs& A, int P, char* smem) {
     constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND, S = Shape<PD>::S;
@@ -119,56 +178,10 @@ __device__ __forceinline__ void step_poly(const StepArgs& A, int P, char* smem) 
     }
     if (act) s_red[s * ND + r] = acc0 + acc1;
     __syncthreads();
-    if (MODE == MODE_DG || MODE == MODE_BILIN) {
-        if (tid == 0) {
-            double e = 0.0;
-            for (int rr = 0; rr < ND; ++rr) {
-                double y = 0.0;
-                for (int ss = 0; ss < S; ++ss) y += (double)s_red[ss * ND + rr];
-                const int64_t q = (int64_t)P * ND + rr;
-                e = e + (MODE == MODE_DG ? (A.u0[q] - A.un[q]) : A.un[q]) * y;
-            }
-            A.partial[P] = e;
-        }
-        return;
-    }
-    if (tid < ND) {
-        double y = 0.0;
+    double y = 0.0;
+    if (tid < ND)
         for (int ss = 0; ss < S; ++ss) y += (double)s_red[ss * ND + tid];
-        const int64_t q = (int64_t)P * ND + tid;
-        if (MODE == MODE_APPLY) {
-            s_b[tid] = y;
-        } else {
-            const double g = A.gvals[*A.step_idx];
-            s_b[tid] = -y + A.rhs_stat[q] + A.rhs_dyn[q] * g;
-        }
-    }
-    __syncthreads();
-    if (tid < ND) {
-        const int i = tid / NP, m = tid % NP;
-        const double* Mi = A.Minv + (int64_t)P * NP * NP + m;
-        const double* bi = s_b + i * NP;
-        double x0 = 0.0, x1 = 0.0;
-#pragma unroll
-        for (int c = 0; c < NP; c += 2) {
-            x0 += Mi[c * NP] * bi[c];
-            if (c + 1 < NP) x1 += Mi[(c + 1) * NP] * bi[c + 1];
-        }
-        const double x = x0 + x1;
-        const int64_t q = (int64_t)P * ND + tid;
-        double v;
-        if (MODE == MODE_STEP) {
-            const double dt2 = A.dt * A.dt;
-            v = dt2 * x + 2.0 * A.un[q] - A.u0[q];
-        } else if (MODE == MODE_FIRST) {
-            const double half_dt2 = 0.5 * (A.dt * A.dt);
-            v = half_dt2 * x + A.u0[q] + A.dt * A.un[q];
-        } else {
-            v = x;
-        }
-        if (!isfinite(v)) atomicOr(A.status, ST_NONFINITE);
-        A.out[q] = v;
-    }
+    finish_poly<PD, MODE>(A, P, y, s_b);
 }
 
 }  // namespace stepk

@@ -34,7 +34,8 @@ class MatrixFree:
     """One PolyDG elastodynamics problem on the GPU.
 
     Parameters mirror set_properties (alpha=10, theta=-1) and the Poly.input
-    TIMESTEP; `precision` is _lib.FP64 (plain) or _lib.MIXED.
+    TIMESTEP; `precision` is _lib.FP64 (plain), _lib.MIXED (FP32 blocks) or
+    _lib.MIXED_MF (FP32 self blocks, neighbour terms matrix-free in FP32).
     """
 
     def __init__(self, mesh: Mesh, degree: int, dt: float, alpha: float = 10.0, theta: float = -1.0,

@@ -135,6 +135,8 @@ def test_create_rejects_bad_input_with_status_codes():
     prm = _lib.Params(2, _lib.FP64, 10.0, -1.0, -1.0)
     assert lib.lymph_create(byref(d), byref(prm), byref(h)) == _lib.LYMPH_ERR_INVALID
     assert lib.lymph_create(None, byref(prm), byref(h)) == _lib.LYMPH_ERR_INVALID
+    prm = _lib.Params(2, 7, 10.0, -1.0, 1e-3)  # unknown precision
+    assert lib.lymph_create(byref(d), byref(prm), byref(h)) == _lib.LYMPH_ERR_INVALID
 
 
 def test_create_without_device_fails_loudly():
