@@ -57,14 +57,14 @@ struct MfPoly {         // Legendre map of a bounding box: xp = (x - c) ih, phi 
 static_assert(sizeof(MfPoly) == 32, "MfPoly is 8 words");
 
 constexpr int MF_THREADS = 128;
+constexpr int MF_SLOTS = MF_THREADS / 3;   // test phase: point slots of three lanes (one per row component)
 
 template <int PD> struct MfShape {
     static constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND;
     static constexpr int L = PD + 1;              // Legendre degrees per direction
     static constexpr int NQ2 = L * L;             // quadrature points per triangle
     static constexpr int CT = MF_THREADS / NQ2;   // triangles per chunk
-    static constexpr int NPT = CT * NQ2;          // points per chunk
-    static constexpr int PARTS = MF_THREADS / NP; // point slices of the test phase
+    static constexpr int NPT = CT * NQ2;          // points per chunk (one evaluating thread each)
     static_assert(ND <= MF_THREADS, "one thread per row of the self block");
 };
 
@@ -85,11 +85,12 @@ template <int PD> struct Blist {
     }
 };
 
-// Legendre polynomials L_0..L_PD on [-1, 1] and their derivatives at x
-// (Bonnet's recurrence; the reference evaluates the same polynomials in
-// closed form, basis_function.f90:268-437).
+// Legendre polynomials L_0..L_PD on [-1, 1] and their derivatives at x,
+// as (L, L') pairs (Bonnet's recurrence; the reference evaluates the same
+// polynomials in closed form, basis_function.f90:268-437).
 template <int PD>
-__device__ __forceinline__ void legendre(float x, float* Lv, float* Ld) {
+__device__ __forceinline__ void legendre(float x, float2* out) {
+    float Lv[PD + 1], Ld[PD + 1];
     Lv[0] = 1.0f;
     Ld[0] = 0.0f;
     if (PD >= 1) {
@@ -101,6 +102,73 @@ __device__ __forceinline__ void legendre(float x, float* Lv, float* Ld) {
         Lv[n + 1] = ((2 * n + 1) * x * Lv[n] - n * Lv[n - 1]) * (1.0f / (n + 1));
         Ld[n + 1] = Ld[n - 1] + (2 * n + 1) * Lv[n];
     }
+#pragma unroll
+    for (int n = 0; n <= PD; ++n) out[n] = make_float2(Lv[n], Ld[n]);
+}
+
+// Field and gradient of one component at a point by sum factorisation over
+// the basis triples (a, b, c): with X_a = (L_a, L'_a)(x) and likewise Y, Z,
+//   w0_ab = sum_c u_abc Z_c,  w1_ab = sum_c u_abc Z'_c,
+//   r0_a = sum_b w0_ab Y_b,  r1_a = sum_b w0_ab Y'_b,  r2_a = sum_b w1_ab Y_b,
+//   v = sum_a r0_a X_a, d_x = sum_a r0_a X'_a, d_y = sum_a r1_a X_a, d_z = sum_a r2_a X_a
+// (unscaled: the caller applies the bounding-box factors); uc[4 i] is the
+// coefficient of basis function i.
+template <int PD>
+__device__ __forceinline__ void eval_sf(const float* uc, const float2* X, const float2* Y, const float2* Z, float& v,
+                                        float& dx, float& dy, float& dz) {
+    constexpr Blist<PD> BL{};
+    constexpr int NP = Deg<PD>::NP;
+    float w0[PD + 1][PD + 1], w1[PD + 1][PD + 1];
+#pragma unroll
+    for (int a = 0; a <= PD; ++a)
+#pragma unroll
+        for (int b = 0; b <= PD; ++b) { w0[a][b] = 0.0f; w1[a][b] = 0.0f; }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const int a = BL.d[i][0], b = BL.d[i][1], c = BL.d[i][2];
+        const float uu = uc[4 * i];
+        w0[a][b] = fmaf(uu, Z[c].x, w0[a][b]);
+        w1[a][b] = fmaf(uu, Z[c].y, w1[a][b]);
+    }
+    v = dx = dy = dz = 0.0f;
+#pragma unroll
+    for (int a = 0; a <= PD; ++a) {
+        float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+#pragma unroll
+        for (int b = 0; b <= PD - a; ++b) {
+            r0 = fmaf(w0[a][b], Y[b].x, r0);
+            r1 = fmaf(w0[a][b], Y[b].y, r1);
+            r2 = fmaf(w1[a][b], Y[b].x, r2);
+        }
+        v = fmaf(r0, X[a].x, v);
+        dx = fmaf(r0, X[a].y, dx);
+        dy = fmaf(r1, X[a].x, dy);
+        dz = fmaf(r2, X[a].x, dz);
+    }
+}
+
+// The transpose: acc_abc += X'_a Y_b Z_c gx + X_a Y'_b Z_c gy + X_a Y_b Z'_c gz
+// + X_a Y_b Z_c s, factored the same way.
+template <int PD>
+__device__ __forceinline__ void test_sf(float* acc, const float2* X, const float2* Y, const float2* Z, float gx, float gy,
+                                        float gz, float s) {
+    constexpr Blist<PD> BL{};
+    constexpr int NP = Deg<PD>::NP;
+    float q0[PD + 1][PD + 1], q1[PD + 1][PD + 1];
+#pragma unroll
+    for (int a = 0; a <= PD; ++a) {
+        const float t0 = fmaf(X[a].y, gx, X[a].x * s), t1 = X[a].x * gy, t2 = X[a].x * gz;
+#pragma unroll
+        for (int b = 0; b <= PD - a; ++b) {
+            q0[a][b] = fmaf(Y[b].x, t0, Y[b].y * t1);
+            q1[a][b] = Y[b].x * t2;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const int a = BL.d[i][0], b = BL.d[i][1], c = BL.d[i][2];
+        acc[i] = fmaf(Z[c].x, q0[a][b], fmaf(Z[c].y, q1[a][b], acc[i]));
+    }
 }
 
 struct MfArgs {
@@ -109,16 +177,24 @@ struct MfArgs {
     const int64_t* bf_ptr;      // per block: its triangles in tri[]
     const MfTri* tri;           // parallel to the block face lists
     const MfPoly* poly;         // [n_poly]
-    const double* u;            // operator input
+    const float4* u32;          // operator input in FP32: [n_poly][Np] (u_0, u_1, u_2, 0)
     float quad[3 * 25];         // (xi, eta, w) of the triangle quadrature points
     float theta;
 };
 
+// One CTA per polyhedron P.  Self block: thread r < ND forms row r of
+// K_PP u_P from the streamed FP32 block.  Neighbour triangles, CT triangles
+// at a time (their geometry, Q's box and Q's FP32 coefficients staged in
+// shared memory): thread t evaluates point t -- Q's field and gradient
+// component by component by sum factorisation, the three flux rows, and P's
+// Legendre values, both kept in shared memory; then thread 3 k + i
+// accumulates row component i of P's test sums over the points k, k + 42,
+// ... of the chunk in Np registers (the sum-factorised transpose).  The 42
+// slots' partial rows are summed in a fixed order at the end.
 template <int PD, int MODE>
-__global__ void __launch_bounds__(MF_THREADS) k_mf(const __grid_constant__ MfArgs A) {
+__global__ void __launch_bounds__(MF_THREADS, 4) k_mf(const __grid_constant__ MfArgs A) {
     using S = MfShape<PD>;
-    constexpr int NP = S::NP, ND = S::ND, L = S::L, NQ2 = S::NQ2, CT = S::CT, NPT = S::NPT, PARTS = S::PARTS;
-    constexpr Blist<PD> BL{};
+    constexpr int NP = S::NP, ND = S::ND, L = S::L, NQ2 = S::NQ2, CT = S::CT, NPT = S::NPT;
     __shared__ __align__(16) float s_quad[3 * NQ2];
     __shared__ __align__(16) float s_uP[ND];
     __shared__ __align__(16) MfTri s_tri[CT];
@@ -126,13 +202,16 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf(const __grid_constant__ MfArg
     __shared__ __align__(16) float4 s_uQ[CT][NP];            // (u_0, u_1, u_2, 0) per basis function
     __shared__ __align__(16) float2 s_leg[NPT][3][L];        // P's (L, L') per point, direction, degree
     __shared__ __align__(16) float4 s_flux[NPT][3];          // (G_i0, G_i1, G_i2, s_i) per point, scaled by P's map
-    __shared__ __align__(16) float s_red[PARTS][ND];
+    __shared__ __align__(16) float s_red[MF_SLOTS][ND];
     __shared__ __align__(16) double s_b[ND];
     const int P = blockIdx.x, tid = threadIdx.x;
-    const double* u = A.u;
 
     for (int i = tid; i < 3 * NQ2; i += MF_THREADS) s_quad[i] = A.quad[i];
-    for (int i = tid; i < ND; i += MF_THREADS) s_uP[i] = (float)u[(int64_t)P * ND + i];
+    for (int i = tid; i < ND; i += MF_THREADS) {
+        const float4 w = A.u32[(int64_t)P * NP + i % NP];
+        const int comp = i / NP;
+        s_uP[i] = comp == 0 ? w.x : (comp == 1 ? w.y : w.z);
+    }
     __syncthreads();
 
     // ---- self block (FP32, streamed once) ----
@@ -150,14 +229,11 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf(const __grid_constant__ MfArg
 
     // ---- neighbour triangles ----
     const MfPoly pP = A.poly[P];
-    const int ta = tid % NP, tpart = tid / NP;  // test phase: basis function, point slice
-    int ax = 0, ay = 0, az = 0;
-    if (tpart < PARTS) {
+    const int slot = tid / 3, ci = tid - 3 * (tid / 3);   // test phase: point slot, row component
+    const bool tact = slot < MF_SLOTS;
+    float acc[NP];
 #pragma unroll
-        for (int b = 0; b < NP; ++b)
-            if (b == ta) { ax = BL.d[b][0]; ay = BL.d[b][1]; az = BL.d[b][2]; }
-    }
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f;
+    for (int i = 0; i < NP; ++i) acc[i] = 0.0f;
     const int rb = A.s.row_ptr[P], re = A.s.row_ptr[P + 1];
     const int64_t fb = A.bf_ptr[rb + 1], fe = A.bf_ptr[re];
     for (int64_t c0 = fb; c0 < fe; c0 += CT) {
@@ -168,15 +244,14 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf(const __grid_constant__ MfArg
             float* dst = (float*)s_tri;
             for (int i = tid; i < nt * 20; i += MF_THREADS) dst[i] = src[i];
         }
-        __syncthreads();
+        // Q's box and coefficients, Q read from global (no barrier after the copy above)
         for (int i = tid; i < nt * 8; i += MF_THREADS) {
             const int t = i / 8, w = i % 8;
-            ((float*)&s_polyQ[t])[w] = ((const float*)(A.poly + s_tri[t].Q))[w];
+            ((float*)&s_polyQ[t])[w] = ((const float*)(A.poly + A.tri[c0 + t].Q))[w];
         }
         for (int i = tid; i < nt * NP; i += MF_THREADS) {
             const int t = i / NP, b = i % NP;
-            const double* uq = u + (int64_t)s_tri[t].Q * ND + b;
-            s_uQ[t][b] = make_float4((float)uq[0], (float)uq[NP], (float)uq[2 * NP], 0.0f);
+            s_uQ[t][b] = A.u32[(int64_t)A.tri[c0 + t].Q * NP + b];
         }
         __syncthreads();
         // ---- per point: u_Q and grad u_Q, the flux, P's Legendre values ----
@@ -189,31 +264,22 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf(const __grid_constant__ MfArg
 #pragma unroll
             for (int d = 0; d < 3; ++d) x[d] = fmaf(eta, T.e2[d], fmaf(xi, T.e1[d], T.o[d]));
             const MfPoly& pq = s_polyQ[t];
-            float Lx[L], Dx[L], Ly[L], Dy[L], Lz[L], Dz[L];
-            legendre<PD>((x[0] - pq.c[0]) * pq.ih[0], Lx, Dx);
-            legendre<PD>((x[1] - pq.c[1]) * pq.ih[1], Ly, Dy);
-            legendre<PD>((x[2] - pq.c[2]) * pq.ih[2], Lz, Dz);
-            float v0 = 0, v1 = 0, v2 = 0;
-            float d00 = 0, d01 = 0, d02 = 0, d10 = 0, d11 = 0, d12 = 0, d20 = 0, d21 = 0, d22 = 0;
-#pragma unroll
-            for (int b = 0; b < NP; ++b) {
-                const int bx = BL.d[b][0], by = BL.d[b][1], bz = BL.d[b][2];
-                const float yz = Ly[by] * Lz[bz];
-                const float ph = Lx[bx] * yz;
-                const float px = Dx[bx] * yz;
-                const float py = Lx[bx] * (Dy[by] * Lz[bz]);
-                const float pz = Lx[bx] * (Ly[by] * Dz[bz]);
-                const float4 uu = s_uQ[t][b];
-                v0 = fmaf(ph, uu.x, v0); v1 = fmaf(ph, uu.y, v1); v2 = fmaf(ph, uu.z, v2);
-                d00 = fmaf(px, uu.x, d00); d01 = fmaf(py, uu.x, d01); d02 = fmaf(pz, uu.x, d02);
-                d10 = fmaf(px, uu.y, d10); d11 = fmaf(py, uu.y, d11); d12 = fmaf(pz, uu.y, d12);
-                d20 = fmaf(px, uu.z, d20); d21 = fmaf(py, uu.z, d21); d22 = fmaf(pz, uu.z, d22);
-            }
+            float2 X[L], Y[L], Z[L];
+            legendre<PD>((x[0] - pq.c[0]) * pq.ih[0], X);
+            legendre<PD>((x[1] - pq.c[1]) * pq.ih[1], Y);
+            legendre<PD>((x[2] - pq.c[2]) * pq.ih[2], Z);
             // Q's map: phi = sc L L L, d_k phi = sc ih_k (...)
             const float sq = pq.sc, gx = sq * pq.ih[0], gy = sq * pq.ih[1], gz = sq * pq.ih[2];
-            const float v[3] = {v0 * sq, v1 * sq, v2 * sq};
-            const float D[3][3] = {{d00 * gx, d01 * gy, d02 * gz}, {d10 * gx, d11 * gy, d12 * gz},
-                                   {d20 * gx, d21 * gy, d22 * gz}};
+            float v[3], D[3][3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                float vj, dx, dy, dz;
+                eval_sf<PD>(&s_uQ[t][0].x + j, X, Y, Z, vj, dx, dy, dz);
+                v[j] = vj * sq;
+                D[j][0] = dx * gx;
+                D[j][1] = dy * gy;
+                D[j][2] = dz * gz;
+            }
             const float* n = T.n;
             const float nv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
             const float trD = D[0][0] + D[1][1] + D[2][2];
@@ -236,43 +302,49 @@ __global__ void __launch_bounds__(MF_THREADS) k_mf(const __grid_constant__ MfArg
                 const float s = -W * (T.sigma * Tv + 0.5f * h);
                 s_flux[tid][i] = make_float4(G[0] * hx, G[1] * hy, G[2] * hz, s * sP);
             }
-            legendre<PD>((x[0] - pP.c[0]) * pP.ih[0], Lx, Dx);
-            legendre<PD>((x[1] - pP.c[1]) * pP.ih[1], Ly, Dy);
-            legendre<PD>((x[2] - pP.c[2]) * pP.ih[2], Lz, Dz);
-#pragma unroll
-            for (int l = 0; l < L; ++l) {
-                s_leg[tid][0][l] = make_float2(Lx[l], Dx[l]);
-                s_leg[tid][1][l] = make_float2(Ly[l], Dy[l]);
-                s_leg[tid][2][l] = make_float2(Lz[l], Dz[l]);
-            }
+            legendre<PD>((x[0] - pP.c[0]) * pP.ih[0], s_leg[tid][0]);
+            legendre<PD>((x[1] - pP.c[1]) * pP.ih[1], s_leg[tid][1]);
+            legendre<PD>((x[2] - pP.c[2]) * pP.ih[2], s_leg[tid][2]);
         }
         __syncthreads();
-        // ---- test against P's basis: thread (a, slice) over the chunk's points ----
-        if (tpart < PARTS) {
-            for (int pt = tpart; pt < nt * NQ2; pt += PARTS) {
-                const float2 lx = s_leg[pt][0][ax], ly = s_leg[pt][1][ay], lz = s_leg[pt][2][az];
-                const float yz = ly.x * lz.x;
-                const float ph = lx.x * yz, px = lx.y * yz, py = lx.x * (ly.y * lz.x), pz = lx.x * (ly.x * lz.y);
-                const float4 f0 = s_flux[pt][0], f1 = s_flux[pt][1], f2 = s_flux[pt][2];
-                acc0 = fmaf(px, f0.x, fmaf(py, f0.y, fmaf(pz, f0.z, fmaf(ph, f0.w, acc0))));
-                acc1 = fmaf(px, f1.x, fmaf(py, f1.y, fmaf(pz, f1.z, fmaf(ph, f1.w, acc1))));
-                acc2 = fmaf(px, f2.x, fmaf(py, f2.y, fmaf(pz, f2.z, fmaf(ph, f2.w, acc2))));
+        // ---- test against P's basis: thread (slot, component) over the chunk's points ----
+        if (tact) {
+            for (int pt = slot; pt < nt * NQ2; pt += MF_SLOTS) {
+                float2 X[L], Y[L], Z[L];
+#pragma unroll
+                for (int l = 0; l < L; ++l) {
+                    X[l] = s_leg[pt][0][l];
+                    Y[l] = s_leg[pt][1][l];
+                    Z[l] = s_leg[pt][2][l];
+                }
+                const float4 f = s_flux[pt][ci];
+                test_sf<PD>(acc, X, Y, Z, f.x, f.y, f.z, f.w);
             }
         }
     }
-    if (tpart < PARTS) {
-        s_red[tpart][ta] = acc0;
-        s_red[tpart][NP + ta] = acc1;
-        s_red[tpart][2 * NP + ta] = acc2;
+    if (tact) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i) s_red[slot][ci * NP + i] = acc[i];
     }
     __syncthreads();
     double y = 0.0;
     if (tid < ND) {
-        y = (double)yself;
-#pragma unroll
-        for (int k = 0; k < PARTS; ++k) y += (double)s_red[k][tid];
+        float t = 0.0f;
+#pragma unroll 6
+        for (int k = 0; k < MF_SLOTS; ++k) t += s_red[k][tid];
+        y = (double)yself + (double)t;
     }
     finish_poly<PD, MODE>(A.s, P, y, s_b);
+}
+
+// u32[P][m] = (u[P][0][m], u[P][1][m], u[P][2][m], 0): the operator input in
+// FP32, converted once per pass instead of once per triangle that reads it.
+__global__ void k_mf_u32(int64_t n, int NP, const double* __restrict__ u, float4* __restrict__ u32) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t P = i / NP, m = i - P * NP;
+        const double* up = u + P * 3 * NP + m;
+        u32[i] = make_float4((float)up[0], (float)up[NP], (float)up[2 * NP], 0.0f);
+    }
 }
 
 // Per-triangle geometry of every neighbour block (FP64 set-up data rounded to
@@ -349,7 +421,7 @@ int launch_mf_t(lymph_ctx* c, const StepArgs& s) {
     a.bf_ptr = c->d_bf_ptr;
     a.tri = (const MfTri*)c->d_mf_tri;
     a.poly = (const MfPoly*)c->d_mf_poly;
-    a.u = (MODE == MODE_FIRST || MODE == MODE_BILIN) ? s.u0 : s.un;
+    a.u32 = (const float4*)c->d_mf_u32;
     for (int i = 0; i < 3 * 25; ++i) a.quad[i] = c->mf_quad[i];
     a.theta = (float)c->theta;
     k_mf<PD, MODE><<<c->n_poly, MF_THREADS, 0, c->stream>>>(a);
@@ -359,6 +431,11 @@ int launch_mf_t(lymph_ctx* c, const StepArgs& s) {
 
 template <int PD>
 int launch_mf_p(lymph_ctx* c, int mode, const StepArgs& s) {
+    const double* u = (mode == MODE_FIRST || mode == MODE_BILIN) ? s.u0 : s.un;
+    const int64_t n = (int64_t)c->n_poly * c->Np;
+    const int64_t nb = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    k_mf_u32<<<(unsigned)nb, 256, 0, c->stream>>>(n, c->Np, u, (float4*)c->d_mf_u32);
+    c->launches++;
     switch (mode) {
         case MODE_STEP: return launch_mf_t<PD, MODE_STEP>(c, s);
         case MODE_FIRST: return launch_mf_t<PD, MODE_FIRST>(c, s);
@@ -388,6 +465,9 @@ int lymph_mf_setup(lymph_ctx* c, const RefTables& R) {
         LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(MfPoly) * (size_t)c->n_poly));
         c->d_mf_poly = p;
         c->device_bytes += (int64_t)(sizeof(MfPoly) * c->n_poly);
+        LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(float4) * (size_t)c->n_poly * c->Np));
+        c->d_mf_u32 = p;
+        c->device_bytes += (int64_t)(sizeof(float4) * c->n_poly * c->Np);
     }
     if (c->n_blocks > 0) {
         k_mf_tris<<<(unsigned)((c->n_blocks + 127) / 128), 128, 0, c->stream>>>(
