@@ -192,7 +192,7 @@ struct MfArgs {
 // ... of the chunk in Np registers (the sum-factorised transpose).  The 42
 // slots' partial rows are summed in a fixed order at the end.
 template <int PD, int MODE>
-__global__ void __launch_bounds__(MF_THREADS, 4) k_mf(const __grid_constant__ MfArgs A) {
+__global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ MfArgs A) {
     using S = MfShape<PD>;
     constexpr int NP = S::NP, ND = S::ND, L = S::L, NQ2 = S::NQ2, CT = S::CT, NPT = S::NPT;
     __shared__ __align__(16) float s_quad[3 * NQ2];
