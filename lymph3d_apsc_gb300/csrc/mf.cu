@@ -178,54 +178,103 @@ struct MfArgs {
     const MfTri* tri;           // parallel to the block face lists
     const MfPoly* poly;         // [n_poly]
     const float4* u32;          // operator input in FP32: [n_poly][Np] (u_0, u_1, u_2, 0)
+    int64_t kself_bytes;        // size of Kself
+    int64_t minv_bytes;         // size of the M^-1 array
     float quad[3 * 25];         // (xi, eta, w) of the triangle quadrature points
     float theta;
 };
 
-// One CTA per polyhedron P.  Self block: thread r < ND forms row r of
-// K_PP u_P from the streamed FP32 block.  Neighbour triangles, CT triangles
-// at a time (their geometry, Q's box and Q's FP32 coefficients staged in
-// shared memory): thread t evaluates point t -- Q's field and gradient
+constexpr int MF_MAXT = 64;   // triangles whose neighbour index is kept in shared memory
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Prefetch [p, p + bytes) of an allocation [base, base + total) into L2 (one
+// bulk prefetch, range widened to 16-byte bounds inside the allocation).
+__device__ __forceinline__ void prefetch_l2(const void* base, int64_t total, const void* p, int64_t bytes) {
+    const uintptr_t b0 = (uintptr_t)base, lim = (b0 + (uintptr_t)total) & ~(uintptr_t)15;
+    uintptr_t s = (uintptr_t)p & ~(uintptr_t)15, e = ((uintptr_t)p + (uintptr_t)bytes + 15) & ~(uintptr_t)15;
+    if (e > lim) e = lim;
+    if (s < b0 || e <= s) return;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s), "r"((uint32_t)(e - s)) : "memory");
+}
+
+// One CTA per polyhedron P.  At the start one thread prefetches into L2 what
+// the end of the CTA reads (the FP32 self block, M^-1, the right-hand sides
+// and the state rows), so those reads do not wait on HBM.  Neighbour
+// triangles, CT triangles at a time, their geometry, Q's box and Q's FP32
+// coefficients copied into shared memory with cp.async one chunk ahead
+// (double-buffered): thread t evaluates point t -- Q's field and gradient
 // component by component by sum factorisation, the three flux rows, and P's
-// Legendre values, both kept in shared memory; then thread 3 k + i
-// accumulates row component i of P's test sums over the points k, k + 42,
-// ... of the chunk in Np registers (the sum-factorised transpose).  The 42
-// slots' partial rows are summed in a fixed order at the end.
+// Legendre values, kept in shared memory; then thread 3 k + i accumulates
+// row component i of P's test sums over the points k, k + 42, ... of the
+// chunk in Np registers (the sum-factorised transpose).  Then the self-block
+// rows (thread r < ND, K_PP streamed from L2) and the 42 slots' partial rows,
+// summed in a fixed order.
 template <int PD, int MODE>
 __global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ MfArgs A) {
     using S = MfShape<PD>;
-    constexpr int NP = S::NP, ND = S::ND, L = S::L, NQ2 = S::NQ2, CT = S::CT, NPT = S::NPT;
+    constexpr int NP = S::NP, ND = S::ND, L = S::L, NQ2 = S::NQ2, CT = S::CT, NPT = S::NPT, NP2 = NP * NP;
+    struct Loop {
+        float2 leg[NPT][3][L];    // P's (L, L') per point, direction, degree
+        float4 flux[NPT][3];      // (G_i0, G_i1, G_i2, s_i) per point, scaled by P's map
+    };
+    union Work {
+        Loop loop;
+        float red[MF_SLOTS][ND];  // after the face loop: the slots' partial rows
+    };
+    __shared__ __align__(16) Work s_w;
     __shared__ __align__(16) float s_quad[3 * NQ2];
     __shared__ __align__(16) float s_uP[ND];
-    __shared__ __align__(16) MfTri s_tri[CT];
-    __shared__ __align__(16) MfPoly s_polyQ[CT];
-    __shared__ __align__(16) float4 s_uQ[CT][NP];            // (u_0, u_1, u_2, 0) per basis function
-    __shared__ __align__(16) float2 s_leg[NPT][3][L];        // P's (L, L') per point, direction, degree
-    __shared__ __align__(16) float4 s_flux[NPT][3];          // (G_i0, G_i1, G_i2, s_i) per point, scaled by P's map
-    __shared__ __align__(16) float s_red[MF_SLOTS][ND];
+    __shared__ __align__(16) int s_Q[MF_MAXT];
+    __shared__ __align__(16) MfTri s_tri[2][CT];
+    __shared__ __align__(16) MfPoly s_polyQ[2][CT];
+    __shared__ __align__(16) float4 s_uQ[2][CT][NP];         // (u_0, u_1, u_2, 0) per basis function
     __shared__ __align__(16) double s_b[ND];
     const int P = blockIdx.x, tid = threadIdx.x;
+    const int rb = A.s.row_ptr[P], re = A.s.row_ptr[P + 1];
+    const int64_t fb = A.bf_ptr[rb + 1], fe = A.bf_ptr[re];
+    const int ntri = (int)(fe - fb);
 
+    if (tid == 0) {
+        const int64_t nb = (int64_t)ND * ND * 4, vb = (int64_t)ND * 8;
+        prefetch_l2(A.Kself, A.kself_bytes, A.Kself + (int64_t)P * ND * ND, nb);
+        prefetch_l2(A.s.Minv, A.minv_bytes, A.s.Minv + (int64_t)P * NP2, (int64_t)NP2 * 8);
+        const int64_t sb = (int64_t)A.s.n_poly * ND * 8;
+        if (MODE == MODE_STEP || MODE == MODE_FIRST) {
+            prefetch_l2(A.s.rhs_stat, sb, A.s.rhs_stat + (int64_t)P * ND, vb);
+            prefetch_l2(A.s.rhs_dyn, sb, A.s.rhs_dyn + (int64_t)P * ND, vb);
+        }
+        prefetch_l2(A.s.u0, sb, A.s.u0 + (int64_t)P * ND, vb);
+        prefetch_l2(A.s.un, sb, A.s.un + (int64_t)P * ND, vb);
+    }
     for (int i = tid; i < 3 * NQ2; i += MF_THREADS) s_quad[i] = A.quad[i];
     for (int i = tid; i < ND; i += MF_THREADS) {
         const float4 w = A.u32[(int64_t)P * NP + i % NP];
         const int comp = i / NP;
         s_uP[i] = comp == 0 ? w.x : (comp == 1 ? w.y : w.z);
     }
+    for (int i = tid; i < ntri && i < MF_MAXT; i += MF_THREADS) s_Q[i] = A.tri[fb + i].Q;
     __syncthreads();
 
-    // ---- self block (FP32, streamed once) ----
-    float yself = 0.0f;
-    if (tid < ND) {
-        const float* Kb = A.Kself + (int64_t)P * ND * ND + tid;
-        float a0 = 0.0f, a1 = 0.0f;
-#pragma unroll 8
-        for (int c = 0; c < ND; c += 2) {
-            a0 = fmaf(__ldcs(Kb + (int64_t)c * ND), s_uP[c], a0);
-            if (c + 1 < ND) a1 = fmaf(__ldcs(Kb + (int64_t)(c + 1) * ND), s_uP[c + 1], a1);
+    // neighbour of triangle i of P (shared memory for the first MF_MAXT)
+    auto getQ = [&](int i) -> int { return i < MF_MAXT ? s_Q[i] : A.tri[fb + i].Q; };
+    auto stage = [&](int c, int b) {  // chunk starting at triangle c into buffer b
+        const int nt = (ntri - c) < CT ? ntri - c : CT;
+        const char* src = (const char*)(A.tri + fb + c);
+        for (int i = tid; i < nt * 5; i += MF_THREADS) cp_async16((char*)s_tri[b] + 16 * i, src + 16 * i);
+        for (int i = tid; i < nt * 2; i += MF_THREADS)
+            cp_async16((char*)&s_polyQ[b][i / 2] + 16 * (i & 1), (const char*)(A.poly + getQ(c + i / 2)) + 16 * (i & 1));
+        for (int i = tid; i < nt * NP; i += MF_THREADS) {
+            const int t = i / NP, bb = i - t * NP;
+            cp_async16(&s_uQ[b][t][bb], A.u32 + (int64_t)getQ(c + t) * NP + bb);
         }
-        yself = a0 + a1;
-    }
+        cp_async_commit();
+    };
 
     // ---- neighbour triangles ----
     const MfPoly pP = A.poly[P];
@@ -234,36 +283,23 @@ __global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ Mf
     float acc[NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) acc[i] = 0.0f;
-    const int rb = A.s.row_ptr[P], re = A.s.row_ptr[P + 1];
-    const int64_t fb = A.bf_ptr[rb + 1], fe = A.bf_ptr[re];
-    for (int64_t c0 = fb; c0 < fe; c0 += CT) {
-        const int nt = (fe - c0) < CT ? (int)(fe - c0) : CT;
-        __syncthreads();  // the previous chunk's staging is consumed
-        {
-            const float* src = (const float*)(A.tri + c0);
-            float* dst = (float*)s_tri;
-            for (int i = tid; i < nt * 20; i += MF_THREADS) dst[i] = src[i];
-        }
-        // Q's box and coefficients, Q read from global (no barrier after the copy above)
-        for (int i = tid; i < nt * 8; i += MF_THREADS) {
-            const int t = i / 8, w = i % 8;
-            ((float*)&s_polyQ[t])[w] = ((const float*)(A.poly + A.tri[c0 + t].Q))[w];
-        }
-        for (int i = tid; i < nt * NP; i += MF_THREADS) {
-            const int t = i / NP, b = i % NP;
-            s_uQ[t][b] = A.u32[(int64_t)A.tri[c0 + t].Q * NP + b];
-        }
-        __syncthreads();
+    if (ntri > 0) stage(0, 0);
+    for (int c = 0, k = 0; c < ntri; c += CT, ++k) {
+        const int b = k & 1, nt = (ntri - c) < CT ? ntri - c : CT;
+        if (c + CT < ntri) stage(c + CT, b ^ 1);
+        else cp_async_commit();
+        cp_async_wait<1>();
+        __syncthreads();  // chunk c staged for all threads; the previous test phase is done
         // ---- per point: u_Q and grad u_Q, the flux, P's Legendre values ----
         if (tid < nt * NQ2) {
             const int t = tid / NQ2, q = tid % NQ2;
-            const MfTri& T = s_tri[t];
+            const MfTri& T = s_tri[b][t];
             const float xi = s_quad[3 * q], eta = s_quad[3 * q + 1];
             const float W = s_quad[3 * q + 2] * T.area;
             float x[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) x[d] = fmaf(eta, T.e2[d], fmaf(xi, T.e1[d], T.o[d]));
-            const MfPoly& pq = s_polyQ[t];
+            const MfPoly& pq = s_polyQ[b][t];
             float2 X[L], Y[L], Z[L];
             legendre<PD>((x[0] - pq.c[0]) * pq.ih[0], X);
             legendre<PD>((x[1] - pq.c[1]) * pq.ih[1], Y);
@@ -274,7 +310,7 @@ __global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ Mf
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 float vj, dx, dy, dz;
-                eval_sf<PD>(&s_uQ[t][0].x + j, X, Y, Z, vj, dx, dy, dz);
+                eval_sf<PD>(&s_uQ[b][t][0].x + j, X, Y, Z, vj, dx, dy, dz);
                 v[j] = vj * sq;
                 D[j][0] = dx * gx;
                 D[j][1] = dy * gy;
@@ -292,7 +328,8 @@ __global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ Mf
             for (int i = 0; i < 3; ++i) {
                 float G[3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) G[k] = cg * ((i == k ? T.lam * nv : 0.0f) + T.mu * (n[i] * v[k] + v[i] * n[k]));
+                for (int kk = 0; kk < 3; ++kk)
+                    G[kk] = cg * ((i == kk ? T.lam * nv : 0.0f) + T.mu * (n[i] * v[kk] + v[i] * n[kk]));
                 float Tv = Tdiag[i] * v[i];
 #pragma unroll
                 for (int j = 0; j < 3; ++j)
@@ -300,11 +337,11 @@ __global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ Mf
                 const float h = T.lam * (n[0] * D[0][i] + n[1] * D[1][i] + n[2] * D[2][i]) + T.mu * n[i] * trD +
                                 T.mu * (n[0] * D[i][0] + n[1] * D[i][1] + n[2] * D[i][2]);
                 const float s = -W * (T.sigma * Tv + 0.5f * h);
-                s_flux[tid][i] = make_float4(G[0] * hx, G[1] * hy, G[2] * hz, s * sP);
+                s_w.loop.flux[tid][i] = make_float4(G[0] * hx, G[1] * hy, G[2] * hz, s * sP);
             }
-            legendre<PD>((x[0] - pP.c[0]) * pP.ih[0], s_leg[tid][0]);
-            legendre<PD>((x[1] - pP.c[1]) * pP.ih[1], s_leg[tid][1]);
-            legendre<PD>((x[2] - pP.c[2]) * pP.ih[2], s_leg[tid][2]);
+            legendre<PD>((x[0] - pP.c[0]) * pP.ih[0], s_w.loop.leg[tid][0]);
+            legendre<PD>((x[1] - pP.c[1]) * pP.ih[1], s_w.loop.leg[tid][1]);
+            legendre<PD>((x[2] - pP.c[2]) * pP.ih[2], s_w.loop.leg[tid][2]);
         }
         __syncthreads();
         // ---- test against P's basis: thread (slot, component) over the chunk's points ----
@@ -313,25 +350,39 @@ __global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ Mf
                 float2 X[L], Y[L], Z[L];
 #pragma unroll
                 for (int l = 0; l < L; ++l) {
-                    X[l] = s_leg[pt][0][l];
-                    Y[l] = s_leg[pt][1][l];
-                    Z[l] = s_leg[pt][2][l];
+                    X[l] = s_w.loop.leg[pt][0][l];
+                    Y[l] = s_w.loop.leg[pt][1][l];
+                    Z[l] = s_w.loop.leg[pt][2][l];
                 }
-                const float4 f = s_flux[pt][ci];
+                const float4 f = s_w.loop.flux[pt][ci];
                 test_sf<PD>(acc, X, Y, Z, f.x, f.y, f.z, f.w);
             }
         }
     }
+    cp_async_wait<0>();
+    // ---- self block (FP32, from L2) ----
+    float yself = 0.0f;
+    if (tid < ND) {
+        const float* Kb = A.Kself + (int64_t)P * ND * ND + tid;
+        float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll 8
+        for (int c = 0; c < ND; c += 2) {
+            a0 = fmaf(__ldcs(Kb + (int64_t)c * ND), s_uP[c], a0);
+            if (c + 1 < ND) a1 = fmaf(__ldcs(Kb + (int64_t)(c + 1) * ND), s_uP[c + 1], a1);
+        }
+        yself = a0 + a1;
+    }
+    __syncthreads();  // the loop buffers are free: reuse them for the slots' rows
     if (tact) {
 #pragma unroll
-        for (int i = 0; i < NP; ++i) s_red[slot][ci * NP + i] = acc[i];
+        for (int i = 0; i < NP; ++i) s_w.red[slot][ci * NP + i] = acc[i];
     }
     __syncthreads();
     double y = 0.0;
     if (tid < ND) {
         float t = 0.0f;
 #pragma unroll 6
-        for (int k = 0; k < MF_SLOTS; ++k) t += s_red[k][tid];
+        for (int kk = 0; kk < MF_SLOTS; ++kk) t += s_w.red[kk][tid];
         y = (double)yself + (double)t;
     }
     finish_poly<PD, MODE>(A.s, P, y, s_b);
@@ -422,6 +473,8 @@ int launch_mf_t(lymph_ctx* c, const StepArgs& s) {
     a.tri = (const MfTri*)c->d_mf_tri;
     a.poly = (const MfPoly*)c->d_mf_poly;
     a.u32 = (const float4*)c->d_mf_u32;
+    a.kself_bytes = (int64_t)c->n_poly * c->nd * c->nd * (int64_t)sizeof(float);
+    a.minv_bytes = (int64_t)c->n_poly * c->Np * c->Np * (int64_t)sizeof(double);
     for (int i = 0; i < 3 * 25; ++i) a.quad[i] = c->mf_quad[i];
     a.theta = (float)c->theta;
     k_mf<PD, MODE><<<c->n_poly, MF_THREADS, 0, c->stream>>>(a);
