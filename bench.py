@@ -66,6 +66,10 @@ CONFIGS = {
     # 48k polyhedra, p = 4, lognormal lambda/mu per polyhedron
     "c2": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=4, material=(1.0, 1.0, 1.0), lognormal=True,
                dt=2e-5, sample_n=8),
+    # a 16^3 x 6 cut of c2 (2,976 polyhedra, p = 4, lognormal lambda / mu): the
+    # small case the ncu captures of the matrix-free neighbour kernel use
+    "c2s": dict(n=16, agglomeration="bfs", group=(4, 12), seed=0, p=4, material=(1.0, 1.0, 1.0), lognormal=True,
+                dt=2e-5, sample_n=6),
     # the surrogate network's forward on the c2 mesh (46,767 polyhedra, p = 3
     # features, H = 256, 3 layers, gated head): its GEMMs on tcgen05 tensor cores
     "c4f": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 1.0, 1.0), lognormal=True,
