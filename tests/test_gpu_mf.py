@@ -90,6 +90,50 @@ def test_mf_operator_and_steps_close_to_fp64(require_gpu, kind, p):
         x.close()
 
 
+def _big_polyhedron_mesh():
+    """5^3 hexahedra x 6 tets, one polyhedron per hexahedron, except the central
+    3 x 3 x 3 block of hexahedra, which is one polyhedron of 162 tetrahedra with
+    108 triangles shared with neighbours (more than the 64 whose neighbour index
+    the kernel keeps in shared memory)."""
+    from lymph3d_apsc_gb300 import mesh as M
+    m = M.cube(5, bc="dirichlet", agglomeration="hex", material=(1.0, 2.0, 1.0), jitter=0.1)
+    cell = np.clip(np.floor(m.coords[m.tet_vert].mean(axis=1) * 5).astype(int), 0, 4)
+    inner = np.all((cell >= 1) & (cell <= 3), axis=1)
+    tp = m.tet_poly.copy()
+    tp[inner] = -1
+    _, tp[~inner] = np.unique(tp[~inner], return_inverse=True)
+    tp[inner] = tp[~inner].max() + 1
+    return m.with_polyhedra(tp)
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_mf_polyhedron_with_many_neighbour_triangles(require_gpu, p):
+    m = _big_polyhedron_mesh()
+    big = m.tet_poly.max()
+    e2 = m.neigh.ravel()
+    t = np.repeat(np.arange(m.n_tet), 4)
+    ok = e2 >= 0
+    shared = (m.tet_poly[t[ok]] == big) & (m.tet_poly[e2[ok]] != big)
+    assert int(shared.sum()) == 108
+    o = _oracle(m, p)
+    mf = _prepared(m, p, _lib.MIXED_MF)
+    f32 = _prepared(m, p, _lib.MIXED)
+    for g in (mf, f32):
+        g.set_state(_lib.SLOT_U0, o.get_state(_lib.SLOT_U0))
+        g.set_state(_lib.SLOT_UN, o.get_state(_lib.SLOT_UN))
+    t0 = 1e-3
+    o.run_steps(t0, 1.0, max_steps=20)
+    mf.run_steps(t0, 1.0, max_steps=20)
+    f32.run_steps(t0, 1.0, max_steps=20)
+    uo = o.get_state(_lib.SLOT_UN)
+    s_mf = rel(mf.get_state(_lib.SLOT_UN), uo)
+    s_32 = rel(f32.get_state(_lib.SLOT_UN), uo)
+    print(f"p={p} big polyhedron: 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}")
+    assert s_mf <= 30.0 * s_32 + 1e-7
+    for x in (mf, f32, o):
+        x.close()
+
+
 @pytest.mark.parametrize("p", [2, 3, 4])
 def test_mf_error_within_1p1_of_fp64(require_gpu, p):
     from lymph3d_apsc_gb300.matrix_free import run_reference_driver as gpu_driver
