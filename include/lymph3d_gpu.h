@@ -65,8 +65,7 @@ extern "C" {
                             quadrature points, tested against P's basis), so no
                             neighbour block is stored or read; FP32
                             accumulation, FP64 combine, mass inverse, update
-                            and error norms.  Not accepted by
-                            lymph_batch_create. */
+                            and error norms. */
 
 /* ---- state slots (the driver's arrays, src/Lymph3D.f90:237-239) --------- */
 #define LYMPH_SLOT_U0   0   /* u0_loc: u^{n-1} (u^0 before the first step)   */

@@ -28,6 +28,11 @@
 
 using namespace stepk;
 
+size_t lymph_mf_batch_problem_bytes();
+void lymph_mf_batch_problem(const lymph_ctx* c, int* status, void* out);
+int lymph_mf_batch_step(cudaStream_t st, int grid, const void* probs, const int2* items, int n_items, int* queue,
+                        const int64_t* step_idx, const double* gvals, int64_t g_stride);
+
 namespace {
 
 constexpr int BATCH_THREADS = 320;   // the p = 4 shape; lower degrees leave lanes idle
@@ -120,7 +125,7 @@ struct lymph_batch {
     std::vector<lymph_ctx*> ctx;
     int precision = LYMPH_FP64;
     cudaStream_t stream = nullptr;
-    BatchProblem* d_probs = nullptr;
+    void* d_probs = nullptr;         // BatchProblem[n], or the matrix-free path's records
     int2* d_items = nullptr;
     int n_items = 0;
     std::vector<int2> items_lpt, items_natural;
@@ -148,6 +153,13 @@ int upload_items(lymph_batch* b) {
 }
 
 int refresh_problems(lymph_batch* b) {
+    if (b->precision == LYMPH_MIXED_MF) {
+        const size_t rb = lymph_mf_batch_problem_bytes();
+        std::vector<char> h(rb * b->ctx.size());
+        for (size_t i = 0; i < b->ctx.size(); ++i) lymph_mf_batch_problem(b->ctx[i], b->d_status, h.data() + rb * i);
+        LYMPH_CUDA_TRY(cudaMemcpyAsync(b->d_probs, h.data(), h.size(), cudaMemcpyHostToDevice, b->stream));
+        return LYMPH_OK;
+    }
     std::vector<BatchProblem> h(b->ctx.size());
     for (size_t i = 0; i < b->ctx.size(); ++i) {
         lymph_ctx* c = b->ctx[i];
@@ -172,15 +184,22 @@ int refresh_problems(lymph_batch* b) {
     return LYMPH_OK;
 }
 
+// kernel launches per batched step
+int step_launches(const lymph_batch* b) { return b->precision == LYMPH_MIXED_MF ? 3 : 2; }
+
 int launch_step(lymph_batch* b, int64_t g_stride) {
-    if (b->precision == LYMPH_MIXED)
-        k_step_batch<float><<<b->grid, BATCH_THREADS, 0, b->stream>>>(b->d_probs, b->d_items, b->n_items, b->d_queue,
+    const BatchProblem* probs = (const BatchProblem*)b->d_probs;
+    if (b->precision == LYMPH_MIXED_MF)
+        LYMPH_TRY(lymph_mf_batch_step(b->stream, b->grid, b->d_probs, b->d_items, b->n_items, b->d_queue, b->d_step_idx,
+                                      b->d_gvals, g_stride));
+    else if (b->precision == LYMPH_MIXED)
+        k_step_batch<float><<<b->grid, BATCH_THREADS, 0, b->stream>>>(probs, b->d_items, b->n_items, b->d_queue,
                                                                      b->d_step_idx, b->d_gvals, g_stride);
     else
-        k_step_batch<double><<<b->grid, BATCH_THREADS, 0, b->stream>>>(b->d_probs, b->d_items, b->n_items, b->d_queue,
+        k_step_batch<double><<<b->grid, BATCH_THREADS, 0, b->stream>>>(probs, b->d_items, b->n_items, b->d_queue,
                                                                       b->d_step_idx, b->d_gvals, g_stride);
     k_batch_bump<<<1, 1, 0, b->stream>>>(b->d_step_idx, b->d_queue);
-    b->launches += 2;
+    b->launches += step_launches(b);
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
 }
@@ -210,7 +229,7 @@ int run_loop(lymph_batch* b, int64_t n, int64_t g_stride, bool use_graph) {
         }
         for (; i + R <= n; i += R) {
             LYMPH_CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
-            b->launches += 2 * R;
+            b->launches += (int64_t)step_launches(b) * R;
         }
     }
     for (; i < n; ++i) LYMPH_TRY(launch_step(b, g_stride));
@@ -259,7 +278,6 @@ int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out) {
         if (!ctxs[i]) { lymph_set_error("lymph_batch_create: null context"); return LYMPH_ERR_INVALID; }
         if (!ctxs[i]->have_matrices) { lymph_set_error("lymph_batch_create: every context needs lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
         if (ctxs[i]->precision != ctxs[0]->precision) { lymph_set_error("lymph_batch_create: mixed precisions in one batch"); return LYMPH_ERR_INVALID; }
-        if (ctxs[i]->precision == LYMPH_MIXED_MF) { lymph_set_error("lymph_batch_create: matrix-free neighbour terms are not batched (use LYMPH_FP64 or LYMPH_MIXED)"); return LYMPH_ERR_INVALID; }
     }
     lymph_batch* b = new lymph_batch();
     b->ctx.assign(ctxs, ctxs + n);
@@ -288,7 +306,8 @@ int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out) {
     std::stable_sort(cost.begin(), cost.end(), [](const std::pair<int64_t, int2>& x, const std::pair<int64_t, int2>& y) { return x.first > y.first; });
     for (auto& c : cost) b->items_lpt.push_back(c.second);
     b->n_items = (int)b->items_natural.size();
-    if (cudaMalloc(&b->d_probs, sizeof(BatchProblem) * n) != cudaSuccess ||
+    const size_t prob_bytes = b->precision == LYMPH_MIXED_MF ? lymph_mf_batch_problem_bytes() : sizeof(BatchProblem);
+    if (cudaMalloc(&b->d_probs, prob_bytes * n) != cudaSuccess ||
         cudaMalloc(&b->d_items, sizeof(int2) * b->n_items) != cudaSuccess ||
         cudaMalloc(&b->d_queue, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_step_idx, sizeof(int64_t)) != cudaSuccess ||
         cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess) {
@@ -369,8 +388,9 @@ int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache,
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
+        const int max_mult = b->precision == LYMPH_MIXED_MF ? 5 : BATCH_MINB;  // CTAs per SM the kernel fits
         for (int ord = 0; ord < 2; ++ord)
-            for (int mult = 1; mult <= BATCH_MINB; ++mult) {
+            for (int mult = 1; mult <= max_mult; ++mult) {
                 b->order = ord;
                 b->grid = mult * b->sms;
                 LYMPH_TRY(upload_items(b));

@@ -29,6 +29,8 @@
 // leapfrog update).  A step then reads the self blocks (1/nb of the
 // operator bytes) and per-triangle geometry instead of every block.
 
+#include <cstring>
+
 #include "step_body.cuh"
 
 namespace {
@@ -215,42 +217,60 @@ __device__ __forceinline__ void prefetch_l2(const void* base, int64_t total, con
 // chunk in Np registers (the sum-factorised transpose).  Then the self-block
 // rows (thread r < ND, K_PP streamed from L2) and the 42 slots' partial rows,
 // summed in a fixed order.
-template <int PD, int MODE>
-__global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ MfArgs A) {
+// Shared-memory layout of one polyhedron's pass; the face-loop buffers and
+// the final reduction share storage.
+template <int PD> struct MfSmem {
     using S = MfShape<PD>;
-    constexpr int NP = S::NP, ND = S::ND, L = S::L, NQ2 = S::NQ2, CT = S::CT, NPT = S::NPT, NP2 = NP * NP;
     struct Loop {
-        float2 leg[NPT][3][L];    // P's (L, L') per point, direction, degree
-        float4 flux[NPT][3];      // (G_i0, G_i1, G_i2, s_i) per point, scaled by P's map
+        float2 leg[S::NPT][3][S::L];   // P's (L, L') per point, direction, degree
+        float4 flux[S::NPT][3];        // (G_i0, G_i1, G_i2, s_i) per point, scaled by P's map
     };
     union Work {
         Loop loop;
-        float red[MF_SLOTS][ND];  // after the face loop: the slots' partial rows
+        float red[MF_SLOTS][S::ND];    // after the face loop: the slots' partial rows
     };
-    __shared__ __align__(16) Work s_w;
-    __shared__ __align__(16) float s_quad[3 * NQ2];
-    __shared__ __align__(16) float s_uP[ND];
-    __shared__ __align__(16) int s_Q[MF_MAXT];
-    __shared__ __align__(16) MfTri s_tri[2][CT];
-    __shared__ __align__(16) MfPoly s_polyQ[2][CT];
-    __shared__ __align__(16) float4 s_uQ[2][CT][NP];         // (u_0, u_1, u_2, 0) per basis function
-    __shared__ __align__(16) double s_b[ND];
-    const int P = blockIdx.x, tid = threadIdx.x;
-    const int rb = A.s.row_ptr[P], re = A.s.row_ptr[P + 1];
+    Work w;
+    float4 uQ[2][S::CT][S::NP];        // (u_0, u_1, u_2, 0) per basis function
+    MfTri tri[2][S::CT];
+    MfPoly polyQ[2][S::CT];
+    double b[S::ND];
+    float quad[3 * S::NQ2];
+    float uP[S::ND];
+    int Q[MF_MAXT];
+};
+
+// The pass of polyhedron P (every thread of the CTA calls it; it
+// synchronises): the per-problem tables come from A, the state, right-hand
+// sides and M^-1 from sa.
+template <int PD, int MODE>
+__device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int P, char* smem) {
+    using S = MfShape<PD>;
+    constexpr int NP = S::NP, ND = S::ND, L = S::L, NQ2 = S::NQ2, CT = S::CT, NP2 = NP * NP;
+    MfSmem<PD>& sm = *reinterpret_cast<MfSmem<PD>*>(smem);
+    auto& s_w = sm.w;
+    auto& s_tri = sm.tri;
+    auto& s_polyQ = sm.polyQ;
+    auto& s_uQ = sm.uQ;
+    float* s_quad = sm.quad;
+    float* s_uP = sm.uP;
+    int* s_Q = sm.Q;
+    double* s_b = sm.b;
+    const int tid = threadIdx.x;
+    const int rb = sa.row_ptr[P], re = sa.row_ptr[P + 1];
     const int64_t fb = A.bf_ptr[rb + 1], fe = A.bf_ptr[re];
     const int ntri = (int)(fe - fb);
 
     if (tid == 0) {
         const int64_t nb = (int64_t)ND * ND * 4, vb = (int64_t)ND * 8;
         prefetch_l2(A.Kself, A.kself_bytes, A.Kself + (int64_t)P * ND * ND, nb);
-        prefetch_l2(A.s.Minv, A.minv_bytes, A.s.Minv + (int64_t)P * NP2, (int64_t)NP2 * 8);
-        const int64_t sb = (int64_t)A.s.n_poly * ND * 8;
+        prefetch_l2(sa.Minv, A.minv_bytes, sa.Minv + (int64_t)P * NP2, (int64_t)NP2 * 8);
+        const int64_t sb = (int64_t)sa.n_poly * ND * 8;
         if (MODE == MODE_STEP || MODE == MODE_FIRST) {
-            prefetch_l2(A.s.rhs_stat, sb, A.s.rhs_stat + (int64_t)P * ND, vb);
-            prefetch_l2(A.s.rhs_dyn, sb, A.s.rhs_dyn + (int64_t)P * ND, vb);
+            prefetch_l2(sa.rhs_stat, sb, sa.rhs_stat + (int64_t)P * ND, vb);
+            prefetch_l2(sa.rhs_dyn, sb, sa.rhs_dyn + (int64_t)P * ND, vb);
         }
-        prefetch_l2(A.s.u0, sb, A.s.u0 + (int64_t)P * ND, vb);
-        prefetch_l2(A.s.un, sb, A.s.un + (int64_t)P * ND, vb);
+        prefetch_l2(sa.u0, sb, sa.u0 + (int64_t)P * ND, vb);
+        prefetch_l2(sa.un, sb, sa.un + (int64_t)P * ND, vb);
     }
     for (int i = tid; i < 3 * NQ2; i += MF_THREADS) s_quad[i] = A.quad[i];
     for (int i = tid; i < ND; i += MF_THREADS) {
@@ -385,7 +405,73 @@ __global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ Mf
         for (int kk = 0; kk < MF_SLOTS; ++kk) t += s_w.red[kk][tid];
         y = (double)yself + (double)t;
     }
-    finish_poly<PD, MODE>(A.s, P, y, s_b);
+    finish_poly<PD, MODE>(sa, P, y, s_b);
+}
+
+template <int PD, int MODE>
+__global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ MfArgs A) {
+    __shared__ __align__(16) char smem[sizeof(MfSmem<PD>)];
+    mf_poly<PD, MODE>(A, A.s, blockIdx.x, smem);
+}
+
+// ---- many problems in one persistent launch per step (lymph_batch) ----
+
+struct MfBatchProblem {
+    MfArgs a;          // the problem's tables; a.s's state pointers are set per step
+    double* buf[2];
+    int cur0;          // buffer parity when the run started
+    int p;
+};
+
+constexpr size_t smax2(size_t x, size_t y) { return x > y ? x : y; }
+constexpr size_t MF_SMEM_MAX =
+    smax2(smax2(sizeof(MfSmem<1>), sizeof(MfSmem<2>)), smax2(sizeof(MfSmem<3>), sizeof(MfSmem<4>)));
+
+// Persistent CTAs pull (problem, polyhedron) items from an atomic queue and
+// run mf_poly with the item's degree: the same per-polyhedron pass as k_mf,
+// so results equal stepping each problem alone.
+__global__ void __launch_bounds__(MF_THREADS, 5)
+k_mf_batch(const MfBatchProblem* __restrict__ probs, const int2* __restrict__ items, int n_items, int* queue,
+           const int64_t* step_idx, const double* gvals, int64_t g_stride) {
+    __shared__ __align__(16) char smem[MF_SMEM_MAX];
+    __shared__ int s_item;
+    const int64_t k = *step_idx;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const int2 w = items[it];
+        const MfBatchProblem& pb = probs[w.x];
+        StepArgs s = pb.a.s;
+        const int cur = pb.cur0 ^ (int)(k & 1);
+        s.un = pb.buf[cur];
+        s.u0 = pb.buf[cur ^ 1];
+        s.out = pb.buf[cur ^ 1];
+        s.gvals = gvals + (int64_t)w.x * g_stride;
+        s.step_idx = step_idx;
+        switch (pb.p) {
+            case 1: mf_poly<1, MODE_STEP>(pb.a, s, w.y, smem); break;
+            case 2: mf_poly<2, MODE_STEP>(pb.a, s, w.y, smem); break;
+            case 3: mf_poly<3, MODE_STEP>(pb.a, s, w.y, smem); break;
+            default: mf_poly<4, MODE_STEP>(pb.a, s, w.y, smem); break;
+        }
+    }
+}
+
+// The FP32 copies of every problem's u^n, a warp per (problem, polyhedron) item.
+__global__ void k_mf_u32_batch(const MfBatchProblem* __restrict__ probs, const int2* __restrict__ items, int n_items,
+                               const int64_t* step_idx) {
+    const int64_t k = *step_idx;
+    const int item = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (item >= n_items) return;
+    const int2 w = items[item];
+    const MfBatchProblem& pb = probs[w.x];
+    const int NP = (pb.p + 1) * (pb.p + 2) * (pb.p + 3) / 6;
+    const double* u = pb.buf[pb.cur0 ^ (int)(k & 1)] + (int64_t)w.y * 3 * NP;
+    float4* o = const_cast<float4*>(pb.a.u32) + (int64_t)w.y * NP;
+    for (int m = lane; m < NP; m += 32) o[m] = make_float4((float)u[m], (float)u[NP + m], (float)u[2 * NP + m], 0.0f);
 }
 
 // u32[P][m] = (u[P][0][m], u[P][1][m], u[P][2][m], 0): the operator input in
@@ -464,8 +550,9 @@ __global__ void k_mf_polys(int n_poly, const double* __restrict__ bbox, MfPoly* 
     out[P] = m;
 }
 
-template <int PD, int MODE>
-int launch_mf_t(lymph_ctx* c, const StepArgs& s) {
+// The context's tables in kernel arguments (s: the step's CSR pattern, state
+// and right-hand sides).
+MfArgs mf_args(const lymph_ctx* c, const StepArgs& s) {
     MfArgs a;
     a.s = s;
     a.Kself = (const float*)c->d_K;
@@ -477,6 +564,12 @@ int launch_mf_t(lymph_ctx* c, const StepArgs& s) {
     a.minv_bytes = (int64_t)c->n_poly * c->Np * c->Np * (int64_t)sizeof(double);
     for (int i = 0; i < 3 * 25; ++i) a.quad[i] = c->mf_quad[i];
     a.theta = (float)c->theta;
+    return a;
+}
+
+template <int PD, int MODE>
+int launch_mf_t(lymph_ctx* c, const StepArgs& s) {
+    const MfArgs a = mf_args(c, s);
     k_mf<PD, MODE><<<c->n_poly, MF_THREADS, 0, c->stream>>>(a);
     c->launches++;
     return LYMPH_OK;
@@ -544,4 +637,45 @@ int lymph_dev_mf(lymph_ctx* c, int mode, const stepk::StepArgs& s) {
         case 4: return launch_mf_p<4>(c, mode, s);
         default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
     }
+}
+
+// ---- batch interface (batch.cu) ----
+
+size_t lymph_mf_batch_problem_bytes() { return sizeof(MfBatchProblem); }
+
+// One problem's record for k_mf_batch; status: the batch's status word.
+void lymph_mf_batch_problem(const lymph_ctx* c, int* status, void* out) {
+    StepArgs s;
+    s.row_ptr = c->d_row_ptr;
+    s.col = c->d_col;
+    s.K = c->d_K;
+    s.Minv = c->d_Minv;
+    s.rhs_stat = c->d_rhs_stat;
+    s.rhs_dyn = c->d_rhs_dyn;
+    s.gvals = nullptr;
+    s.step_idx = nullptr;
+    s.u0 = s.un = nullptr;
+    s.out = nullptr;
+    s.partial = nullptr;
+    s.dt = c->dt;
+    s.status = status;
+    s.n_poly = c->n_poly;
+    MfBatchProblem pb;
+    pb.a = mf_args(c, s);
+    pb.buf[0] = c->d_buf[0];
+    pb.buf[1] = c->d_buf[1];
+    pb.cur0 = c->cur;
+    pb.p = c->p;
+    std::memcpy(out, &pb, sizeof(pb));
+}
+
+// One batched leapfrog step: the FP32 copies of every problem's u^n, then the
+// persistent pass over all items (the caller advances the step counter).
+int lymph_mf_batch_step(cudaStream_t st, int grid, const void* probs, const int2* items, int n_items, int* queue,
+                        const int64_t* step_idx, const double* gvals, int64_t g_stride) {
+    const MfBatchProblem* pb = (const MfBatchProblem*)probs;
+    k_mf_u32_batch<<<(unsigned)((n_items + 3) / 4), 128, 0, st>>>(pb, items, n_items, step_idx);
+    k_mf_batch<<<grid, MF_THREADS, 0, st>>>(pb, items, n_items, queue, step_idx, gvals, g_stride);
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
 }

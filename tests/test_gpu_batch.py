@@ -2,7 +2,8 @@
 CFL bound.
 
 * a batch of uneven problems (degrees 1-4, different meshes and dt) advanced
-  by lymph_batch_run equals each problem stepped alone, bit for bit;
+  by lymph_batch_run equals each problem stepped alone, bit for bit, in FP64,
+  with FP32 blocks and with matrix-free neighbour terms;
 * the autotuner leaves every problem's state as it found it;
 * the point-source RHS is the delta functional: b . c = dir . u_h(x0);
 * lymph_max_eigenvalue matches the largest |eigenvalue| of M^-1 K built
@@ -46,14 +47,15 @@ def _gvals(solvers, n):
     return np.array([[time_function(t) for t in E.time_sequence(s.dt, s.dt, n)] for s in solvers])
 
 
-@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED])
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED, _lib.MIXED_MF])
 @pytest.mark.parametrize("n_steps", [37, 5])
 def test_batch_equals_single_contexts_bitwise(require_gpu, precision, n_steps):
     batch_solvers = [_prepared(sp, precision) for sp in SPECS]
     alone = [_prepared(sp, precision) for sp in SPECS]
     b = E.Batch(batch_solvers)
     ms = b.run(_gvals(batch_solvers, n_steps))
-    assert ms > 0 and b.launch_count() == 2 * n_steps
+    per_step = 3 if precision == _lib.MIXED_MF else 2  # + the FP32 copy of u^n
+    assert ms > 0 and b.launch_count() == per_step * n_steps
     for s, a in zip(batch_solvers, alone):
         a.run_steps(a.dt, 1e9, max_steps=n_steps)
         assert np.array_equal(s.get_state(_lib.SLOT_UN), a.get_state(_lib.SLOT_UN))

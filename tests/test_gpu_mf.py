@@ -198,12 +198,3 @@ def test_mf_blocks_are_the_fp64_operator(require_gpu, p):
         assert np.array_equal(a.blocks(_lib.BLOCKS_K), b.blocks(_lib.BLOCKS_K))
         for which in range(5):
             assert np.array_equal(a.mass(which), b.mass(which))
-
-
-def test_batch_rejects_mf(require_gpu):
-    from lymph3d_apsc_gb300.ensemble import Batch
-    g = _prepared(_mesh("tet_dir"), 2, _lib.MIXED_MF)
-    with pytest.raises(LymphError) as e:
-        Batch([g])
-    assert e.value.code == _lib.LYMPH_ERR_INVALID
-    g.close()
