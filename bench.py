@@ -454,7 +454,35 @@ def run_surrogate(cfg, steps):
                          "judge_err_max": st["judge_err_max"]})
             log(f"[bench] {mode} res_tol {tol:g}: {el:.2f}s (plain {t_plain:.2f}s) x{t_plain / el:.2f}, "
                 f"rel L2 {runs[-1]['rel_L2_vs_plain']:.2e}, accepted {st['accepted']}/{st['blocks']}")
-    launches = g.launch_count()
+    # the same plain and surrogate runs on a context with matrix-free FP32
+    # neighbour terms (LYMPH_MIXED_MF), measured against the FP64 plain run
+    gm = MatrixFree(m, cfg["p"], cfg["dt"], precision=_lib.MIXED_MF)
+    gm.MAKE_MATRICES_FREE()
+    gm.MAKE_RHS_FREE(_lib.RHS_STAT, _lib.F_NULL, _lib.GD_NULL, _lib.GN_NULL)
+    E.point_source(gm, [0.5, 0.5, 0.5], [0.0, 0.0, 1.0])
+    syncm = lambda: gm.get_state(_lib.SLOT_UN)[:1]  # noqa: E731
+    for mode, nn in (("plain_mixed_mf", "plain"), ("taylor_mixed_mf", None), ("network_mixed_mf", net)):
+        for tol in (sc["res_tols"][:1] if nn != "plain" else [None]):
+            gm.set_state(_lib.SLOT_U0, u0)
+            gm.set_state(_lib.SLOT_UN, un)
+            syncm()
+            a = time.perf_counter()
+            if nn == "plain":
+                S.run_plain(gm, steps, gfun, t0)
+                st = {"blocks": 0, "accepted": 0, "plain_steps": steps, "judge_err_max": 0.0}
+            else:
+                _, st = S.run_hybrid(gm, nn, steps, gfun, t0, K=K, graph=graph, res_tol=tol)
+            syncm()
+            el = time.perf_counter() - a
+            g.set_state(_lib.SLOT_UN, gm.get_state(_lib.SLOT_UN))
+            runs.append({"mode": mode, "res_tol": tol, "seconds": el, "speedup_vs_plain": t_plain / el,
+                         "value": dofs * steps / el, "rel_L2_vs_plain": rel_l2(), "blocks": st["blocks"],
+                         "accepted": st["accepted"], "plain_steps": st["plain_steps"],
+                         "judge_err_max": st["judge_err_max"]})
+            log(f"[bench] {mode} res_tol {tol}: {el:.2f}s (plain FP64 {t_plain:.2f}s) x{t_plain / el:.2f}, "
+                f"rel L2 {runs[-1]['rel_L2_vs_plain']:.2e}, accepted {st['accepted']}/{st['blocks']}")
+    launches = g.launch_count() + gm.launch_count()
+    gm.close()
     out = {"dofs": dofs, "n_poly": g.n_poly, "t_plain": t_plain, "runs": runs, "held_out": held,
            "train": {"trajectories": sc["n_traj"], "iters": sc["iters"], "data_s": t_data, "train_s": t_train,
                      "loss_first": float(np.mean(hist[:50])), "loss_last": float(np.mean(hist[-500:]))},
@@ -585,11 +613,18 @@ def main():
             return
         with ClockSampler(info["gpu"]) as clk:
             r = run_surrogate(cfg, args.steps)
-        # the headline: the fastest run whose final state is within the stated
-        # relative L2 distance of the plain run's
+        # the headline: the fastest surrogate run on the FP64 operator whose
+        # final state is within the stated relative L2 distance of the plain
+        # run's; beside it the fastest run of any kind (the surrogate on the
+        # matrix-free mixed operator included) within the same distance
         bar = cfg["surrogate"]["stated_rel_l2"]
-        ok_runs = [x for x in r["runs"] if x["rel_L2_vs_plain"] <= bar]
-        best = max(ok_runs or r["runs"], key=lambda x: x["speedup_vs_plain"] if ok_runs else -x["rel_L2_vs_plain"])
+
+        def fastest(cands):
+            ok = [x for x in cands if x["rel_L2_vs_plain"] <= bar]
+            return max(ok or cands, key=lambda x: x["speedup_vs_plain"] if ok else -x["rel_L2_vs_plain"])
+
+        best = fastest([x for x in r["runs"] if not x["mode"].endswith("_mixed_mf")])
+        best_any = fastest(r["runs"])
         line = {"metric": metric, "value": best["value"], "unit": "DOF-steps/s", "n_gpus": 1, "steps": args.steps,
                 "warmup": cfg["surrogate"]["warm"], "ms_per_step": 1e3 * best["seconds"] / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (network bf16/f32)",
@@ -599,6 +634,8 @@ def main():
                            "dofs": r["dofs"], "l2_flush": "inputs larger than L2"},
                 "plain_value": r["dofs"] * args.steps / r["t_plain"], "stated_rel_L2_vs_plain": bar,
                 "headline_run": {k: best[k] for k in ("mode", "res_tol", "speedup_vs_plain", "rel_L2_vs_plain")},
+                "fastest_within_stated_l2": {k: best_any[k] for k in ("mode", "res_tol", "speedup_vs_plain",
+                                                                      "rel_L2_vs_plain", "value")},
                 "runs": r["runs"],
                 "held_out_error_ratio_network_vs_taylor": [a / b for a, b in r["held_out"]],
                 "train": r["train"], "gpu_launches": r["launches"], "clocks": clk.summary()}
