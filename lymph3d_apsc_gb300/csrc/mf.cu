@@ -5,9 +5,10 @@
 // triangles P shares with Q of face-quadrature terms (MAKE_STIFFNESS_FACE,
 // src/assemble_element.f90:404-661, inserted by MAKE_MATRICES_FREE,
 // src/matrix_free.f90:412-433):
-//     K_PQ = -theta/2 I + S - IT/2 ... per triangle, per quadrature point q
-// with weights W_q = w_q |face|, P's outward normal n and the material of
-// P's tetrahedron.  Contracting the block with u_Q point by point gives the
+//     K_PQ = -theta/2 I - S - IT/2
+// with I, IT and S the consistency, symmetry and penalty integrals over each
+// shared triangle, quadrature weights W_q = w_q |face|, P's outward normal n
+// and the material of P's tetrahedron.  Contracting the block with u_Q point by point gives the
 // same sums in another order:
 //     (K_PQ u_Q)_(i,a) = sum_q  grad phi^P_a . G_i  +  phi^P_a s_i,
 //     G_ik = -theta/2 W (lambda (n.v) delta_ik + mu (n_i v_k + v_i n_k)),
@@ -18,16 +19,18 @@
 // n_i n_j / 2 off it).  h is the reference's symmetry term IT with its
 // (i, j) order (it is the traction of u_Q only when lambda = mu).
 //
-// So the neighbour blocks are never stored: one CTA per polyhedron P applies
-// its FP32 self block (streamed from HBM), then, for each triangle P shares
-// with a neighbour, evaluates u_Q and grad u_Q at the triangle's quadrature
-// points from the Legendre basis on Q's bounding box, forms G and s, and
-// tests them against P's basis -- all in FP32 from per-triangle geometry
-// precomputed once (quadrature origin and edge vectors, normal, area,
-// material, penalty).  The row sums are combined in FP64 in a fixed order and
-// finished exactly like the fused kernel (right-hand side, M^-1 in FP64,
-// leapfrog update).  A step then reads the self blocks (1/nb of the
-// operator bytes) and per-triangle geometry instead of every block.
+// So the neighbour blocks are never stored.  One CTA per polyhedron P (or,
+// for a batch of problems, persistent CTAs over (problem, polyhedron) items)
+// evaluates u_Q and grad u_Q at the quadrature points of every triangle P
+// shares with a neighbour Q, from the Legendre basis on Q's bounding box,
+// forms G and s, tests them against P's basis, and applies its FP32 self
+// block.  Everything runs in FP32 from per-triangle geometry precomputed
+// once (quadrature origin and edge vectors, normal, area, material, penalty);
+// both basis contractions are sum-factorised over the Legendre degree
+// triples.  The row sums are combined in FP64 in a fixed order and finished
+// exactly like the fused kernel (right-hand side, M^-1 in FP64, leapfrog
+// update).  A step reads the self blocks (1/nb of the operator bytes) and the
+// per-triangle geometry instead of every block.
 
 #include <cstring>
 
