@@ -41,7 +41,8 @@ namespace {
 using namespace stepk;
 
 struct MfTri {          // one triangle of a neighbour block, seen from the row polyhedron P
-    float o[3];         // quadrature point x_q = o + xi_q e1 + eta_q e2
+    float oP[3];        // quadrature point x_q = c_P + oP + xi_q e1 + eta_q e2 (c_P: P's box centre)
+    float oQ[3];        // the same point as c_Q + oQ + xi_q e1 + eta_q e2 (Q's box centre)
     float e1[3];
     float e2[3];
     float n[3];         // P's outward unit normal
@@ -49,9 +50,9 @@ struct MfTri {          // one triangle of a neighbour block, seen from the row 
     float lam, mu;      // material of P's tetrahedron
     float sigma;        // penalty alpha p^2 / min(h_P, h_Q) (lambda + 2 mu)
     int32_t Q;          // neighbour polyhedron
-    int32_t pad[3];
 };
-static_assert(sizeof(MfTri) == 80, "MfTri is 20 words");
+static_assert(sizeof(MfTri) == 96, "MfTri is 6 x 16 bytes");
+constexpr int MF_TRI_CHUNKS = (int)(sizeof(MfTri) / 16);
 
 struct MfPoly {         // Legendre map of a bounding box: xp = (x - c) ih, phi = sc L(xp_x) L(xp_y) L(xp_z)
     float c[3];
@@ -289,7 +290,7 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     auto stage = [&](int c, int b) {  // chunk starting at triangle c into buffer b
         const int nt = (ntri - c) < CT ? ntri - c : CT;
         const char* src = (const char*)(A.tri + fb + c);
-        for (int i = tid; i < nt * 5; i += MF_THREADS) cp_async16((char*)s_tri[b] + 16 * i, src + 16 * i);
+        for (int i = tid; i < nt * MF_TRI_CHUNKS; i += MF_THREADS) cp_async16((char*)s_tri[b] + 16 * i, src + 16 * i);
         for (int i = tid; i < nt * 2; i += MF_THREADS)
             cp_async16((char*)&s_polyQ[b][i / 2] + 16 * (i & 1), (const char*)(A.poly + getQ(c + i / 2)) + 16 * (i & 1));
         for (int i = tid; i < nt * NP; i += MF_THREADS) {
@@ -319,14 +320,20 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
             const MfTri& T = s_tri[b][t];
             const float xi = s_quad[3 * q], eta = s_quad[3 * q + 1];
             const float W = s_quad[3 * q + 2] * T.area;
-            float x[3];
+            // the point relative to Q's and to P's box centre (small operands,
+            // so the Legendre arguments keep FP32 relative accuracy)
+            float xq[3], xp[3];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) x[d] = fmaf(eta, T.e2[d], fmaf(xi, T.e1[d], T.o[d]));
+            for (int d = 0; d < 3; ++d) {
+                const float r = fmaf(eta, T.e2[d], xi * T.e1[d]);
+                xq[d] = T.oQ[d] + r;
+                xp[d] = T.oP[d] + r;
+            }
             const MfPoly& pq = s_polyQ[b][t];
             float2 X[L], Y[L], Z[L];
-            legendre<PD>((x[0] - pq.c[0]) * pq.ih[0], X);
-            legendre<PD>((x[1] - pq.c[1]) * pq.ih[1], Y);
-            legendre<PD>((x[2] - pq.c[2]) * pq.ih[2], Z);
+            legendre<PD>(xq[0] * pq.ih[0], X);
+            legendre<PD>(xq[1] * pq.ih[1], Y);
+            legendre<PD>(xq[2] * pq.ih[2], Z);
             // Q's map: phi = sc L L L, d_k phi = sc ih_k (...)
             const float sq = pq.sc, gx = sq * pq.ih[0], gy = sq * pq.ih[1], gz = sq * pq.ih[2];
             float v[3], D[3][3];
@@ -362,9 +369,9 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
                 const float s = -W * (T.sigma * Tv + 0.5f * h);
                 s_w.loop.flux[tid][i] = make_float4(G[0] * hx, G[1] * hy, G[2] * hz, s * sP);
             }
-            legendre<PD>((x[0] - pP.c[0]) * pP.ih[0], s_w.loop.leg[tid][0]);
-            legendre<PD>((x[1] - pP.c[1]) * pP.ih[1], s_w.loop.leg[tid][1]);
-            legendre<PD>((x[2] - pP.c[2]) * pP.ih[2], s_w.loop.leg[tid][2]);
+            legendre<PD>(xp[0] * pP.ih[0], s_w.loop.leg[tid][0]);
+            legendre<PD>(xp[1] * pP.ih[1], s_w.loop.leg[tid][1]);
+            legendre<PD>(xp[2] * pP.ih[2], s_w.loop.leg[tid][2]);
         }
         __syncthreads();
         // ---- test against P's basis: thread (slot, component) over the chunk's points ----
@@ -496,8 +503,9 @@ __global__ void k_mf_tris(int64_t n_blocks, const int32_t* __restrict__ blk_row,
                           const int32_t* __restrict__ neigh, const int32_t* __restrict__ tet_poly,
                           const int32_t* __restrict__ tet_mat, const double* __restrict__ mat,
                           const double* __restrict__ fk, const double* __restrict__ nrm,
-                          const double* __restrict__ area, const double* __restrict__ hk, const RefTables* ref,
-                          double alpha, int p, MfTri* out, int* status) {
+                          const double* __restrict__ area, const double* __restrict__ hk,
+                          const double* __restrict__ bbox, const RefTables* ref, double alpha, int p, MfTri* out,
+                          int* status) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n_blocks) return;
     const int P = blk_row[k], Q = col[k];
@@ -519,7 +527,11 @@ __global__ void k_mf_tris(int64_t n_blocks, const int32_t* __restrict__ blk_row,
                 cmap[j][l] = s;
             }
         for (int j = 0; j < 3; ++j) {
-            T.o[j] = (float)(cmap[j][2] + cmap[j][3]);
+            const double o = cmap[j][2] + cmap[j][3];
+            const double cP = (bbox[P * 6 + 2 * j] + bbox[P * 6 + 2 * j + 1]) / 2.0;
+            const double cQ = (bbox[Q * 6 + 2 * j] + bbox[Q * 6 + 2 * j + 1]) / 2.0;
+            T.oP[j] = (float)(o - cP);
+            T.oQ[j] = (float)(o - cQ);
             T.e1[j] = (float)cmap[j][0];
             T.e2[j] = (float)cmap[j][1];
             T.n[j] = (float)nrm[(int64_t)t * 12 + f * 3 + j];
@@ -531,7 +543,6 @@ __global__ void k_mf_tris(int64_t n_blocks, const int32_t* __restrict__ blk_row,
         T.mu = (float)mu;
         T.sigma = (float)(alpha * (double)(p * p) / fmin(hk[P], hk[Q]) * (lam + 2 * mu));
         T.Q = Q;
-        T.pad[0] = T.pad[1] = T.pad[2] = 0;
         out[e] = T;
     }
 }
@@ -621,8 +632,8 @@ int lymph_mf_setup(lymph_ctx* c, const RefTables& R) {
     if (c->n_blocks > 0) {
         k_mf_tris<<<(unsigned)((c->n_blocks + 127) / 128), 128, 0, c->stream>>>(
             c->n_blocks, c->d_blk_row, c->d_col, c->d_bf_ptr, c->d_bf, c->d_neigh, c->d_tet_poly, c->d_tet_mat,
-            c->d_mat, c->d_fk, c->d_normal, c->d_area, c->d_hk, c->d_ref, c->alpha, c->p, (MfTri*)c->d_mf_tri,
-            c->d_status);
+            c->d_mat, c->d_fk, c->d_normal, c->d_area, c->d_hk, c->d_bbox, c->d_ref, c->alpha, c->p,
+            (MfTri*)c->d_mf_tri, c->d_status);
         c->launches++;
     }
     k_mf_polys<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->d_bbox, (MfPoly*)c->d_mf_poly);
