@@ -251,11 +251,11 @@ def step_bytes(g, precision):
     """Algorithmic bytes of one step: the operator blocks once, plus per
     polyhedron u^{n-1}, u^n, u^{n+1}, the two right-hand sides and M^-1.  The
     matrix-free neighbour path stores only the self blocks; its per-triangle
-    geometry (96 bytes per triangle side) is counted with them."""
+    geometry (80 bytes per triangle side) is counted with them."""
     nd, Np = g.nd, g.Np
     per_poly = g.n_poly * (3 * nd * 8 + 2 * Np * Np * 8 + 2 * nd * 8)
     if precision == 2:
-        return g.n_poly * nd * nd * 4 + mf_triangles(g) * 96 + per_poly
+        return g.n_poly * nd * nd * 4 + mf_triangles(g) * 80 + per_poly
     es = {0: 8, 1: 4}[precision]
     return g.n_blocks * nd * nd * es + per_poly
 

@@ -51,7 +51,7 @@ struct MfTri {          // one triangle of a neighbour block, seen from the row 
     float sigma;        // penalty alpha p^2 / min(h_P, h_Q) (lambda + 2 mu)
     int32_t Q;          // neighbour polyhedron
 };
-static_assert(sizeof(MfTri) == 96, "MfTri is 6 x 16 bytes");
+static_assert(sizeof(MfTri) == 80, "MfTri is 5 x 16 bytes");
 constexpr int MF_TRI_CHUNKS = (int)(sizeof(MfTri) / 16);
 
 struct MfPoly {         // Legendre map of a bounding box: xp = (x - c) ih, phi = sc L(xp_x) L(xp_y) L(xp_z)
