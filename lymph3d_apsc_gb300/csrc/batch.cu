@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <filesystem>
 #include <fstream>
 #include <map>
 #include <mutex>
@@ -110,10 +111,10 @@ void tune_store(const std::string& key, int grid, int order) {
     std::lock_guard<std::mutex> l(g_tune_mu);
     std::string path = tune_cache_path();
     size_t slash = path.rfind('/');
-    if (slash != std::string::npos) {
-        std::string dir = path.substr(0, slash);
-        std::string cmd = "mkdir -p '" + dir + "'";
-        if (std::system(cmd.c_str()) != 0) return;
+    if (slash != std::string::npos && slash > 0) {
+        std::error_code ec;  // the cache is optional: a directory that cannot be made skips the store
+        std::filesystem::create_directories(path.substr(0, slash), ec);
+        if (ec) return;
     }
     std::ofstream f(path, std::ios::app);
     f << key << " " << grid << " " << order << "\n";
