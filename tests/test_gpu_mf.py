@@ -135,6 +135,38 @@ def test_mf_polyhedron_with_many_neighbour_triangles(require_gpu, p):
         x.close()
 
 
+@pytest.mark.parametrize("theta", [0.0, 1.0])
+@pytest.mark.parametrize("p", [2, 3])
+def test_mf_other_interior_penalty_forms(require_gpu, theta, p):
+    """theta = 0 (incomplete) and 1 (non-symmetric interior penalty): the
+    matrix-free terms carry theta in the consistency term like the assembly."""
+    m = _mesh("bfs_ref_jitter")
+    o = Oracle(m, p, 1e-3, theta=theta)
+    o.make_matrices()
+    o.make_rhs(0, 0, 0, 0)
+    o.make_rhs(1, 1, 1, 1)
+    o.modal_project(0, 0)
+    o.modal_project(1, 2)
+    o.first_step(0.0)
+    runs = []
+    for prec in (_lib.MIXED_MF, _lib.MIXED):
+        g = MatrixFree(m, p, 1e-3, theta=theta, precision=prec)
+        g.MAKE_MATRICES_FREE()
+        g.MAKE_RHS_FREE(_lib.RHS_STAT, _lib.F_NULL, _lib.GD_NULL, _lib.GN_NULL)
+        g.MAKE_RHS_FREE(_lib.RHS_DYN, _lib.F_TIME, _lib.GD, _lib.GN)
+        g.set_state(_lib.SLOT_U0, o.get_state(_lib.SLOT_U0))
+        g.set_state(_lib.SLOT_UN, o.get_state(_lib.SLOT_UN))
+        g.run_steps(1e-3, 1.0, max_steps=20)
+        runs.append(g)
+    o.run_steps(1e-3, 1.0, max_steps=20)
+    uo = o.get_state(_lib.SLOT_UN)
+    s_mf, s_32 = (rel(g.get_state(_lib.SLOT_UN), uo) for g in runs)
+    print(f"p={p} theta={theta}: 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}")
+    assert s_mf <= 30.0 * s_32 + 1e-7
+    for x in runs + [o]:
+        x.close()
+
+
 @pytest.mark.parametrize("p", [2, 3, 4])
 def test_mf_error_within_1p1_of_fp64(require_gpu, p):
     from lymph3d_apsc_gb300.matrix_free import run_reference_driver as gpu_driver
