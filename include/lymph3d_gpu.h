@@ -392,17 +392,24 @@ int lymph_max_eigenvalue(lymph_ctx* ctx, int32_t iters, double* lam);
  * (TIME_STEP_MATRIX_FREE each) with one persistent kernel per step over all
  * (problem, polyhedron) items, launched as CUDA graphs; gvals holds the
  * time-function value of every problem at every step, [n][n_steps].  Results
- * equal stepping each context alone, bit for bit. */
+ * equal stepping each context alone, bit for bit, with the default schedule
+ * (see lymph_batch_autotune for tuned tile shapes). */
 typedef struct lymph_batch lymph_batch;
 int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out);
 int lymph_batch_destroy(lymph_batch* batch);
 int lymph_batch_run(lymph_batch* batch, int64_t n_steps, const double* gvals, float* ms_total);
 /* Times trial_steps steps for each candidate (1..4 persistent CTAs per SM,
- * items largest-cost-first or problem-major) and keeps the fastest; the
- * problems' states are restored afterwards.  The choice is cached per batch
- * signature in $LYMPH_TUNE_CACHE (default ~/.cache/lymph3d_gb300_tune.txt)
- * and reused when use_cache is non-zero. */
+ * 1..5 for LYMPH_MIXED_MF; items largest-cost-first or problem-major; for
+ * LYMPH_FP64 / LYMPH_MIXED also three tile shapes, the column slices per
+ * degree) and keeps the fastest; the problems' states are restored
+ * afterwards.  The choice is cached per batch signature in $LYMPH_TUNE_CACHE
+ * (default ~/.cache/lymph3d_gb300_tune2.txt) and reused when use_cache is
+ * non-zero.  With tile shape 0 (the default before tuning) results equal
+ * stepping each context alone bit for bit; the other shapes group each
+ * row's partial sums differently: deterministic, equal up to rounding. */
 int lymph_batch_autotune(lymph_batch* batch, int32_t trial_steps, int32_t use_cache, int32_t* grid, int32_t* order);
+/* The current schedule: grid size, item order, tile shape (any pointer may be null). */
+int lymph_batch_schedule(const lymph_batch* batch, int32_t* grid, int32_t* order, int32_t* shape);
 int lymph_batch_launch_count(const lymph_batch* batch, int64_t* count);
 
 /* Number of kernels this context launched so far (all kinds). */

@@ -12,7 +12,11 @@
 // parity and time-function value) and resets the queue; the loop is launched
 // as CUDA graphs of 16 steps.  The grid size and the item order (largest
 // cost first or problem-major) are picked by a timing autotuner whose choice
-// is cached per batch signature.
+// is cached per batch signature.  The autotuner also picks the tile shape:
+// the number of column slices S per degree (kBatchShapes).  Shape 0, the
+// default before tuning, is the single-problem kernel's, so results are then
+// bit-identical to stepping each context alone; the other shapes group the
+// row's partial sums differently (deterministic, equal to rounding).
 
 #include <algorithm>
 #include <cstdlib>
@@ -46,14 +50,25 @@ struct BatchProblem {
     int p;
 };
 
-template <typename KT> struct BatchSmem {
-    static constexpr size_t b1 = SmemSize<1, KT>::bytes, b2 = SmemSize<2, KT>::bytes, b3 = SmemSize<3, KT>::bytes,
-                            b4 = SmemSize<4, KT>::bytes;
-    static constexpr size_t m12 = b1 > b2 ? b1 : b2, m34 = b3 > b4 ? b3 : b4;
-    static constexpr size_t bytes = m12 > m34 ? m12 : m34;
-};
+// Tile shapes the autotuner chooses from: column slices S for p = 1..4
+// (index 0 unused); every ND * S fits the CTA's 320 threads.
+constexpr int BATCH_SHAPES = 3;
+constexpr int kBatchShapes[BATCH_SHAPES][5] = {{0, 8, 8, 4, 3}, {0, 16, 10, 5, 3}, {0, 24, 10, 5, 2}};
 
-template <typename KT>
+constexpr size_t zmax(size_t a, size_t b) { return a > b ? a : b; }
+template <typename KT, int V> struct ShapeSmem {
+    static constexpr size_t bytes =
+        zmax(zmax(SmemSize<1, KT, kBatchShapes[V][1]>::bytes, SmemSize<2, KT, kBatchShapes[V][2]>::bytes),
+             zmax(SmemSize<3, KT, kBatchShapes[V][3]>::bytes, SmemSize<4, KT, kBatchShapes[V][4]>::bytes));
+};
+template <typename KT> struct BatchSmem {
+    static constexpr size_t bytes = zmax(ShapeSmem<KT, 0>::bytes, zmax(ShapeSmem<KT, 1>::bytes, ShapeSmem<KT, 2>::bytes));
+};
+static_assert(Deg<1>::ND * kBatchShapes[2][1] <= BATCH_THREADS && Deg<2>::ND * kBatchShapes[1][2] <= BATCH_THREADS &&
+                  Deg<3>::ND * kBatchShapes[1][3] <= BATCH_THREADS && Deg<4>::ND * kBatchShapes[0][4] <= BATCH_THREADS,
+              "every tile shape fits the CTA");
+
+template <typename KT, int V>
 __global__ void __launch_bounds__(BATCH_THREADS, BATCH_MINB)
 k_step_batch(const BatchProblem* __restrict__ probs, const int2* __restrict__ items, int n_items, int* queue,
              const int64_t* step_idx, const double* gvals, int64_t g_stride) {
@@ -75,10 +90,10 @@ k_step_batch(const BatchProblem* __restrict__ probs, const int2* __restrict__ it
         A.gvals = gvals + (int64_t)w.x * g_stride;
         A.step_idx = step_idx;
         switch (probs[w.x].p) {
-            case 1: step_poly<1, KT, MODE_STEP>(A, w.y, smem); break;
-            case 2: step_poly<2, KT, MODE_STEP>(A, w.y, smem); break;
-            case 3: step_poly<3, KT, MODE_STEP>(A, w.y, smem); break;
-            default: step_poly<4, KT, MODE_STEP>(A, w.y, smem); break;
+            case 1: step_poly<1, KT, MODE_STEP, kBatchShapes[V][1]>(A, w.y, smem); break;
+            case 2: step_poly<2, KT, MODE_STEP, kBatchShapes[V][2]>(A, w.y, smem); break;
+            case 3: step_poly<3, KT, MODE_STEP, kBatchShapes[V][3]>(A, w.y, smem); break;
+            default: step_poly<4, KT, MODE_STEP, kBatchShapes[V][4]>(A, w.y, smem); break;
         }
     }
 }
@@ -92,22 +107,22 @@ std::string tune_cache_path() {
     const char* e = std::getenv("LYMPH_TUNE_CACHE");
     if (e && *e) return e;
     const char* h = std::getenv("HOME");
-    return std::string(h ? h : "/tmp") + "/.cache/lymph3d_gb300_tune.txt";
+    return std::string(h ? h : "/tmp") + "/.cache/lymph3d_gb300_tune2.txt";
 }
 
 std::mutex g_tune_mu;
 
-bool tune_lookup(const std::string& key, int* grid, int* order) {
+bool tune_lookup(const std::string& key, int* grid, int* order, int* shape) {
     std::lock_guard<std::mutex> l(g_tune_mu);
     std::ifstream f(tune_cache_path());
     std::string k;
-    int g, o;
-    while (f >> k >> g >> o)
-        if (k == key) { *grid = g; *order = o; return true; }
+    int g, o, sh;
+    while (f >> k >> g >> o >> sh)
+        if (k == key && sh >= 0 && sh < BATCH_SHAPES) { *grid = g; *order = o; *shape = sh; return true; }
     return false;
 }
 
-void tune_store(const std::string& key, int grid, int order) {
+void tune_store(const std::string& key, int grid, int order, int shape) {
     std::lock_guard<std::mutex> l(g_tune_mu);
     std::string path = tune_cache_path();
     size_t slash = path.rfind('/');
@@ -117,7 +132,7 @@ void tune_store(const std::string& key, int grid, int order) {
         if (ec) return;
     }
     std::ofstream f(path, std::ios::app);
-    f << key << " " << grid << " " << order << "\n";
+    f << key << " " << grid << " " << order << " " << shape << "\n";
 }
 
 }  // namespace
@@ -132,6 +147,7 @@ struct lymph_batch {
     std::vector<int2> items_lpt, items_natural;
     int order = 0;       // 0 = largest cost first, 1 = problem-major
     int grid = 0;
+    int shape = 0;       // tile shape (kBatchShapes row) of the FP64 / FP32-block kernel
     int* d_queue = nullptr;
     int64_t* d_step_idx = nullptr;
     double* d_gvals = nullptr;
@@ -185,6 +201,19 @@ int refresh_problems(lymph_batch* b) {
     return LYMPH_OK;
 }
 
+template <typename KT>
+void launch_shape(lymph_batch* b, const BatchProblem* probs, int64_t g_stride) {
+    auto go = [&](auto kernel) {
+        kernel<<<b->grid, BATCH_THREADS, 0, b->stream>>>(probs, b->d_items, b->n_items, b->d_queue, b->d_step_idx,
+                                                         b->d_gvals, g_stride);
+    };
+    switch (b->shape) {
+        case 1: go(k_step_batch<KT, 1>); break;
+        case 2: go(k_step_batch<KT, 2>); break;
+        default: go(k_step_batch<KT, 0>); break;
+    }
+}
+
 // kernel launches per batched step
 int step_launches(const lymph_batch* b) { return b->precision == LYMPH_MIXED_MF ? 3 : 2; }
 
@@ -194,11 +223,9 @@ int launch_step(lymph_batch* b, int64_t g_stride) {
         LYMPH_TRY(lymph_mf_batch_step(b->stream, b->grid, b->d_probs, b->d_items, b->n_items, b->d_queue, b->d_step_idx,
                                       b->d_gvals, g_stride));
     else if (b->precision == LYMPH_MIXED)
-        k_step_batch<float><<<b->grid, BATCH_THREADS, 0, b->stream>>>(probs, b->d_items, b->n_items, b->d_queue,
-                                                                     b->d_step_idx, b->d_gvals, g_stride);
+        launch_shape<float>(b, probs, g_stride);
     else
-        k_step_batch<double><<<b->grid, BATCH_THREADS, 0, b->stream>>>(probs, b->d_items, b->n_items, b->d_queue,
-                                                                      b->d_step_idx, b->d_gvals, g_stride);
+        launch_shape<double>(b, probs, g_stride);
     k_batch_bump<<<1, 1, 0, b->stream>>>(b->d_step_idx, b->d_queue);
     b->launches += step_launches(b);
     LYMPH_CUDA_TRY(cudaGetLastError());
@@ -318,8 +345,9 @@ int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out) {
     cudaMemsetAsync(b->d_status, 0, sizeof(int), b->stream);
     b->grid = 4 * b->sms;
     b->order = 0;
-    int g, o;
-    if (tune_lookup(b->key, &g, &o)) { b->grid = g; b->order = o; }
+    b->shape = 0;
+    int g, o, sh;
+    if (tune_lookup(b->key, &g, &o, &sh)) { b->grid = g; b->order = o; b->shape = sh; }
     int rc = upload_items(b);
     if (rc) return fail(rc);
     *out = b;
@@ -362,15 +390,17 @@ int lymph_batch_run(lymph_batch* b, int64_t n_steps, const double* gvals, float*
 
 int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache, int32_t* grid, int32_t* order) {
     if (!b || trial_steps < 1) return LYMPH_ERR_INVALID;
-    int g0, o0;
-    if (use_cache && tune_lookup(b->key, &g0, &o0)) {
+    int g0, o0, s0;
+    if (use_cache && tune_lookup(b->key, &g0, &o0, &s0)) {
         b->grid = g0;
         b->order = o0;
+        b->shape = s0;
         LYMPH_TRY(upload_items(b));
     } else {
-        // candidates: persistent grids of 1..4 CTAs per SM, two item orders.
-        // The trial steps advance the real state, so the state is saved and
-        // restored around the trials.
+        // candidates: persistent grids of 1..4 CTAs per SM (1..5 for the
+        // matrix-free kernel), two item orders and, for the block kernel, the
+        // tile shapes.  The trial steps advance the real state, so the state
+        // is saved and restored around the trials.
         std::vector<std::vector<double>> save(b->ctx.size() * 2);
         for (size_t i = 0; i < b->ctx.size(); ++i) {
             lymph_ctx* c = b->ctx[i];
@@ -385,13 +415,16 @@ int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache,
         std::vector<double> g((size_t)b->ctx.size() * (trial_steps + 1), 0.0);
         LYMPH_TRY(upload_g(b, g.data(), trial_steps + 1));
         float best = 1e30f;
-        int bg = b->grid, bo = b->order;
+        int bg = b->grid, bo = b->order, bs = b->shape;
+        const int n_shapes = b->precision == LYMPH_MIXED_MF ? 1 : BATCH_SHAPES;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         const int max_mult = b->precision == LYMPH_MIXED_MF ? 5 : BATCH_MINB;  // CTAs per SM the kernel fits
+        for (int shp = 0; shp < n_shapes; ++shp)
         for (int ord = 0; ord < 2; ++ord)
             for (int mult = 1; mult <= max_mult; ++mult) {
+                b->shape = shp;
                 b->order = ord;
                 b->grid = mult * b->sms;
                 LYMPH_TRY(upload_items(b));
@@ -402,7 +435,7 @@ int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache,
                 cudaEventSynchronize(e1);
                 float ms = 0.0f;
                 cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < best) { best = ms; bg = b->grid; bo = ord; }
+                if (ms < best) { best = ms; bg = b->grid; bo = ord; bs = shp; }
             }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -416,12 +449,21 @@ int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache,
         LYMPH_CUDA_TRY(cudaMemset(b->d_status, 0, sizeof(int)));
         b->grid = bg;
         b->order = bo;
+        b->shape = bs;
         LYMPH_TRY(upload_items(b));
-        tune_store(b->key, bg, bo);
+        tune_store(b->key, bg, bo, bs);
     }
     if (grid) *grid = b->grid;
     if (order) *order = b->order;
     LYMPH_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    return LYMPH_OK;
+}
+
+int lymph_batch_schedule(const lymph_batch* b, int32_t* grid, int32_t* order, int32_t* shape) {
+    if (!b) return LYMPH_ERR_INVALID;
+    if (grid) *grid = b->grid;
+    if (order) *order = b->order;
+    if (shape) *shape = b->shape;
     return LYMPH_OK;
 }
 

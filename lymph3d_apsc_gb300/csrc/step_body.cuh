@@ -52,8 +52,8 @@ __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 // and the row partial sums in the accumulation type, then the FP64 right-hand
 // side at an offset rounded up to 16 bytes (with FP32 blocks and odd ND the
 // raw offset is not 8-byte aligned).
-template <int PD, typename KT> struct SmemSize {
-    static constexpr int ND = Deg<PD>::ND, S = Shape<PD>::S;
+template <int PD, typename KT, int S_ = Shape<PD>::S> struct SmemSize {
+    static constexpr int ND = Deg<PD>::ND, S = S_;
     static constexpr size_t b_offset = ((sizeof(KT) * (size_t)(NBB * ND + S * ND)) + 15) & ~(size_t)15;
     static constexpr size_t bytes = b_offset + sizeof(double) * ND;
 };
@@ -122,18 +122,19 @@ __device__ __forceinline__ void finish_poly(const StepArgs& A, int P, double y, 
 
 // The block row of polyhedron P is one contiguous column-major
 // [ND x nb*ND] matrix (its blocks are adjacent in memory), multiplied by the
-// gathered coefficients of the column polyhedra, then finish_poly.  Every
-// thread of the CTA must call this (it synchronises); threads beyond the
+// gathered coefficients of the column polyhedra, then finish_poly.  S_ is
+// the number of column slices (the tile shape; the CTA needs ND * S_ threads).
+// Every thread of the CTA must call this (it synchronises); threads beyond the
 // degree's shape only help with the gather.
-template <int PD, typename KT, int MODE>
+template <int PD, typename KT, int MODE, int S_ = Shape<PD>::S>
 __device__ __forceinline__ void step_poly(const StepArgs& A, int P, char* smem) {
-    constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND, S = Shape<PD>::S;
+    constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND, S = S_;
     constexpr int CPT = (ND + S - 1) / S;
     using AT = KT;  // FP64 blocks accumulate in FP64, FP32 blocks in FP32
     AT* s_u = (AT*)smem;
     AT* s_red = s_u + NBB * ND;
-    double* s_b = (double*)(smem + SmemSize<PD, KT>::b_offset);
-    static_assert(SmemSize<PD, KT>::b_offset % 16 == 0, "FP64 rhs must be 16-byte aligned");
+    double* s_b = (double*)(smem + SmemSize<PD, KT, S>::b_offset);
+    static_assert(SmemSize<PD, KT, S>::b_offset % 16 == 0, "FP64 rhs must be 16-byte aligned");
     const int nthr = blockDim.x;
     const int tid = threadIdx.x;
     const int r = tid % ND, s = tid / ND;

@@ -111,6 +111,12 @@ class Batch:
               "lymph_batch_autotune")
         return g.value, o.value
 
+    def schedule(self):
+        """(grid, order, tile shape) the batch runs with."""
+        g, o, sh = c_int32(), c_int32(), c_int32()
+        check(self.lib.lymph_batch_schedule(self.h, byref(g), byref(o), byref(sh)), "lymph_batch_schedule")
+        return g.value, o.value, sh.value
+
     def run(self, gvals: np.ndarray) -> float:
         """gvals: (n_problems, n_steps) time-function values; returns the
         device time of the loop in ms."""
