@@ -367,10 +367,11 @@ def run_ensemble(cfg, precision, steps, warmup, info):
     t1 = time.perf_counter()
     b = E.Batch(solvers)
     grid, order = b.autotune(trial_steps=2)
+    shape = b.schedule()[2]
     t2 = time.perf_counter()
     dofs = sum(m["dofs"] for m in meta)
     log(f"[bench] ensemble of {len(meta)}: {dofs} DOFs, {sum(m['n_blocks'] for m in meta)} blocks, set-up "
-        f"{t1 - t0:.1f}s, autotune {t2 - t1:.1f}s -> grid {grid}, order {order}")
+        f"{t1 - t0:.1f}s, autotune {t2 - t1:.1f}s -> grid {grid}, order {order}, tile shape {shape}")
     b.run(E.ensemble_gvals(meta, warmup))
     g = E.ensemble_gvals(meta, steps)
     l0 = b.launch_count()
@@ -387,7 +388,7 @@ def run_ensemble(cfg, precision, steps, warmup, info):
     for s in solvers:
         s.close()
     return {"dofs": dofs, "steps": steps, "ms": ms, "seq_ms": seq_ms, "launches": launches, "clocks": clk.summary(),
-            "grid": grid, "order": order, "finite": finite, "meta": meta}
+            "grid": grid, "order": order, "shape": shape, "finite": finite, "meta": meta}
 
 
 def run_surrogate(cfg, steps):
@@ -642,6 +643,7 @@ def main():
         print(json.dumps(line), flush=True)
         return
     if cfg.get("ensemble"):
+        from lymph3d_apsc_gb300.ensemble import BATCH_TILE_SHAPES
         r = run_ensemble(cfg, precision, args.steps, args.warmup, info)
         value = r["dofs"] * r["steps"] / (r["ms"] / 1e3)
         degrees = {}
@@ -655,7 +657,9 @@ def main():
                                        f"n~U{{{cfg['n_range'][0]}..{cfg['n_range'][1]}}}, BFS groups 4-16, p~U{{1..4}}, "
                                        "Ricker f0~U[5,20] Hz, x0~U[0.2,0.8]^3, own CFL dt (0.8 x 2/sqrt(lambda_max))",
                            "problems": len(r["meta"]), "degrees": degrees, "dofs": r["dofs"],
-                           "autotuned_grid": r["grid"], "autotuned_order": ["largest-first", "problem-major"][r["order"]]},
+                           "autotuned_grid": r["grid"], "autotuned_order": ["largest-first", "problem-major"][r["order"]],
+                           "autotuned_tile_shape": None if precision == 2 else
+                           {"column_slices_p1_to_p4": list(BATCH_TILE_SHAPES[r["shape"]])}},
                 "sequential_value": r["dofs"] * r["steps"] / (r["seq_ms"] / 1e3),
                 "batched_speedup_vs_sequential": r["seq_ms"] / r["ms"],
                 "state_finite": r["finite"], "gpu_launches": r["launches"], "clocks": r["clocks"]}

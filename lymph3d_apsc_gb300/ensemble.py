@@ -83,6 +83,11 @@ def double_couple(s: MatrixFree, x0, strike, normal, M0: float, which: int = _li
     return tet.value
 
 
+# The batch kernel's tile shapes: column slices S for p = 1..4 (the C table
+# kBatchShapes in csrc/batch.cu); lymph_batch_schedule reports the index.
+BATCH_TILE_SHAPES = ((8, 8, 4, 3), (16, 10, 5, 3), (24, 10, 5, 2))
+
+
 class Batch:
     """Problems advanced together; each keeps its own context."""
 
