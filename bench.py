@@ -505,11 +505,9 @@ def run_mpnn_forward(cfg, info):
     graph = S.build_graph(m)
     N = m.n_poly
     out = {"n_nodes": N}
-    for label, simt, ws, ps in (("tensor_cores", "0", "1", "1"), ("tensor_cores_tile_per_cta", "0", "1", "0"),
-                                ("tensor_cores_cpasync", "0", "0", "0"), ("simt", "1", "1", "1")):
+    for label, simt, ws in (("tensor_cores", "0", "1"), ("tensor_cores_cpasync", "0", "0"), ("simt", "1", "1")):
         os.environ["LYMPH_MPNN_SIMT"] = simt
         os.environ["LYMPH_UMMA_WS"] = ws
-        os.environ["LYMPH_UMMA_PERSIST"] = ps
         net = S.surrogate_net(cfg["p"], H=mf["H"], L=mf["L"])
         net.set_graph(graph)
         x = np.random.default_rng(0).standard_normal((N, net.F)).astype(np.float32)
@@ -525,7 +523,6 @@ def run_mpnn_forward(cfg, info):
         net.close()
     os.environ.pop("LYMPH_MPNN_SIMT", None)
     os.environ.pop("LYMPH_UMMA_WS", None)
-    os.environ.pop("LYMPH_UMMA_PERSIST", None)
     return out
 
 
@@ -608,7 +605,6 @@ def main():
                              "tensor_issue_tflops": 2.0 * tfl},
                 "simt_ms": r["simt"]["ms"], "speedup_vs_simt": r["simt"]["ms"] / tc["ms"],
                 "cpasync_kernel_ms": r["tensor_cores_cpasync"]["ms"],
-                "tile_per_cta_kernel_ms": r["tensor_cores_tile_per_cta"]["ms"],
                 "uses_tensor_cores": tc["tensor_cores"], "gpu_launches": r["launches_per_forward"] * cfg["mpnn_forward"]["reps"],
                 "clocks": tc["clocks"]}
         print(json.dumps(line), flush=True)

@@ -32,7 +32,7 @@
 
 #include "common.cuh"
 #include "umma_gemm.cuh"
-#include "umma_ps.cuh"
+#include "umma_ws.cuh"
 
 int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);  // out = M^-1 K u (step.cu)
 int lymph_dev_apply_fp32(lymph_ctx* c, const float* K32, const double* u, double* out);
@@ -278,8 +278,6 @@ struct lymph_mpnn {
     bool wt_dirty = true;
     bool use_umma = true;         // LYMPH_MPNN_SIMT=1 selects the SIMT GEMMs for the forward too
     bool use_ws = true;           // LYMPH_UMMA_WS=0 selects the cp.async tensor-core kernel over the TMA one
-    bool use_ps = true;           // LYMPH_UMMA_PERSIST=0 selects the one-tile-per-CTA TMA kernel over the persistent one
-    int sms = 0;
     int* d_status = nullptr;      // bit 0: a tensor-core wait ran out
 };
 
@@ -388,19 +386,6 @@ void umma_gemm(lymph_mpnn* n, int pi, int M, const umma::Seg* segs, int nseg, co
         if (ok) {
             w.nseg = nseg; w.M = M; w.N = N; w.Npad = Npad; w.Ktot = Ktot;
             w.bias = bias; w.C = C; w.ldc = ldc; w.Z = Z; w.R = R; w.epi = epi; w.status = n->d_status;
-            if (n->use_ps) {
-                static bool attr_ps = false;
-                if (!attr_ps) {
-                    cudaFuncSetAttribute(umma::k_umma_gemm_ps, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)umma::PS_SMEM);
-                    attr_ps = true;
-                }
-                const int tiles = ((M + umma::BM - 1) / umma::BM) * ((Npad + umma::WS_BN - 1) / umma::WS_BN);
-                const int grid = tiles < n->sms ? tiles : n->sms;
-                umma::k_umma_gemm_ps<<<grid, umma::PS_THREADS, umma::PS_SMEM, n->stream>>>(w);
-                n->launches++;
-                return;
-            }
             static bool attr = false;
             if (!attr) {
                 cudaFuncSetAttribute(umma::k_umma_gemm_ws, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -870,14 +855,6 @@ int lymph_mpnn_create(int32_t F, int32_t H, int32_t O, int32_t L, int32_t G, lym
     n->use_umma = !(simt && simt[0] == '1');
     const char* ws = std::getenv("LYMPH_UMMA_WS");
     n->use_ws = !(ws && ws[0] == '0');
-    const char* ps = std::getenv("LYMPH_UMMA_PERSIST");
-    n->use_ps = !(ps && ps[0] == '0');
-    {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n->sms, cudaDevAttrMultiProcessorCount, dev);
-        if (n->sms <= 0) n->use_ps = false;
-    }
     if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) { delete n; lymph_set_error("lymph_mpnn_create: stream"); return LYMPH_ERR_CUDA; }
     size_t b = sizeof(float) * (size_t)n->n_par;
     if (cudaMalloc(&n->d_p, b) != cudaSuccess || cudaMalloc(&n->d_g, b) != cudaSuccess || cudaMalloc(&n->d_m, b) != cudaSuccess ||

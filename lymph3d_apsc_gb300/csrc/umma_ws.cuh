@@ -85,70 +85,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
-// Epilogue of one 128 x nb tile: warp (lane quarter q4) reads its 32 TMEM
-// lanes 32 columns at a time from tmem_acc, transposes them through its
-// shared-memory slot stg (32 x EPI_LD floats) and stores 16-byte row segments
-// with bias / ReLU / pre-activation / residual.
-__device__ __forceinline__ void ws_epilogue(const WsArgs& a, uint32_t tmem_acc, int q4, int lane, float* stg, int m0,
-                                            int n0, int nb) {
-    const bool vec = (a.N % 4 == 0) && (a.ldc % 4 == 0) && ((uintptr_t)a.C % 16 == 0) &&
-                     (!a.Z || (uintptr_t)a.Z % 16 == 0) && (!a.R || (uintptr_t)a.R % 16 == 0) &&
-                     (!a.bias || (uintptr_t)a.bias % 16 == 0);
-    const int nl = (a.N - n0) < nb ? (a.N - n0) : nb;
-    for (int c0 = 0; c0 < nl; c0 += 32) {
-        uint32_t r[32];
-        tmem_ld32(tmem_acc + ((uint32_t)(q4 * 32) << 16) + (uint32_t)c0, r);
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-            *(float4*)(stg + lane * EPI_LD + 4 * q) = make_float4(
-                __uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]), __uint_as_float(r[4 * q + 2]),
-                __uint_as_float(r[4 * q + 3]));
-        __syncwarp();
-        if (vec) {
-            const int cq = lane % 8, col = n0 + c0 + 4 * cq;
-            const bool cv = col < a.N;
-            const float4 b = (cv && a.bias) ? *(const float4*)(a.bias + col) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 2
-            for (int i = 0; i < 8; ++i) {
-                const int rr = 4 * i + lane / 8, row = m0 + q4 * 32 + rr;
-                if (!cv || row >= a.M) continue;
-                float4 x = *(const float4*)(stg + rr * EPI_LD + 4 * cq);
-                x.x += b.x; x.y += b.y; x.z += b.z; x.w += b.w;
-                const int64_t o = (int64_t)row * a.ldc + col;
-                if (a.epi == EPI_STORE) {
-                    *(float4*)(a.C + o) = x;
-                } else {
-                    if (a.Z) *(float4*)(a.Z + o) = x;
-                    float4 y = make_float4(fmaxf(x.x, 0.f), fmaxf(x.y, 0.f), fmaxf(x.z, 0.f), fmaxf(x.w, 0.f));
-                    if (a.epi == EPI_RES_RELU) {
-                        const float4 rv = *(const float4*)(a.R + o);
-                        y.x += rv.x; y.y += rv.y; y.z += rv.z; y.w += rv.w;
-                    }
-                    *(float4*)(a.C + o) = y;
-                }
-            }
-        } else {
-            const int col = n0 + c0 + lane;
-            const bool cv = col < a.N;
-            const float b = (cv && a.bias) ? a.bias[col] : 0.0f;
-            for (int i = 0; i < 32; ++i) {
-                const int row = m0 + q4 * 32 + i;
-                if (!cv || row >= a.M) continue;
-                const float x = stg[i * EPI_LD + lane] + b;
-                const int64_t o = (int64_t)row * a.ldc + col;
-                if (a.epi == EPI_STORE) {
-                    a.C[o] = x;
-                } else {
-                    if (a.Z) a.Z[o] = x;
-                    const float rl = x > 0.0f ? x : 0.0f;
-                    a.C[o] = (a.epi == EPI_RES_RELU) ? a.R[o] + rl : rl;
-                }
-            }
-        }
-        __syncwarp();
-    }
-}
-
 __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_constant__ WsArgs a) {
     extern __shared__ __align__(1024) char smem_raw[];
     char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -252,7 +188,63 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (done) {
             const int q4 = warp % 4;  // the TMEM lane quarter this warp may read
-            ws_epilogue(a, tmem, q4, lane, (float*)smem + q4 * 32 * EPI_LD, m0, n0, nb);
+            float* stg = (float*)smem + q4 * 32 * EPI_LD;
+            const bool vec = (a.N % 4 == 0) && (a.ldc % 4 == 0) && ((uintptr_t)a.C % 16 == 0) &&
+                             (!a.Z || (uintptr_t)a.Z % 16 == 0) && (!a.R || (uintptr_t)a.R % 16 == 0) &&
+                             (!a.bias || (uintptr_t)a.bias % 16 == 0);
+            const int nl = (a.N - n0) < nb ? (a.N - n0) : nb;
+            for (int c0 = 0; c0 < nl; c0 += 32) {
+                uint32_t r[32];
+                tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)c0, r);
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    *(float4*)(stg + lane * EPI_LD + 4 * q) = make_float4(
+                        __uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]), __uint_as_float(r[4 * q + 2]),
+                        __uint_as_float(r[4 * q + 3]));
+                __syncwarp();
+                if (vec) {
+                    const int cq = lane % 8, col = n0 + c0 + 4 * cq;
+                    const bool cv = col < a.N;
+                    const float4 b = (cv && a.bias) ? *(const float4*)(a.bias + col) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 2
+                    for (int i = 0; i < 8; ++i) {
+                        const int rr = 4 * i + lane / 8, row = m0 + q4 * 32 + rr;
+                        if (!cv || row >= a.M) continue;
+                        float4 x = *(const float4*)(stg + rr * EPI_LD + 4 * cq);
+                        x.x += b.x; x.y += b.y; x.z += b.z; x.w += b.w;
+                        const int64_t o = (int64_t)row * a.ldc + col;
+                        if (a.epi == EPI_STORE) {
+                            *(float4*)(a.C + o) = x;
+                        } else {
+                            if (a.Z) *(float4*)(a.Z + o) = x;
+                            float4 y = make_float4(fmaxf(x.x, 0.f), fmaxf(x.y, 0.f), fmaxf(x.z, 0.f), fmaxf(x.w, 0.f));
+                            if (a.epi == EPI_RES_RELU) {
+                                const float4 rv = *(const float4*)(a.R + o);
+                                y.x += rv.x; y.y += rv.y; y.z += rv.z; y.w += rv.w;
+                            }
+                            *(float4*)(a.C + o) = y;
+                        }
+                    }
+                } else {
+                    const int col = n0 + c0 + lane;
+                    const bool cv = col < a.N;
+                    const float b = (cv && a.bias) ? a.bias[col] : 0.0f;
+                    for (int i = 0; i < 32; ++i) {
+                        const int row = m0 + q4 * 32 + i;
+                        if (!cv || row >= a.M) continue;
+                        const float x = stg[i * EPI_LD + lane] + b;
+                        const int64_t o = (int64_t)row * a.ldc + col;
+                        if (a.epi == EPI_STORE) {
+                            a.C[o] = x;
+                        } else {
+                            if (a.Z) a.Z[o] = x;
+                            const float rl = x > 0.0f ? x : 0.0f;
+                            a.C[o] = (a.epi == EPI_RES_RELU) ? a.R[o] + rl : rl;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
         }
     }
     // teardown: after an abort, let the work in flight finish (bounded) before
