@@ -54,13 +54,11 @@ struct MfTri {          // one triangle of a neighbour block, seen from the row 
 static_assert(sizeof(MfTri) == 80, "MfTri is 5 x 16 bytes");
 constexpr int MF_TRI_CHUNKS = (int)(sizeof(MfTri) / 16);
 
-struct MfPoly {         // Legendre map of a bounding box: xp = (x - c) ih, phi = sc L(xp_x) L(xp_y) L(xp_z)
-    float c[3];
-    float ih[3];
+struct MfPoly {         // Legendre scaling of a bounding box: xp = (x - centre) ih, phi = sc L(xp_x) L(xp_y) L(xp_z)
+    float ih[3];        // (the points are stored relative to the centres: MfTri)
     float sc;
-    float pad;
 };
-static_assert(sizeof(MfPoly) == 32, "MfPoly is 8 words");
+static_assert(sizeof(MfPoly) == 16, "MfPoly is one 16-byte copy");
 
 constexpr int MF_THREADS = 128;
 constexpr int MF_SLOTS = MF_THREADS / 3;   // test phase: point slots of three lanes (one per row component)
@@ -291,8 +289,7 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
         const int nt = (ntri - c) < CT ? ntri - c : CT;
         const char* src = (const char*)(A.tri + fb + c);
         for (int i = tid; i < nt * MF_TRI_CHUNKS; i += MF_THREADS) cp_async16((char*)s_tri[b] + 16 * i, src + 16 * i);
-        for (int i = tid; i < nt * 2; i += MF_THREADS)
-            cp_async16((char*)&s_polyQ[b][i / 2] + 16 * (i & 1), (const char*)(A.poly + getQ(c + i / 2)) + 16 * (i & 1));
+        for (int i = tid; i < nt; i += MF_THREADS) cp_async16(&s_polyQ[b][i], A.poly + getQ(c + i));
         for (int i = tid; i < nt * NP; i += MF_THREADS) {
             const int t = i / NP, bb = i - t * NP;
             cp_async16(&s_uQ[b][t][bb], A.u32 + (int64_t)getQ(c + t) * NP + bb);
@@ -554,13 +551,11 @@ __global__ void k_mf_polys(int n_poly, const double* __restrict__ bbox, MfPoly* 
     double hprod = 1.0;
     for (int d = 0; d < 3; ++d) {
         const double a = bbox[P * 6 + 2 * d], b = bbox[P * 6 + 2 * d + 1];
-        const double hb = (b - a) / 2.0, mb = (b + a) / 2.0;
-        m.c[d] = (float)mb;
+        const double hb = (b - a) / 2.0;
         m.ih[d] = (float)(1.0 / hb);
         hprod *= hb;
     }
     m.sc = (float)(1.0 / sqrt(hprod));
-    m.pad = 0.0f;
     out[P] = m;
 }
 
