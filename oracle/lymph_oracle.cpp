@@ -1349,6 +1349,71 @@ int oracle_nodal_values(void* h, int slot, double* out) {
     return 0;
 }
 
+// The neighbour product K_PQ u_Q evaluated point by point instead of from the
+// assembled block: the contraction the matrix-free mixed path applies on the
+// device (csrc/mf.cu), in FP64 with this oracle's face points, bases, normals
+// and penalty (MAKE_STIFFNESS_FACE, assemble_element.f90:404-661, inserted as
+// in matrix_free.f90:412-433).  Per quadrature point of a triangle of P's
+// tetrahedron t shared with Q, with v = u_Q(x), D_jk = d_k u_Q,j (x):
+//   out_(i,a) += sum_k d_k phi^P_a G_ik + phi^P_a s_i,
+//   G_ik = -theta/2 W (lambda (n.v) delta_ik + mu (n_i v_k + v_i n_k)),
+//   s_i  = -W (sigma (T v)_i + h_i / 2),
+//   h_i  = lambda sum_j n_j D_ji + mu n_i tr D + mu sum_k n_k D_ik.
+// Test infrastructure: it checks that rearrangement against the assembled
+// block.
+int oracle_neighbour_apply_pointwise(void* h, int P, int Qp, const double* uq, double* out) {
+    const Oracle& o = *(const Oracle*)h;
+    if (P < 0 || P >= o.n_poly || Qp < 0 || Qp >= o.n_poly || P == Qp) return LYMPH_ERR_INVALID;
+    const int Np = o.Np, nq2 = o.Q.nq2;
+    for (int r = 0; r < o.nd; ++r) out[r] = 0.0;
+    double bbP[3][2], bbQ[3][2];
+    get_bb(o, P, bbP);
+    get_bb(o, Qp, bbQ);
+    std::vector<double> pts, phP(Np), dP(3 * Np), phQ(Np), dQ(3 * Np);
+    for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1]; ++k) {
+        const int t = o.poly_tets[k];
+        const int mid = o.tet_mat[t];
+        const double lam = o.mat[mid * 3 + 1], mu = o.mat[mid * 3 + 2];
+        for (int f = 0; f < 4; ++f) {
+            const int E2 = o.neigh[t * 4 + f];
+            if (E2 < 0 || o.tet_poly[E2] != Qp) continue;
+            const double* n = &o.normal[t * 12 + f * 3];
+            const double ar = o.area[t * 4 + f];
+            const double sigma = o.alpha * (o.p * o.p) / std::min(o.hk[P], o.hk[Qp]) * (lam + 2 * mu);
+            const double T[3][3] = {{n[0] * n[0] + 0.5 * n[1] * n[1] + 0.5 * n[2] * n[2], 0.5 * n[0] * n[1], 0.5 * n[0] * n[2]},
+                                    {0.5 * n[1] * n[0], n[1] * n[1] + 0.5 * n[0] * n[0] + 0.5 * n[2] * n[2], 0.5 * n[1] * n[2]},
+                                    {0.5 * n[2] * n[0], 0.5 * n[2] * n[1], n[2] * n[2] + 0.5 * n[0] * n[0] + 0.5 * n[1] * n[1]}};
+            face_points(o, t, f, pts);
+            for (int q = 0; q < nq2; ++q) {
+                const double W = o.Q.weitria2[q] * ar;
+                eval_basis_point(&pts[q * 3], bbQ, Np, o.blist.data(), phQ.data(), dQ.data());
+                eval_basis_point(&pts[q * 3], bbP, Np, o.blist.data(), phP.data(), dP.data());
+                double v[3] = {0, 0, 0}, D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                for (int j = 0; j < 3; ++j)
+                    for (int b = 0; b < Np; ++b) {
+                        const double c = uq[j * Np + b];
+                        v[j] += phQ[b] * c;
+                        for (int kk = 0; kk < 3; ++kk) D[j][kk] += dQ[kk * Np + b] * c;
+                    }
+                const double nv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
+                const double trD = D[0][0] + D[1][1] + D[2][2];
+                for (int i = 0; i < 3; ++i) {
+                    double G[3];
+                    for (int kk = 0; kk < 3; ++kk)
+                        G[kk] = -0.5 * o.theta * W * ((i == kk ? lam * nv : 0.0) + mu * (n[i] * v[kk] + v[i] * n[kk]));
+                    const double Tv = T[i][0] * v[0] + T[i][1] * v[1] + T[i][2] * v[2];
+                    const double hh = lam * (n[0] * D[0][i] + n[1] * D[1][i] + n[2] * D[2][i]) + mu * n[i] * trD +
+                                      mu * (n[0] * D[i][0] + n[1] * D[i][1] + n[2] * D[i][2]);
+                    const double si = -W * (sigma * Tv + 0.5 * hh);
+                    for (int a = 0; a < Np; ++a)
+                        out[i * Np + a] += dP[a] * G[0] + dP[Np + a] * G[1] + dP[2 * Np + a] * G[2] + phP[a] * si;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
 int oracle_get_pattern(void* h, int32_t* row_ptr, int32_t* col, int64_t* n_blocks_out) {
     Oracle& o = *(Oracle*)h;
     int64_t nb = 0;

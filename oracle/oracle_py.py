@@ -69,6 +69,7 @@ def load():
             "oracle_solve_lu": (c_int, [P_F64, P_F64, c_int, P_F64]),
             "oracle_time_function": (c_double, [c_double]),
             "oracle_match_faces": (c_int, [c_int, P_I32, P_I32, P_I32]),
+            "oracle_neighbour_apply_pointwise": (c_int, [c_void_p, c_int, c_int, P_F64, P_F64]),
         }
         for k, (r, a) in sigs.items():
             f = getattr(lib, k)
@@ -181,6 +182,14 @@ class Oracle:
         rp, col = self.pattern()
         out = np.empty((col.size, self.nd, self.nd))
         self.lib.oracle_get_blocks(self.h, which, _p(out))
+        return out
+
+    def neighbour_apply_pointwise(self, P, Q, uq):
+        """K_PQ u_Q from the face quadrature point by point (FP64)."""
+        uq = np.ascontiguousarray(uq, dtype=np.float64)
+        out = np.empty(self.nd)
+        self._chk(self.lib.oracle_neighbour_apply_pointwise(self.h, int(P), int(Q), _p(uq), _p(out)),
+                  "oracle_neighbour_apply_pointwise")
         return out
 
     def block_dict(self, which=0):

@@ -1,0 +1,46 @@
+"""The matrix-free neighbour contraction against the assembled block (CPU).
+
+The mixed path with matrix-free neighbour terms (csrc/mf.cu) never forms the
+neighbour block K_PQ: it evaluates u_Q and its gradient at P's face
+quadrature points, forms the flux (G, s) and tests it against P's basis.  The
+oracle evaluates that same point-wise contraction in FP64
+(oracle_neighbour_apply_pointwise), and this test checks it against K_PQ u_Q
+from the oracle's assembled blocks: the two are the same sums in another
+order, so they agree to FP64 rounding (1e-12 normwise relative per block),
+with heterogeneous materials (lambda != mu per polyhedron), jittered
+tetrahedra and every interior-penalty variant theta = -1, 0, 1.
+"""
+import numpy as np
+import pytest
+
+from lymph3d_apsc_gb300 import mesh as M
+from oracle.oracle_py import Oracle
+
+
+def _mesh():
+    m0 = M.cube(3, bc="dirichlet", agglomeration="bfs", seed=1, group=(4, 12), jitter=0.15)
+    return M.cube(3, bc="dirichlet", agglomeration="bfs", seed=1, group=(4, 12), jitter=0.15,
+                  poly_materials=M.lognormal_materials(m0.n_poly, seed=3))
+
+
+@pytest.mark.parametrize("theta", [-1.0, 0.0, 1.0])
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_pointwise_neighbour_product_equals_the_block(p, theta):
+    m = _mesh()
+    o = Oracle(m, p, 1e-3, theta=theta)
+    o.make_matrices()
+    blocks = o.block_dict(0)
+    rng = np.random.default_rng(p)
+    worst, pairs = 0.0, 0
+    for (P, Q), K in blocks.items():
+        if P == Q:
+            continue
+        u = rng.standard_normal(o.nd)
+        want = K @ u
+        got = o.neighbour_apply_pointwise(P, Q, u)
+        worst = max(worst, float(np.linalg.norm(got - want) / np.linalg.norm(want)))
+        pairs += 1
+    o.close()
+    assert pairs >= 50
+    print(f"p={p} theta={theta}: {pairs} neighbour blocks, worst relative difference {worst:.2e}")
+    assert worst <= 1e-12, worst
