@@ -34,13 +34,16 @@
 namespace umma {
 
 constexpr int WS_STAGES = 3;
-constexpr int WS_THREADS = 192;
+constexpr int WS_SPLIT_WARPS = 8;                   // split / epilogue warps (2 ..), a multiple of 4
+constexpr int WS_SPLIT = 32 * WS_SPLIT_WARPS;
+constexpr int WS_THREADS = 64 + WS_SPLIT;
 constexpr int WS_BN = 256;
 constexpr size_t WS_TILE_A = (size_t)BM * BK * 4;                      // 16 KB
 constexpr size_t WS_STAGE = 2 * WS_TILE_A + (size_t)WS_BN * BK * 4;     // 64 KB
 constexpr size_t WS_BAR_OFF = WS_STAGES * WS_STAGE;
 constexpr size_t WS_SMEM = WS_BAR_OFF + 256 + 1024;  // + barriers, + room to align to 1 KB
-static_assert((size_t)4 * 32 * EPI_LD * 4 <= WS_STAGE, "epilogue staging exceeds a stage");
+static_assert((size_t)WS_SPLIT_WARPS * 32 * EPI_LD * 4 <= WS_BAR_OFF, "epilogue staging exceeds the stages");
+static_assert(WS_SPLIT_WARPS % 4 == 0, "whole groups of 4 warps (one per TMEM lane quarter)");
 
 struct alignas(64) WsArgs {
     CUtensorMap mapA[3];  // per K segment: [M][K_s] FP32, box 32 x 128, 128-byte swizzle
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
         s_abort = 0;
         for (int s = 0; s < WS_STAGES; ++s) {
             mbar_init(smem_u32(&full[s]), 1);
-            mbar_init(smem_u32(&split[s]), 128);
+            mbar_init(smem_u32(&split[s]), WS_SPLIT);
             mbar_init(smem_u32(&empty[s]), 1);
         }
         mbar_init(smem_u32(acc), 1);
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
             float4* hi = (float4*)(smem + st * WS_STAGE);
             float4* lo = (float4*)(smem + st * WS_STAGE + WS_TILE_A);
 #pragma unroll 4
-            for (int i = u; i < BM * BK / 4; i += 128) {
+            for (int i = u; i < BM * BK / 4; i += WS_SPLIT) {
                 const float4 v = hi[i];
                 float4 h, l;
                 h.x = __uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u); l.x = v.x - h.x;
@@ -188,12 +191,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (done) {
             const int q4 = warp % 4;  // the TMEM lane quarter this warp may read
-            float* stg = (float*)smem + q4 * 32 * EPI_LD;
+            float* stg = (float*)smem + (warp - 2) * 32 * EPI_LD;
+            const int grp = (warp - 2) / 4;  // groups of 4 warps take interleaved 32-column blocks
             const bool vec = (a.N % 4 == 0) && (a.ldc % 4 == 0) && ((uintptr_t)a.C % 16 == 0) &&
                              (!a.Z || (uintptr_t)a.Z % 16 == 0) && (!a.R || (uintptr_t)a.R % 16 == 0) &&
                              (!a.bias || (uintptr_t)a.bias % 16 == 0);
             const int nl = (a.N - n0) < nb ? (a.N - n0) : nb;
-            for (int c0 = 0; c0 < nl; c0 += 32) {
+            for (int c0 = 32 * grp; c0 < nl; c0 += 32 * (WS_SPLIT_WARPS / 4)) {
                 uint32_t r[32];
                 tmem_ld32(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)c0, r);
 #pragma unroll
