@@ -34,7 +34,7 @@
 namespace umma {
 
 constexpr int WS_STAGES = 3;
-constexpr int WS_SPLIT_WARPS = 8;                   // split / epilogue warps (2 ..), a multiple of 4
+constexpr int WS_SPLIT_WARPS = 16;                  // split / epilogue warps (2 ..), a multiple of 4
 constexpr int WS_SPLIT = 32 * WS_SPLIT_WARPS;
 constexpr int WS_THREADS = 64 + WS_SPLIT;
 constexpr int WS_BN = 256;
