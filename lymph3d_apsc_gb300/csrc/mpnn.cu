@@ -132,41 +132,12 @@ __global__ void k_aggregate(int n, int width, const int32_t* __restrict__ ptr, c
 // The same with one warp per node and 16-byte loads (width a multiple of 4):
 // each neighbour row is read as one coalesced segment; the sum over the
 // neighbours runs in the CSR order, as in k_aggregate.
-// Widths up to AGG_SEGS x 128 keep a lane's columns in registers, so each
-// neighbour's index and weight are read once and its row segments load
-// together (the neighbour loop outermost; each element still sums in CSR
-// order).
-constexpr int AGG_SEGS = 4;
-
 __global__ void __launch_bounds__(256) k_aggregate_v4(int n, int width, const int32_t* __restrict__ ptr,
                                                       const int32_t* __restrict__ idx, const float* __restrict__ val,
                                                       const float* __restrict__ in, float* out) {
     const int i = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
     if (i >= n) return;
     const int k0 = ptr[i], k1 = ptr[i + 1];
-    if (width <= AGG_SEGS * 128) {
-        float4 s[AGG_SEGS];
-#pragma unroll
-        for (int j = 0; j < AGG_SEGS; ++j) s[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int k = k0; k < k1; ++k) {
-            const float w = val[k];
-            const float* row = in + (int64_t)idx[k] * width;
-#pragma unroll
-            for (int j = 0; j < AGG_SEGS; ++j) {
-                const int c = 4 * lane + 128 * j;
-                if (c < width) {
-                    const float4 v = *(const float4*)(row + c);
-                    s[j].x += w * v.x; s[j].y += w * v.y; s[j].z += w * v.z; s[j].w += w * v.w;
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < AGG_SEGS; ++j) {
-            const int c = 4 * lane + 128 * j;
-            if (c < width) *(float4*)(out + (int64_t)i * width + c) = s[j];
-        }
-        return;
-    }
     for (int c = 4 * lane; c < width; c += 128) {
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int k = k0; k < k1; ++k) {
