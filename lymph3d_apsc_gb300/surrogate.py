@@ -1,7 +1,7 @@
 """Learned surrogate: a per-polyhedron message-passing network that advances
 the modal state K steps at a time, with the plain leapfrog stepper as its
-fallback and judge.  No counterpart in the reference (config 4 of the
-project specification).
+fallback and judge.  No counterpart in the reference (the reference has no
+learned component).
 
 One surrogate block, from (u^{n-1}, u^n) at time t_n:
   1. one plain step gives u^{n+1};
