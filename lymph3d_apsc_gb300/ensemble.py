@@ -139,7 +139,7 @@ class Batch:
 
 def make_ensemble(n_problems: int = 64, seed: int = 2, n_range=(8, 32), p_range=(1, 4), group=(4, 16),
                   precision: int = _lib.FP64, cfl: float = 0.8, material=(1.0, 1.0, 1.0), eig_iters: int = 60):
-    """The seeded ensemble of config 3.  Returns (solvers, meta) with the
+    """A seeded ensemble of independent problems.  Returns (solvers, meta) with the
     solvers assembled, sources set, dt chosen as cfl * 2/sqrt(lambda_max) and
     the first leapfrog step taken from rest."""
     rng = np.random.default_rng(seed)
