@@ -390,7 +390,8 @@ int lymph_max_eigenvalue(lymph_ctx* ctx, int32_t iters, double* lam);
  * references n assembled contexts (same precision; any degrees, meshes and
  * dt).  lymph_batch_run advances every problem n_steps leapfrog steps
  * (TIME_STEP_MATRIX_FREE each) with one persistent kernel per step over all
- * (problem, polyhedron) items, launched as CUDA graphs; gvals holds the
+ * (problem, polyhedron) items (LYMPH_MIXED_MF: one per degree present, each
+ * over that degree's items), launched as CUDA graphs; gvals holds the
  * time-function value of every problem at every step, [n][n_steps].  Results
  * equal stepping each context alone, bit for bit, with the default schedule
  * (see lymph_batch_autotune for tuned tile shapes). */
@@ -399,7 +400,9 @@ int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out);
 int lymph_batch_destroy(lymph_batch* batch);
 int lymph_batch_run(lymph_batch* batch, int64_t n_steps, const double* gvals, float* ms_total);
 /* Times trial_steps steps for each candidate (1..4 persistent CTAs per SM,
- * 1..5 for LYMPH_MIXED_MF; items largest-cost-first or problem-major; for
+ * for LYMPH_MIXED_MF 1..what one SM holds of the lowest degree's kernel, each
+ * degree's grid capped at what the SMs hold of its own kernel; items
+ * largest-cost-first or problem-major; for
  * LYMPH_FP64 / LYMPH_MIXED also three tile shapes, the column slices per
  * degree) and keeps the fastest; the problems' states are restored
  * afterwards.  The choice is cached per batch signature in $LYMPH_TUNE_CACHE

@@ -16,7 +16,10 @@
 // the number of column slices S per degree (kBatchShapes).  Shape 0, the
 // default before tuning, is the single-problem kernel's, so results are then
 // bit-identical to stepping each context alone; the other shapes group the
-// row's partial sums differently (deterministic, equal to rounding).
+// row's partial sums differently (deterministic, equal to rounding).  On the
+// matrix-free path (mf.cu) the items are grouped by degree and each degree
+// present gets its own persistent launch per step, so every degree runs
+// with its own register and shared-memory budget.
 
 #include <algorithm>
 #include <cstdlib>
@@ -34,14 +37,16 @@
 using namespace stepk;
 
 size_t lymph_mf_batch_problem_bytes();
+int lymph_mf_batch_ctas_per_sm(int p);
 void lymph_mf_batch_problem(const lymph_ctx* c, int* status, void* out);
-int lymph_mf_batch_step(cudaStream_t st, int grid, const void* probs, const int2* items, int n_items, int* queue,
-                        const int64_t* step_idx, const double* gvals, int64_t g_stride);
+int lymph_mf_batch_step(cudaStream_t st, const int* grid, const void* probs, const int2* items, const int* off,
+                        int* queue, const int64_t* step_idx, const double* gvals, int64_t g_stride, int* launched);
 
 namespace {
 
 constexpr int BATCH_THREADS = 320;   // the p = 4 shape; lower degrees leave lanes idle
 constexpr int BATCH_MINB = 4;
+constexpr int BATCH_QUEUES = 4;      // item counters: one per degree on the matrix-free path
 
 struct BatchProblem {
     StepArgs a;        // per-problem pointers; u0/un/out are filled per step
@@ -100,7 +105,7 @@ k_step_batch(const BatchProblem* __restrict__ probs, const int2* __restrict__ it
 
 __global__ void k_batch_bump(int64_t* idx, int* queue) {
     *idx += 1;
-    *queue = 0;
+    for (int i = 0; i < BATCH_QUEUES; ++i) queue[i] = 0;
 }
 
 std::string tune_cache_path() {
@@ -148,7 +153,9 @@ struct lymph_batch {
     int order = 0;       // 0 = largest cost first, 1 = problem-major
     int grid = 0;
     int shape = 0;       // tile shape (kBatchShapes row) of the FP64 / FP32-block kernel
-    int* d_queue = nullptr;
+    int* d_queue = nullptr;          // BATCH_QUEUES item counters (one per degree on the matrix-free path)
+    int mf_off[5] = {0, 0, 0, 0, 0};  // matrix-free path: degree p's items are [mf_off[p - 1], mf_off[p])
+    int mf_occ[4] = {1, 1, 1, 1};     // matrix-free path: CTAs per SM of each degree's kernel
     int64_t* d_step_idx = nullptr;
     double* d_gvals = nullptr;
     int64_t gvals_cap = 0;
@@ -156,6 +163,7 @@ struct lymph_batch {
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     int64_t launches = 0;
+    int step_nl = 2;     // kernels one batched step launches
     int sms = 0;
     std::string key;
 };
@@ -163,8 +171,21 @@ struct lymph_batch {
 namespace {
 
 int upload_items(lymph_batch* b) {
-    const std::vector<int2>& v = b->order == 0 ? b->items_lpt : b->items_natural;
-    LYMPH_CUDA_TRY(cudaMemcpyAsync(b->d_items, v.data(), v.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    const std::vector<int2>& v0 = b->order == 0 ? b->items_lpt : b->items_natural;
+    std::vector<int2> grouped;
+    const std::vector<int2>* v = &v0;
+    if (b->precision == LYMPH_MIXED_MF) {
+        // one group per degree, each in the chosen order
+        for (int p = 1; p <= 4; ++p) {
+            b->mf_off[p - 1] = (int)grouped.size();
+            for (const int2& w : v0)
+                if (b->ctx[w.x]->p == p) grouped.push_back(w);
+        }
+        b->mf_off[4] = (int)grouped.size();
+        v = &grouped;
+    }
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(b->d_items, v->data(), v->size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(b->stream));  // the host vector goes out of scope
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
     return LYMPH_OK;
 }
@@ -214,20 +235,27 @@ void launch_shape(lymph_batch* b, const BatchProblem* probs, int64_t g_stride) {
     }
 }
 
-// kernel launches per batched step
-int step_launches(const lymph_batch* b) { return b->precision == LYMPH_MIXED_MF ? 3 : 2; }
-
 int launch_step(lymph_batch* b, int64_t g_stride) {
     const BatchProblem* probs = (const BatchProblem*)b->d_probs;
-    if (b->precision == LYMPH_MIXED_MF)
-        LYMPH_TRY(lymph_mf_batch_step(b->stream, b->grid, b->d_probs, b->d_items, b->n_items, b->d_queue, b->d_step_idx,
-                                      b->d_gvals, g_stride));
-    else if (b->precision == LYMPH_MIXED)
+    int nl = 1;
+    if (b->precision == LYMPH_MIXED_MF) {
+        // per degree: the tuned grid, at most what the SMs hold of that
+        // degree's kernel and at most one CTA per item
+        int grid[4];
+        for (int p = 1; p <= 4; ++p) {
+            const int n = b->mf_off[p] - b->mf_off[p - 1];
+            grid[p - 1] = std::min(std::min(b->grid, b->mf_occ[p - 1] * b->sms), n);
+        }
+        LYMPH_TRY(lymph_mf_batch_step(b->stream, grid, b->d_probs, b->d_items, b->mf_off, b->d_queue, b->d_step_idx,
+                                      b->d_gvals, g_stride, &nl));
+    } else if (b->precision == LYMPH_MIXED) {
         launch_shape<float>(b, probs, g_stride);
-    else
+    } else {
         launch_shape<double>(b, probs, g_stride);
+    }
     k_batch_bump<<<1, 1, 0, b->stream>>>(b->d_step_idx, b->d_queue);
-    b->launches += step_launches(b);
+    b->step_nl = nl + 1;
+    b->launches += b->step_nl;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
 }
@@ -237,7 +265,7 @@ int launch_step(lymph_batch* b, int64_t g_stride) {
 int run_loop(lymph_batch* b, int64_t n, int64_t g_stride, bool use_graph) {
     LYMPH_TRY(refresh_problems(b));
     LYMPH_CUDA_TRY(cudaMemsetAsync(b->d_step_idx, 0, sizeof(int64_t), b->stream));
-    LYMPH_CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
+    LYMPH_CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, BATCH_QUEUES * sizeof(int), b->stream));
     const int R = 16;
     int64_t i = 0;
     if (use_graph && n >= R) {
@@ -257,7 +285,7 @@ int run_loop(lymph_batch* b, int64_t n, int64_t g_stride, bool use_graph) {
         }
         for (; i + R <= n; i += R) {
             LYMPH_CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
-            b->launches += (int64_t)step_launches(b) * R;
+            b->launches += (int64_t)b->step_nl * R;
         }
     }
     for (; i < n; ++i) LYMPH_TRY(launch_step(b, g_stride));
@@ -337,12 +365,14 @@ int lymph_batch_create(lymph_ctx* const* ctxs, int32_t n, lymph_batch** out) {
     const size_t prob_bytes = b->precision == LYMPH_MIXED_MF ? lymph_mf_batch_problem_bytes() : sizeof(BatchProblem);
     if (cudaMalloc(&b->d_probs, prob_bytes * n) != cudaSuccess ||
         cudaMalloc(&b->d_items, sizeof(int2) * b->n_items) != cudaSuccess ||
-        cudaMalloc(&b->d_queue, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_step_idx, sizeof(int64_t)) != cudaSuccess ||
+        cudaMalloc(&b->d_queue, BATCH_QUEUES * sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_step_idx, sizeof(int64_t)) != cudaSuccess ||
         cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess) {
         lymph_set_error("lymph_batch_create: device allocation failed");
         return fail(LYMPH_ERR_OOM);
     }
     cudaMemsetAsync(b->d_status, 0, sizeof(int), b->stream);
+    if (b->precision == LYMPH_MIXED_MF)
+        for (int p = 1; p <= 4; ++p) b->mf_occ[p - 1] = lymph_mf_batch_ctas_per_sm(p);
     b->grid = 4 * b->sms;
     b->order = 0;
     b->shape = 0;
@@ -397,9 +427,9 @@ int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache,
         b->shape = s0;
         LYMPH_TRY(upload_items(b));
     } else {
-        // candidates: persistent grids of 1..4 CTAs per SM (1..5 for the
-        // matrix-free kernel), two item orders and, for the block kernel, the
-        // tile shapes.  The trial steps advance the real state, so the state
+        // candidates: persistent grids of 1..k CTAs per SM (k: what one SM
+        // holds of the step kernel), two item orders and, for the block
+        // kernel, the tile shapes.  The trial steps advance the real state, so the state
         // is saved and restored around the trials.
         std::vector<std::vector<double>> save(b->ctx.size() * 2);
         for (size_t i = 0; i < b->ctx.size(); ++i) {
@@ -420,7 +450,8 @@ int lymph_batch_autotune(lymph_batch* b, int32_t trial_steps, int32_t use_cache,
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
-        const int max_mult = b->precision == LYMPH_MIXED_MF ? 5 : BATCH_MINB;  // CTAs per SM the kernel fits
+        const int max_mult =
+            b->precision == LYMPH_MIXED_MF ? *std::max_element(b->mf_occ, b->mf_occ + 4) : BATCH_MINB;
         for (int shp = 0; shp < n_shapes; ++shp)
         for (int ord = 0; ord < 2; ++ord)
             for (int mult = 1; mult <= max_mult; ++mult) {

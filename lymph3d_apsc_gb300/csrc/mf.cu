@@ -69,6 +69,9 @@ template <int PD> struct MfShape {
     static constexpr int NQ2 = L * L;             // quadrature points per triangle
     static constexpr int CT = MF_THREADS / NQ2;   // triangles per chunk
     static constexpr int NPT = CT * NQ2;          // points per chunk (one evaluating thread each)
+    // a point's (L, L') values of the three directions, padded to an odd
+    // number of 16-byte words so the points of a warp fall on distinct banks
+    static constexpr int LEGW = ((3 * L + 1) / 2 % 2 == 1) ? 2 * ((3 * L + 1) / 2) : 2 * ((3 * L + 1) / 2) + 2;
     static_assert(ND <= MF_THREADS, "one thread per row of the self block");
 };
 
@@ -110,68 +113,85 @@ __device__ __forceinline__ void legendre(float x, float2* out) {
     for (int n = 0; n <= PD; ++n) out[n] = make_float2(Lv[n], Ld[n]);
 }
 
-// Field and gradient of one component at a point by sum factorisation over
-// the basis triples (a, b, c): with X_a = (L_a, L'_a)(x) and likewise Y, Z,
+// Position of basis function (a, b, c) in the reference's order.
+template <int PD> struct Bidx {
+    int i[PD + 1][PD + 1][PD + 1];
+    constexpr Bidx() : i() {
+        constexpr Blist<PD> BL{};
+        for (int k = 0; k < Deg<PD>::NP; ++k) i[BL.d[k][0]][BL.d[k][1]][BL.d[k][2]] = k;
+    }
+};
+
+// Field and gradient of the three components at a point by sum
+// factorisation over the basis triples (a, b, c): with X_a = (L_a, L'_a)(x)
+// and likewise Y, Z,
 //   w0_ab = sum_c u_abc Z_c,  w1_ab = sum_c u_abc Z'_c,
 //   r0_a = sum_b w0_ab Y_b,  r1_a = sum_b w0_ab Y'_b,  r2_a = sum_b w1_ab Y_b,
 //   v = sum_a r0_a X_a, d_x = sum_a r0_a X'_a, d_y = sum_a r1_a X_a, d_z = sum_a r2_a X_a
-// (unscaled: the caller applies the bounding-box factors); uc[4 i] is the
-// coefficient of basis function i.
+// (unscaled: the caller applies the bounding-box factors).  uc[i] holds
+// (u_0, u_1, u_2, 0) of basis function i.  Each w sum runs over c = p-a-b
+// down to 0 (the basis order), each r sum over b = 0.., each output over
+// a = 0..; one (a, b) group is live at a time, so the three components cost
+// no more registers than one did with every w_ab held.
 template <int PD>
-__device__ __forceinline__ void eval_sf(const float* uc, const float2* X, const float2* Y, const float2* Z, float& v,
-                                        float& dx, float& dy, float& dz) {
-    constexpr Blist<PD> BL{};
-    constexpr int NP = Deg<PD>::NP;
-    float w0[PD + 1][PD + 1], w1[PD + 1][PD + 1];
+__device__ __forceinline__ void eval_sf3(const float4* uc, const float2* X, const float2* Y, const float2* Z,
+                                         float (&o)[3][4]) {
+    constexpr Bidx<PD> BI{};
 #pragma unroll
-    for (int a = 0; a <= PD; ++a)
-#pragma unroll
-        for (int b = 0; b <= PD; ++b) { w0[a][b] = 0.0f; w1[a][b] = 0.0f; }
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        const int a = BL.d[i][0], b = BL.d[i][1], c = BL.d[i][2];
-        const float uu = uc[4 * i];
-        w0[a][b] = fmaf(uu, Z[c].x, w0[a][b]);
-        w1[a][b] = fmaf(uu, Z[c].y, w1[a][b]);
-    }
-    v = dx = dy = dz = 0.0f;
+    for (int j = 0; j < 3; ++j) o[j][0] = o[j][1] = o[j][2] = o[j][3] = 0.0f;
 #pragma unroll
     for (int a = 0; a <= PD; ++a) {
-        float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+        float r[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r[j][0] = r[j][1] = r[j][2] = 0.0f;
 #pragma unroll
         for (int b = 0; b <= PD - a; ++b) {
-            r0 = fmaf(w0[a][b], Y[b].x, r0);
-            r1 = fmaf(w0[a][b], Y[b].y, r1);
-            r2 = fmaf(w1[a][b], Y[b].x, r2);
+            float w0[3] = {0.0f, 0.0f, 0.0f}, w1[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int c = PD - a - b; c >= 0; --c) {
+                const float4 uu = uc[BI.i[a][b][c]];
+                const float u3[3] = {uu.x, uu.y, uu.z};
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    w0[j] = fmaf(u3[j], Z[c].x, w0[j]);
+                    w1[j] = fmaf(u3[j], Z[c].y, w1[j]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                r[j][0] = fmaf(w0[j], Y[b].x, r[j][0]);
+                r[j][1] = fmaf(w0[j], Y[b].y, r[j][1]);
+                r[j][2] = fmaf(w1[j], Y[b].x, r[j][2]);
+            }
         }
-        v = fmaf(r0, X[a].x, v);
-        dx = fmaf(r0, X[a].y, dx);
-        dy = fmaf(r1, X[a].x, dy);
-        dz = fmaf(r2, X[a].x, dz);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            o[j][0] = fmaf(r[j][0], X[a].x, o[j][0]);
+            o[j][1] = fmaf(r[j][0], X[a].y, o[j][1]);
+            o[j][2] = fmaf(r[j][1], X[a].x, o[j][2]);
+            o[j][3] = fmaf(r[j][2], X[a].x, o[j][3]);
+        }
     }
 }
 
 // The transpose: acc_abc += X'_a Y_b Z_c gx + X_a Y'_b Z_c gy + X_a Y_b Z'_c gz
-// + X_a Y_b Z_c s, factored the same way.
+// + X_a Y_b Z_c s, factored the same way (one (a, b) factor pair live at a time).
 template <int PD>
 __device__ __forceinline__ void test_sf(float* acc, const float2* X, const float2* Y, const float2* Z, float gx, float gy,
                                         float gz, float s) {
-    constexpr Blist<PD> BL{};
-    constexpr int NP = Deg<PD>::NP;
-    float q0[PD + 1][PD + 1], q1[PD + 1][PD + 1];
+    constexpr Bidx<PD> BI{};
 #pragma unroll
     for (int a = 0; a <= PD; ++a) {
         const float t0 = fmaf(X[a].y, gx, X[a].x * s), t1 = X[a].x * gy, t2 = X[a].x * gz;
 #pragma unroll
         for (int b = 0; b <= PD - a; ++b) {
-            q0[a][b] = fmaf(Y[b].x, t0, Y[b].y * t1);
-            q1[a][b] = Y[b].x * t2;
-        }
-    }
+            const float q0 = fmaf(Y[b].x, t0, Y[b].y * t1), q1 = Y[b].x * t2;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) {
-        const int a = BL.d[i][0], b = BL.d[i][1], c = BL.d[i][2];
-        acc[i] = fmaf(Z[c].x, q0[a][b], fmaf(Z[c].y, q1[a][b], acc[i]));
+            for (int c = 0; c <= PD - a - b; ++c) {
+                float& r = acc[BI.i[a][b][c]];
+                r = fmaf(Z[c].x, q0, fmaf(Z[c].y, q1, r));
+            }
+        }
     }
 }
 
@@ -224,7 +244,7 @@ __device__ __forceinline__ void prefetch_l2(const void* base, int64_t total, con
 template <int PD> struct MfSmem {
     using S = MfShape<PD>;
     struct Loop {
-        float2 leg[S::NPT][3][S::L];   // P's (L, L') per point, direction, degree
+        float2 leg[S::NPT][S::LEGW];   // P's (L, L') per point: direction-major, then degree
         float4 flux[S::NPT][3];        // (G_i0, G_i1, G_i2, s_i) per point, scaled by P's map
     };
     union Work {
@@ -334,14 +354,16 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
             // Q's map: phi = sc L L L, d_k phi = sc ih_k (...)
             const float sq = pq.sc, gx = sq * pq.ih[0], gy = sq * pq.ih[1], gz = sq * pq.ih[2];
             float v[3], D[3][3];
+            {
+                float o[3][4];
+                eval_sf3<PD>(s_uQ[b][t], X, Y, Z, o);
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                float vj, dx, dy, dz;
-                eval_sf<PD>(&s_uQ[b][t][0].x + j, X, Y, Z, vj, dx, dy, dz);
-                v[j] = vj * sq;
-                D[j][0] = dx * gx;
-                D[j][1] = dy * gy;
-                D[j][2] = dz * gz;
+                for (int j = 0; j < 3; ++j) {
+                    v[j] = o[j][0] * sq;
+                    D[j][0] = o[j][1] * gx;
+                    D[j][1] = o[j][2] * gy;
+                    D[j][2] = o[j][3] * gz;
+                }
             }
             const float* n = T.n;
             const float nv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
@@ -366,23 +388,24 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
                 const float s = -W * (T.sigma * Tv + 0.5f * h);
                 s_w.loop.flux[tid][i] = make_float4(G[0] * hx, G[1] * hy, G[2] * hz, s * sP);
             }
-            legendre<PD>(xp[0] * pP.ih[0], s_w.loop.leg[tid][0]);
-            legendre<PD>(xp[1] * pP.ih[1], s_w.loop.leg[tid][1]);
-            legendre<PD>(xp[2] * pP.ih[2], s_w.loop.leg[tid][2]);
+            legendre<PD>(xp[0] * pP.ih[0], &s_w.loop.leg[tid][0]);
+            legendre<PD>(xp[1] * pP.ih[1], &s_w.loop.leg[tid][L]);
+            legendre<PD>(xp[2] * pP.ih[2], &s_w.loop.leg[tid][2 * L]);
         }
         __syncthreads();
         // ---- test against P's basis: thread (slot, component) over the chunk's points ----
         if (tact) {
             for (int pt = slot; pt < nt * NQ2; pt += MF_SLOTS) {
-                float2 X[L], Y[L], Z[L];
+                float2 LG[2 * ((3 * L + 1) / 2)];
+                const float4* lp = reinterpret_cast<const float4*>(s_w.loop.leg[pt]);
 #pragma unroll
-                for (int l = 0; l < L; ++l) {
-                    X[l] = s_w.loop.leg[pt][0][l];
-                    Y[l] = s_w.loop.leg[pt][1][l];
-                    Z[l] = s_w.loop.leg[pt][2][l];
+                for (int k = 0; k < (3 * L + 1) / 2; ++k) {
+                    const float4 q = lp[k];
+                    LG[2 * k] = make_float2(q.x, q.y);
+                    LG[2 * k + 1] = make_float2(q.z, q.w);
                 }
                 const float4 f = s_w.loop.flux[pt][ci];
-                test_sf<PD>(acc, X, Y, Z, f.x, f.y, f.z, f.w);
+                test_sf<PD>(acc, LG, LG + L, LG + 2 * L, f.x, f.y, f.z, f.w);
             }
         }
     }
@@ -415,8 +438,13 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     finish_poly<PD, MODE>(sa, P, y, s_b);
 }
 
+// CTAs per SM that the register budget is sized for, per degree (index p;
+// measured on the 46,767-polyhedron mesh: more CTAs per SM pay while the
+// registers still hold the test sums without spilling).
+constexpr int MF_MINB[5] = {5, 9, 8, 7, 5};
+
 template <int PD, int MODE>
-__global__ void __launch_bounds__(MF_THREADS, 5) k_mf(const __grid_constant__ MfArgs A) {
+__global__ void __launch_bounds__(MF_THREADS, MF_MINB[PD]) k_mf(const __grid_constant__ MfArgs A) {
     __shared__ __align__(16) char smem[sizeof(MfSmem<PD>)];
     mf_poly<PD, MODE>(A, A.s, blockIdx.x, smem);
 }
@@ -430,17 +458,16 @@ struct MfBatchProblem {
     int p;
 };
 
-constexpr size_t smax2(size_t x, size_t y) { return x > y ? x : y; }
-constexpr size_t MF_SMEM_MAX =
-    smax2(smax2(sizeof(MfSmem<1>), sizeof(MfSmem<2>)), smax2(sizeof(MfSmem<3>), sizeof(MfSmem<4>)));
-
-// Persistent CTAs pull (problem, polyhedron) items from an atomic queue and
-// run mf_poly with the item's degree: the same per-polyhedron pass as k_mf,
-// so results equal stepping each problem alone.
-__global__ void __launch_bounds__(MF_THREADS, 5)
+// Persistent CTAs pull (problem, polyhedron) items of degree PD from an
+// atomic queue and run mf_poly on each: the same per-polyhedron pass as k_mf,
+// so results equal stepping each problem alone.  One launch per degree
+// present, so each degree runs with its own register and shared-memory
+// budget (the CTAs per SM of k_mf).
+template <int PD>
+__global__ void __launch_bounds__(MF_THREADS, MF_MINB[PD])
 k_mf_batch(const MfBatchProblem* __restrict__ probs, const int2* __restrict__ items, int n_items, int* queue,
            const int64_t* step_idx, const double* gvals, int64_t g_stride) {
-    __shared__ __align__(16) char smem[MF_SMEM_MAX];
+    __shared__ __align__(16) char smem[sizeof(MfSmem<PD>)];
     __shared__ int s_item;
     const int64_t k = *step_idx;
     for (;;) {
@@ -458,12 +485,7 @@ k_mf_batch(const MfBatchProblem* __restrict__ probs, const int2* __restrict__ it
         s.out = pb.buf[cur ^ 1];
         s.gvals = gvals + (int64_t)w.x * g_stride;
         s.step_idx = step_idx;
-        switch (pb.p) {
-            case 1: mf_poly<1, MODE_STEP>(pb.a, s, w.y, smem); break;
-            case 2: mf_poly<2, MODE_STEP>(pb.a, s, w.y, smem); break;
-            case 3: mf_poly<3, MODE_STEP>(pb.a, s, w.y, smem); break;
-            default: mf_poly<4, MODE_STEP>(pb.a, s, w.y, smem); break;
-        }
+        mf_poly<PD, MODE_STEP>(pb.a, s, w.y, smem);
     }
 }
 
@@ -652,6 +674,20 @@ int lymph_dev_mf(lymph_ctx* c, int mode, const stepk::StepArgs& s) {
 
 size_t lymph_mf_batch_problem_bytes() { return sizeof(MfBatchProblem); }
 
+// CTAs of k_mf_batch<p> one SM holds (registers and shared memory).
+int lymph_mf_batch_ctas_per_sm(int p) {
+    int n = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (p) {
+        case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mf_batch<1>, MF_THREADS, 0); break;
+        case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mf_batch<2>, MF_THREADS, 0); break;
+        case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mf_batch<3>, MF_THREADS, 0); break;
+        case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_mf_batch<4>, MF_THREADS, 0); break;
+        default: return 1;
+    }
+    return (e == cudaSuccess && n >= 1) ? n : 1;
+}
+
 // One problem's record for k_mf_batch; status: the batch's status word.
 void lymph_mf_batch_problem(const lymph_ctx* c, int* status, void* out) {
     StepArgs s;
@@ -678,13 +714,34 @@ void lymph_mf_batch_problem(const lymph_ctx* c, int* status, void* out) {
     std::memcpy(out, &pb, sizeof(pb));
 }
 
-// One batched leapfrog step: the FP32 copies of every problem's u^n, then the
-// persistent pass over all items (the caller advances the step counter).
-int lymph_mf_batch_step(cudaStream_t st, int grid, const void* probs, const int2* items, int n_items, int* queue,
-                        const int64_t* step_idx, const double* gvals, int64_t g_stride) {
+// One batched leapfrog step: the FP32 copies of every problem's u^n, then one
+// persistent pass per degree over that degree's items, items[off[p - 1],
+// off[p]) with grid[p - 1] CTAs and queue counter queue[p - 1] (the caller
+// advances the step counter and clears the counters).  Returns the number of
+// kernels launched in *launched.
+int lymph_mf_batch_step(cudaStream_t st, const int* grid, const void* probs, const int2* items, const int* off,
+                        int* queue, const int64_t* step_idx, const double* gvals, int64_t g_stride, int* launched) {
     const MfBatchProblem* pb = (const MfBatchProblem*)probs;
-    k_mf_u32_batch<<<(unsigned)((n_items + 3) / 4), 128, 0, st>>>(pb, items, n_items, step_idx);
-    k_mf_batch<<<grid, MF_THREADS, 0, st>>>(pb, items, n_items, queue, step_idx, gvals, g_stride);
+    const int n_all = off[4];
+    int nl = 0;
+    if (n_all > 0) {
+        k_mf_u32_batch<<<(unsigned)((n_all + 3) / 4), 128, 0, st>>>(pb, items, n_all, step_idx);
+        ++nl;
+    }
+    for (int p = 1; p <= 4; ++p) {
+        const int n = off[p] - off[p - 1];
+        if (n <= 0 || grid[p - 1] <= 0) continue;
+        const int2* it = items + off[p - 1];
+        int* q = queue + (p - 1);
+        switch (p) {
+            case 1: k_mf_batch<1><<<grid[0], MF_THREADS, 0, st>>>(pb, it, n, q, step_idx, gvals, g_stride); break;
+            case 2: k_mf_batch<2><<<grid[1], MF_THREADS, 0, st>>>(pb, it, n, q, step_idx, gvals, g_stride); break;
+            case 3: k_mf_batch<3><<<grid[2], MF_THREADS, 0, st>>>(pb, it, n, q, step_idx, gvals, g_stride); break;
+            default: k_mf_batch<4><<<grid[3], MF_THREADS, 0, st>>>(pb, it, n, q, step_idx, gvals, g_stride); break;
+        }
+        ++nl;
+    }
+    if (launched) *launched = nl;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
 }

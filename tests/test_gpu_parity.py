@@ -23,7 +23,8 @@ Bars (written in each assertion):
   * graph-launched loop vs step-by-step calls, and two runs: bit-identical.
 Meshes are generated (structured cubes, optionally jittered, agglomerated
 one-tet-per-polyhedron, per hexahedron, or by seeded BFS groups) at sizes the
-oracle finishes in seconds.
+oracle finishes in seconds; the smallest is one polyhedron with no neighbour
+at all (every face on the boundary, Dirichlet and Neumann).
 """
 import math
 
@@ -42,6 +43,8 @@ TOL_ERR = 1e-10
 
 
 def _mesh(kind):
+    if kind == "one_poly":  # the whole cube one polyhedron of 6 tets: no neighbour blocks
+        return M.cube(1, bc="reference", agglomeration="hex", material=(1.0, 2.0, 1.0))
     if kind == "tet_dir":
         return M.cube(2, bc="dirichlet", agglomeration="tet")
     if kind == "tet_ref_jitter":
@@ -57,7 +60,7 @@ def _mesh(kind):
     raise KeyError(kind)
 
 
-KINDS = ["tet_dir", "tet_ref_jitter", "hex_dir", "bfs_ref_jitter", "bfs_lognormal"]
+KINDS = ["one_poly", "tet_dir", "tet_ref_jitter", "hex_dir", "bfs_ref_jitter", "bfs_lognormal"]
 
 
 def rel(a, b):
