@@ -232,9 +232,9 @@ __device__ __forceinline__ void prefetch_l2(const void* base, int64_t total, con
 // and the state rows), so those reads do not wait on HBM.  Neighbour
 // triangles, CT triangles at a time, their geometry, Q's box and Q's FP32
 // coefficients copied into shared memory with cp.async one chunk ahead
-// (double-buffered): thread t evaluates point t -- Q's field and gradient
-// component by component by sum factorisation, the three flux rows, and P's
-// Legendre values, kept in shared memory; then thread 3 k + i accumulates
+// (double-buffered): thread t evaluates point t -- Q's field and gradient,
+// the three components together by sum factorisation, the three flux rows,
+// and P's Legendre values, kept in shared memory; then thread 3 k + i accumulates
 // row component i of P's test sums over the points k, k + 42, ... of the
 // chunk in Np registers (the sum-factorised transpose).  Then the self-block
 // rows (thread r < ND, K_PP streamed from L2) and the 42 slots' partial rows,
@@ -388,9 +388,17 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
                 const float s = -W * (T.sigma * Tv + 0.5f * h);
                 s_w.loop.flux[tid][i] = make_float4(G[0] * hx, G[1] * hy, G[2] * hz, s * sP);
             }
-            legendre<PD>(xp[0] * pP.ih[0], &s_w.loop.leg[tid][0]);
-            legendre<PD>(xp[1] * pP.ih[1], &s_w.loop.leg[tid][L]);
-            legendre<PD>(xp[2] * pP.ih[2], &s_w.loop.leg[tid][2 * L]);
+            // P's values, written as 16-byte words (the padded row keeps the
+            // stores of a quarter-warp on distinct banks)
+            constexpr int LW = (3 * L + 1) / 2;
+            float2 LP[2 * LW];
+            legendre<PD>(xp[0] * pP.ih[0], LP);
+            legendre<PD>(xp[1] * pP.ih[1], LP + L);
+            legendre<PD>(xp[2] * pP.ih[2], LP + 2 * L);
+            if (2 * LW > 3 * L) LP[2 * LW - 1] = make_float2(0.0f, 0.0f);
+            float4* lw = reinterpret_cast<float4*>(s_w.loop.leg[tid]);
+#pragma unroll
+            for (int k = 0; k < LW; ++k) lw[k] = make_float4(LP[2 * k].x, LP[2 * k].y, LP[2 * k + 1].x, LP[2 * k + 1].y);
         }
         __syncthreads();
         // ---- test against P's basis: thread (slot, component) over the chunk's points ----
@@ -410,22 +418,23 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
         }
     }
     cp_async_wait<0>();
-    // ---- self block (FP32, from L2) ----
+    __syncthreads();  // the loop buffers are free: reuse them for the slots' rows
+    if (tact) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i) s_w.red[slot][ci * NP + i] = acc[i];
+    }
+    // ---- self block (FP32, from L2; the test sums are parked, so the
+    // registers go to loads in flight) ----
     float yself = 0.0f;
     if (tid < ND) {
         const float* Kb = A.Kself + (int64_t)P * ND * ND + tid;
         float a0 = 0.0f, a1 = 0.0f;
-#pragma unroll 8
+#pragma unroll
         for (int c = 0; c < ND; c += 2) {
             a0 = fmaf(__ldcs(Kb + (int64_t)c * ND), s_uP[c], a0);
             if (c + 1 < ND) a1 = fmaf(__ldcs(Kb + (int64_t)(c + 1) * ND), s_uP[c + 1], a1);
         }
         yself = a0 + a1;
-    }
-    __syncthreads();  // the loop buffers are free: reuse them for the slots' rows
-    if (tact) {
-#pragma unroll
-        for (int i = 0; i < NP; ++i) s_w.red[slot][ci * NP + i] = acc[i];
     }
     __syncthreads();
     double y = 0.0;
