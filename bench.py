@@ -337,21 +337,25 @@ def pinned_array(n):
 
 
 def run_e2e(g, t, steps):
-    """K steps through the reference-facing C ABI with host buffers."""
+    """K steps through the reference-facing C ABI with host buffers in the
+    reference's u(ie, k) layout (TIME_STEP_MATRIX_FREE's u0_loc, un_loc in,
+    usol_loc out)."""
     from lymph3d_apsc_gb300 import _lib
     nv = g.n_poly * g.nd
     u0, p0 = pinned_array(nv)
     un, _ = pinned_array(nv)
-    u0[:] = g.get_state(_lib.SLOT_U0).ravel()
-    un[:] = g.get_state(_lib.SLOT_UN).ravel()
+    fort = _lib.LAYOUT_FORTRAN
+    u0[:] = g.get_state(_lib.SLOT_U0, fort).ravel()
+    un[:] = g.get_state(_lib.SLOT_UN, fort).ravel()
+    P = _lib.P_F64
     t0 = time.perf_counter()
     for _ in range(steps):
-        g.set_state(_lib.SLOT_U0, u0)
-        g.set_state(_lib.SLOT_UN, un)
+        _lib.check(g.lib.lymph_set_state(g.ctx, _lib.SLOT_U0, u0.ctypes.data_as(P), fort), "set_state")
+        _lib.check(g.lib.lymph_set_state(g.ctx, _lib.SLOT_UN, un.ctypes.data_as(P), fort), "set_state")
         g.TIME_STEP_MATRIX_FREE(t)
         t += g.dt
         u0, un = un, u0
-        g.lib.lymph_get_state(g.ctx, _lib.SLOT_UN, un.ctypes.data_as(_lib.P_F64), _lib.LAYOUT_POLY_MAJOR)
+        _lib.check(g.lib.lymph_get_state(g.ctx, _lib.SLOT_UN, un.ctypes.data_as(P), fort), "get_state")
     el = time.perf_counter() - t0
     return {"value": g.n_poly * g.nd * steps / el, "seconds": el, "pinned": p0, "t": t,
             "h2d_bytes_per_step": 2 * nv * 8, "d2h_bytes_per_step": nv * 8}
@@ -701,7 +705,7 @@ def main():
         e = r["e2e"]
         line["e2e"] = {"value": info["sum"](e["value"]), "unit": "DOF-steps/s",
                        "h2d_bytes_per_step": e["h2d_bytes_per_step"], "d2h_bytes_per_step": e["d2h_bytes_per_step"],
-                       "pinned_host": e["pinned"]}
+                       "pinned_host": e["pinned"], "host_layout": "reference u(ie, k), column-major"}
     if info["rank"] == 0 and not args.no_cpu_baseline:
         cb = cpu_sample(cfg)
         line["cpu_baseline"] = {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",

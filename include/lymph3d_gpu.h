@@ -205,7 +205,11 @@ int lymph_run_steps(lymph_ctx* ctx, double stop_time, int64_t max_steps, double*
 /* Device-to-device copy between two state slots. */
 int lymph_copy_state(lymph_ctx* ctx, int dst_slot, int src_slot);
 
-/* Copies a state slot to / from host memory in the given layout. */
+/* Copies a state slot to / from host memory in the given layout
+ * (synchronous on return).  LYMPH_LAYOUT_FORTRAN is transposed on the device
+ * (a staging buffer of the state's size is allocated on the first such call),
+ * so both layouts move as one direct copy; a page-locked host buffer moves
+ * by DMA. */
 int lymph_get_state(lymph_ctx* ctx, int slot, double* host, int layout);
 int lymph_set_state(lymph_ctx* ctx, int slot, const double* host, int layout);
 

@@ -149,6 +149,40 @@ int set_g(lymph_ctx* c, double g) {
 
 bool valid_slot(int s) { return s >= 0 && s < LYMPH_NUM_SLOTS; }
 
+// dst = src^T for a row-major rows x cols src (32 x 32 tiles through
+// shared memory, so both sides are read and written in full lines).  The
+// state's two layouts: [n_poly][3Np] on the device, the reference's u(ie, k)
+// (column-major, element index fastest) = [3Np][n_poly] row-major on the host.
+__global__ void k_transpose(const double* __restrict__ src, double* __restrict__ dst, int64_t rows, int64_t cols) {
+    __shared__ double tile[32][33];
+    const int64_t tiles_r = (rows + 31) / 32;   // one CTA per 32 x 32 tile, row tiles fastest
+    const int64_t r0 = (int64_t)(blockIdx.x % tiles_r) * 32, c0 = (int64_t)(blockIdx.x / tiles_r) * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int j = ty; j < 32; j += 8) {
+        const int64_t r = r0 + j, col = c0 + tx;
+        if (r < rows && col < cols) tile[j][tx] = src[r * cols + col];
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int64_t col = c0 + j, r = r0 + tx;
+        if (col < cols && r < rows) dst[col * rows + r] = tile[tx][j];
+    }
+}
+
+int transpose(lymph_ctx* c, const double* src, double* dst, int64_t rows, int64_t cols) {
+    const int64_t tiles = ((rows + 31) / 32) * ((cols + 31) / 32);
+    if (tiles <= 0) return LYMPH_OK;
+    k_transpose<<<(unsigned)tiles, dim3(32, 8), 0, c->stream>>>(src, dst, rows, cols);
+    c->launches++;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+int layout_buffer(lymph_ctx* c) {
+    if (!c->d_layout) LYMPH_TRY(dalloc(c, &c->d_layout, (size_t)c->n_poly * c->nd));
+    return LYMPH_OK;
+}
+
 }  // namespace
 
 void lymph_set_error(const std::string& msg) { g_last_error = msg; }
@@ -194,7 +228,7 @@ int lymph_destroy(lymph_ctx* c) {
                     c->d_poly_tets, c->d_row_ptr, c->d_col, c->d_blk_row, c->d_bf_ptr, c->d_bf, c->d_K, c->d_K32, c->d_M,
                     c->d_Mm, c->d_R, c->d_Rm, c->d_RT, c->d_RmT, c->d_Minv, c->d_rhs_stat, c->d_rhs_dyn, c->d_buf[0], c->d_buf[1],
                     c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status,
-                    c->d_mf_tri, c->d_mf_poly, c->d_mf_u32};
+                    c->d_mf_tri, c->d_mf_poly, c->d_mf_u32, c->d_layout};
     for (void* p : ptrs) dfree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -598,32 +632,30 @@ int lymph_run_steps(lymph_ctx* c, double stop_time, int64_t max_steps, double* t
 int lymph_get_state(lymph_ctx* c, int slot, double* host, int layout) {
     if (!c || !host || !valid_slot(slot)) return LYMPH_ERR_INVALID;
     size_t nv = (size_t)c->n_poly * c->nd;
-    if (layout != LYMPH_LAYOUT_FORTRAN) {
-        // direct copy: a page-locked caller buffer moves by DMA
-        LYMPH_CUDA_TRY(cudaMemcpyAsync(host, lymph_slot_ptr(c, slot), nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-        LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
-        return LYMPH_OK;
+    const double* src = lymph_slot_ptr(c, slot);
+    if (layout == LYMPH_LAYOUT_FORTRAN) {
+        // transposed on the device, then one direct copy
+        LYMPH_TRY(layout_buffer(c));
+        LYMPH_TRY(transpose(c, src, c->d_layout, c->n_poly, c->nd));
+        src = c->d_layout;
     }
-    std::vector<double> tmp(nv);
-    LYMPH_CUDA_TRY(cudaMemcpyAsync(tmp.data(), lymph_slot_ptr(c, slot), nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    // a page-locked caller buffer moves by DMA
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(host, src, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
-    for (int P = 0; P < c->n_poly; ++P)
-        for (int k = 0; k < c->nd; ++k) host[(size_t)k * c->n_poly + P] = tmp[(size_t)P * c->nd + k];
     return LYMPH_OK;
 }
 
 int lymph_set_state(lymph_ctx* c, int slot, const double* host, int layout) {
     if (!c || !host || !valid_slot(slot)) return LYMPH_ERR_INVALID;
     size_t nv = (size_t)c->n_poly * c->nd;
+    double* dst = lymph_slot_ptr(c, slot);
     if (layout != LYMPH_LAYOUT_FORTRAN) {
-        LYMPH_CUDA_TRY(cudaMemcpyAsync(lymph_slot_ptr(c, slot), host, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
-        return LYMPH_OK;
+        LYMPH_CUDA_TRY(cudaMemcpyAsync(dst, host, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    } else {
+        LYMPH_TRY(layout_buffer(c));
+        LYMPH_CUDA_TRY(cudaMemcpyAsync(c->d_layout, host, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        LYMPH_TRY(transpose(c, c->d_layout, dst, c->nd, c->n_poly));
     }
-    std::vector<double> tmp(nv);
-    for (int P = 0; P < c->n_poly; ++P)
-        for (int k = 0; k < c->nd; ++k) tmp[(size_t)P * c->nd + k] = host[(size_t)k * c->n_poly + P];
-    LYMPH_CUDA_TRY(cudaMemcpyAsync(lymph_slot_ptr(c, slot), tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return LYMPH_OK;
 }

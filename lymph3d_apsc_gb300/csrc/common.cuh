@@ -109,6 +109,7 @@ struct lymph_ctx {
     int64_t* d_step_idx = nullptr;
     double* d_partial = nullptr;    // per-polyhedron partial sums (error norms)
     double* d_scalar = nullptr;
+    double* d_layout = nullptr;     // staging of a state in the reference's (ie, k) layout (allocated on first use)
     int* d_status = nullptr;
     bool have_matrices = false, have_rhs_stat = false, have_rhs_dyn = false;
     int64_t launches = 0;
