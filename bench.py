@@ -271,11 +271,14 @@ def mf_triangles(g):
 
 def mf_flops(g):
     """FP32 FLOPs of one matrix-free neighbour apply: per quadrature point of
-    every triangle side, the field and gradient of Q (12 Np FMA), the test
-    against P's basis (12 Np FMA) and the two bases' tensor products (2 x 7 Np
-    multiplies), plus the self block's 2 (3Np)^2."""
-    nq2 = (g.degree + 1) ** 2
-    return mf_triangles(g) * nq2 * 62.0 * g.Np + 2.0 * g.n_poly * g.nd * g.nd
+    every triangle side (the path's triangle rule, lymph_mf_face_rule), the
+    field and gradient of Q (12 Np FMA), the test against P's basis (12 Np
+    FMA) and the two bases' tensor products (2 x 7 Np multiplies), plus the
+    self block's 2 (3Np)^2."""
+    from ctypes import byref, c_int32
+    nq = c_int32()
+    g.lib.lymph_mf_face_rule(g.degree, byref(nq), None)
+    return mf_triangles(g) * nq.value * 62.0 * g.Np + 2.0 * g.n_poly * g.nd * g.nd
 
 
 def step_flops(g):

@@ -389,6 +389,14 @@ int lymph_get_dt(const lymph_ctx* ctx, double* dt);
  * tests dt against hmax. */
 int lymph_max_eigenvalue(lymph_ctx* ctx, int32_t iters, double* lam);
 
+/* The triangle rule of the LYMPH_MIXED_MF neighbour terms for degree p
+ * (1..4): *n nodes; if xyw is not null it receives (xi, eta, w) per node on
+ * the reference triangle (0,0), (1,0), (0,1), weights summing to 1/2.  Exact
+ * to degree 2p, the degree of the face integrands, like the reference's
+ * collapsed Gauss rule (mapping_quadrature_2D, Poly_ref_mappings.f90:137-186),
+ * with fewer nodes.  Needs no device. */
+int lymph_mf_face_rule(int32_t p, int32_t* n, double* xyw);
+
 /* ---- many problems in one persistent launch per step -------------------
  * No counterpart in the reference (one problem per MPI job).  A batch
  * references n assembled contexts (same precision; any degrees, meshes and

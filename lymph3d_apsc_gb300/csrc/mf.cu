@@ -60,13 +60,77 @@ struct MfPoly {         // Legendre scaling of a bounding box: xp = (x - centre)
 };
 static_assert(sizeof(MfPoly) == 16, "MfPoly is one 16-byte copy");
 
+// The triangle rule of the neighbour terms.  The integrand of every term of
+// K_PQ u_Q on a triangle is a polynomial of total degree <= 2p in the
+// triangle's parameters (xi, eta): phi^P and u_Q are degree-p polynomials
+// composed with affine maps, and the material is constant per tetrahedron.
+// The reference's collapsed Gauss rule with (p+1)^2 points
+// (mapping_quadrature_2D, Poly_ref_mappings.f90:137-186) is exact to that
+// degree, and so is each rule below, with fewer points: 3 / 6 / 12 / 16 for
+// p = 1..4 against 4 / 9 / 16 / 25.  Both give the same integrals in exact
+// arithmetic.  These are fully symmetric rules with interior nodes and
+// positive weights on the reference triangle (0,0), (1,0), (0,1), weights
+// summing to 1/2 like the reference's.  Each orbit of the symmetry group
+// (the centroid; (a, a, 1-2a) in barycentric coordinates, 3 points; (a, b,
+// 1-a-b), 6 points) has one weight.  The nodes and weights solve the moment
+// equations sum_q w_q xi^i eta^j = i! j! / (i+j+2)! for i + j <= 2p
+// (derive_face_rules.py beside this file solves them to 40 digits;
+// tests/test_abi_cpu.py checks every moment of the values below).
+constexpr int MF_FACE_NQ[5] = {0, 3, 6, 12, 16};
+constexpr int MF_FACE_NQ_MAX = 16;
+// (xi, eta, w) per node, degrees 1..4 one after another
+constexpr double kFaceRule[3 * (3 + 6 + 12 + 16)] = {
+    // p = 1, exact to degree 2
+    0.16666666666666666667, 0.16666666666666666667, 0.16666666666666666667,
+    0.16666666666666666667, 0.66666666666666666667, 0.16666666666666666667,
+    0.66666666666666666667, 0.16666666666666666667, 0.16666666666666666667,
+    // p = 2, exact to degree 4
+    0.09157621350977074346, 0.09157621350977074346, 0.054975871827660933819,
+    0.09157621350977074346, 0.81684757298045851308, 0.054975871827660933819,
+    0.81684757298045851308, 0.09157621350977074346, 0.054975871827660933819,
+    0.44594849091596488632, 0.44594849091596488632, 0.11169079483900573285,
+    0.44594849091596488632, 0.10810301816807022736, 0.11169079483900573285,
+    0.10810301816807022736, 0.44594849091596488632, 0.11169079483900573285,
+    // p = 3, exact to degree 6
+    0.24928674517091042129, 0.24928674517091042129, 0.058393137863189683013,
+    0.24928674517091042129, 0.50142650965817915742, 0.058393137863189683013,
+    0.50142650965817915742, 0.24928674517091042129, 0.058393137863189683013,
+    0.06308901449150222834, 0.06308901449150222834, 0.02542245318510340846,
+    0.06308901449150222834, 0.87382197101699554332, 0.02542245318510340846,
+    0.87382197101699554332, 0.06308901449150222834, 0.02542245318510340846,
+    0.31035245103378440542, 0.053145049844816947353, 0.041425537809186787597,
+    0.053145049844816947353, 0.31035245103378440542, 0.041425537809186787597,
+    0.31035245103378440542, 0.63650249912139864723, 0.041425537809186787597,
+    0.63650249912139864723, 0.31035245103378440542, 0.041425537809186787597,
+    0.053145049844816947353, 0.63650249912139864723, 0.041425537809186787597,
+    0.63650249912139864723, 0.053145049844816947353, 0.041425537809186787597,
+    // p = 4, exact to degree 8
+    0.33333333333333333333, 0.33333333333333333333, 0.072157803838893584126,
+    0.45929258829272315603, 0.45929258829272315603, 0.047545817133642312397,
+    0.45929258829272315603, 0.081414823414553687942, 0.047545817133642312397,
+    0.081414823414553687942, 0.45929258829272315603, 0.047545817133642312397,
+    0.17056930775176020662, 0.17056930775176020662, 0.051608685267359125141,
+    0.17056930775176020662, 0.65886138449647958676, 0.051608685267359125141,
+    0.65886138449647958676, 0.17056930775176020662, 0.051608685267359125141,
+    0.050547228317030975458, 0.050547228317030975458, 0.016229248811599040155,
+    0.050547228317030975458, 0.89890554336593804908, 0.016229248811599040155,
+    0.89890554336593804908, 0.050547228317030975458, 0.016229248811599040155,
+    0.72849239295540428124, 0.26311282963463811342, 0.013615157087217497132,
+    0.26311282963463811342, 0.72849239295540428124, 0.013615157087217497132,
+    0.72849239295540428124, 0.0083947774099576053372, 0.013615157087217497132,
+    0.0083947774099576053372, 0.72849239295540428124, 0.013615157087217497132,
+    0.26311282963463811342, 0.0083947774099576053372, 0.013615157087217497132,
+    0.0083947774099576053372, 0.26311282963463811342, 0.013615157087217497132,
+};
+constexpr int face_rule_offset(int p) { return p <= 1 ? 0 : face_rule_offset(p - 1) + MF_FACE_NQ[p - 1]; }
+
 constexpr int MF_THREADS = 128;
 constexpr int MF_SLOTS = MF_THREADS / 3;   // test phase: point slots of three lanes (one per row component)
 
 template <int PD> struct MfShape {
     static constexpr int NP = Deg<PD>::NP, ND = Deg<PD>::ND;
     static constexpr int L = PD + 1;              // Legendre degrees per direction
-    static constexpr int NQ2 = L * L;             // quadrature points per triangle
+    static constexpr int NQ2 = MF_FACE_NQ[PD];    // quadrature points per triangle
     static constexpr int CT = MF_THREADS / NQ2;   // triangles per chunk
     static constexpr int NPT = CT * NQ2;          // points per chunk (one evaluating thread each)
     // a point's (L, L') values of the three directions, padded to an odd
@@ -204,7 +268,7 @@ struct MfArgs {
     const float4* u32;          // operator input in FP32: [n_poly][Np] (u_0, u_1, u_2, 0)
     int64_t kself_bytes;        // size of Kself
     int64_t minv_bytes;         // size of the M^-1 array
-    float quad[3 * 25];         // (xi, eta, w) of the triangle quadrature points
+    float quad[3 * MF_FACE_NQ_MAX];   // (xi, eta, w) of the triangle rule's nodes
     float theta;
 };
 
@@ -449,8 +513,9 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
 
 // CTAs per SM that the register budget is sized for, per degree (index p;
 // measured on the 46,767-polyhedron mesh: more CTAs per SM pay while the
-// registers still hold the test sums without spilling).
-constexpr int MF_MINB[5] = {5, 9, 8, 7, 5};
+// registers still hold the test sums without spilling; at p = 1 shared
+// memory holds 8).
+constexpr int MF_MINB[5] = {5, 8, 8, 7, 5};
 
 template <int PD, int MODE>
 __global__ void __launch_bounds__(MF_THREADS, MF_MINB[PD]) k_mf(const __grid_constant__ MfArgs A) {
@@ -602,7 +667,7 @@ MfArgs mf_args(const lymph_ctx* c, const StepArgs& s) {
     a.u32 = (const float4*)c->d_mf_u32;
     a.kself_bytes = (int64_t)c->n_poly * c->nd * c->nd * (int64_t)sizeof(float);
     a.minv_bytes = (int64_t)c->n_poly * c->Np * c->Np * (int64_t)sizeof(double);
-    for (int i = 0; i < 3 * 25; ++i) a.quad[i] = c->mf_quad[i];
+    for (int i = 0; i < 3 * MF_FACE_NQ_MAX; ++i) a.quad[i] = c->mf_quad[i];
     a.theta = (float)c->theta;
     return a;
 }
@@ -636,13 +701,12 @@ int launch_mf_p(lymph_ctx* c, int mode, const StepArgs& s) {
 // The per-triangle and per-polyhedron FP32 tables of the matrix-free
 // neighbour terms (after geometry and the block pattern exist).
 int lymph_mf_setup(lymph_ctx* c, const RefTables& R) {
-    const int nq2 = (c->p + 1) * (c->p + 1);
-    for (int q = 0; q < 25; ++q) {
-        const bool in = q < nq2;
-        c->mf_quad[3 * q + 0] = in ? (float)R.nodtria2[q * 4 + 0] : 0.0f;
-        c->mf_quad[3 * q + 1] = in ? (float)R.nodtria2[q * 4 + 1] : 0.0f;
-        c->mf_quad[3 * q + 2] = in ? (float)R.weitria2[q] : 0.0f;
-    }
+    (void)R;
+    if (c->p < 1 || c->p > 4) { lymph_set_error("matrix-free neighbour terms: degree not supported"); return LYMPH_ERR_INVALID; }
+    const int nq = MF_FACE_NQ[c->p];
+    const double* rule = kFaceRule + 3 * face_rule_offset(c->p);
+    for (int q = 0; q < MF_FACE_NQ_MAX; ++q)
+        for (int k = 0; k < 3; ++k) c->mf_quad[3 * q + k] = q < nq ? (float)rule[3 * q + k] : 0.0f;
     if (!c->d_mf_tri) {
         void* p = nullptr;
         LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(MfTri) * (size_t)(c->n_block_faces > 0 ? c->n_block_faces : 1)));
@@ -752,5 +816,13 @@ int lymph_mf_batch_step(cudaStream_t st, const int* grid, const void* probs, con
     }
     if (launched) *launched = nl;
     LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+extern "C" int lymph_mf_face_rule(int32_t p, int32_t* n, double* xyw) {
+    if (p < 1 || p > 4 || !n) return LYMPH_ERR_INVALID;
+    *n = MF_FACE_NQ[p];
+    if (xyw)
+        for (int i = 0; i < 3 * MF_FACE_NQ[p]; ++i) xyw[i] = kFaceRule[3 * face_rule_offset(p) + i];
     return LYMPH_OK;
 }

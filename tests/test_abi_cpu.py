@@ -155,3 +155,27 @@ def test_create_without_device_fails_loudly():
     with pytest.raises(_lib.LymphError):
         from lymph3d_apsc_gb300 import MatrixFree
         MatrixFree(m, 1, 1e-3)
+
+
+def test_matrix_free_face_rules_are_exact_to_degree_2p():
+    """The triangle rules of the matrix-free neighbour terms (no device
+    needed): interior nodes, positive weights summing to 1/2, and every
+    monomial xi^i eta^j with i + j <= 2p integrated to i! j! / (i+j+2)!
+    within 1e-15 -- the degree of the face integrands, to which the
+    reference's collapsed Gauss rule with (p+1)^2 nodes is also exact."""
+    from ctypes import POINTER, byref, c_double, c_int32
+    from math import factorial
+    lib = _lib.load()
+    for p in (1, 2, 3, 4):
+        n = c_int32()
+        assert lib.lymph_mf_face_rule(p, byref(n), None) == 0
+        assert n.value == {1: 3, 2: 6, 3: 12, 4: 16}[p] < (p + 1) ** 2
+        xyw = np.zeros(3 * n.value)
+        assert lib.lymph_mf_face_rule(p, byref(n), xyw.ctypes.data_as(POINTER(c_double))) == 0
+        xi, eta, w = xyw[0::3], xyw[1::3], xyw[2::3]
+        assert np.all(w > 0) and np.all(xi > 0) and np.all(eta > 0) and np.all(xi + eta < 1)
+        for i in range(2 * p + 1):
+            for j in range(2 * p + 1 - i):
+                exact = factorial(i) * factorial(j) / factorial(i + j + 2)
+                assert abs(np.sum(w * xi ** i * eta ** j) - exact) <= 1e-15, (p, i, j)
+    assert lib.lymph_mf_face_rule(5, byref(n), None) != 0
