@@ -516,6 +516,7 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
 // registers still hold the test sums without spilling; at p = 1 shared
 // memory holds 8).
 constexpr int MF_MINB[5] = {5, 8, 8, 7, 5};
+constexpr int MF_BATCH_MINB[5] = {5, 8, 8, 7, 5};   // the same for k_mf_batch<p>
 
 template <int PD, int MODE>
 __global__ void __launch_bounds__(MF_THREADS, MF_MINB[PD]) k_mf(const __grid_constant__ MfArgs A) {
@@ -538,7 +539,7 @@ struct MfBatchProblem {
 // present, so each degree runs with its own register and shared-memory
 // budget (the CTAs per SM of k_mf).
 template <int PD>
-__global__ void __launch_bounds__(MF_THREADS, MF_MINB[PD])
+__global__ void __launch_bounds__(MF_THREADS, MF_BATCH_MINB[PD])
 k_mf_batch(const MfBatchProblem* __restrict__ probs, const int2* __restrict__ items, int n_items, int* queue,
            const int64_t* step_idx, const double* gvals, int64_t g_stride) {
     __shared__ __align__(16) char smem[sizeof(MfSmem<PD>)];
