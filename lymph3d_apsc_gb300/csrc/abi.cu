@@ -228,7 +228,7 @@ int lymph_destroy(lymph_ctx* c) {
                     c->d_poly_tets, c->d_row_ptr, c->d_col, c->d_blk_row, c->d_bf_ptr, c->d_bf, c->d_K, c->d_K32, c->d_M,
                     c->d_Mm, c->d_R, c->d_Rm, c->d_RT, c->d_RmT, c->d_Minv, c->d_rhs_stat, c->d_rhs_dyn, c->d_buf[0], c->d_buf[1],
                     c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status,
-                    c->d_mf_tri, c->d_mf_poly, c->d_mf_u32, c->d_layout};
+                    c->d_mf_tri, c->d_mf_poly, c->d_mf_u32, c->d_mf_range, c->d_layout};
     for (void* p : ptrs) dfree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

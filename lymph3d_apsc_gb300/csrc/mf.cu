@@ -262,7 +262,7 @@ __device__ __forceinline__ void test_sf(float* acc, const float2* X, const float
 struct MfArgs {
     StepArgs s;                 // CSR pattern, M^-1, right-hand sides, state, status
     const float* Kself;         // [n_poly][ND * ND] column-major self blocks
-    const int64_t* bf_ptr;      // per block: its triangles in tri[]
+    const longlong2* range;     // per polyhedron: its neighbour triangles tri[x, y)
     const MfTri* tri;           // parallel to the block face lists
     const MfPoly* poly;         // [n_poly]
     const float4* u32;          // operator input in FP32: [n_poly][Np] (u_0, u_1, u_2, 0)
@@ -342,8 +342,8 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     int* s_Q = sm.Q;
     double* s_b = sm.b;
     const int tid = threadIdx.x;
-    const int rb = sa.row_ptr[P], re = sa.row_ptr[P + 1];
-    const int64_t fb = A.bf_ptr[rb + 1], fe = A.bf_ptr[re];
+    const longlong2 rg = A.range[P];  // one load (the row's block range would be two dependent ones)
+    const int64_t fb = rg.x, fe = rg.y;
     const int ntri = (int)(fe - fb);
 
     if (tid == 0) {
@@ -641,6 +641,16 @@ __global__ void k_mf_tris(int64_t n_blocks, const int32_t* __restrict__ blk_row,
     }
 }
 
+// range[P] = the neighbour triangles of row P: the blocks after the self
+// block (which comes first in every row), bf_ptr[row_ptr[P] + 1] to
+// bf_ptr[row_ptr[P + 1]].
+__global__ void k_mf_range(int n_poly, const int32_t* __restrict__ row_ptr, const int64_t* __restrict__ bf_ptr,
+                           longlong2* __restrict__ range) {
+    const int P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= n_poly) return;
+    range[P] = make_longlong2(bf_ptr[row_ptr[P] + 1], bf_ptr[row_ptr[P + 1]]);
+}
+
 __global__ void k_mf_polys(int n_poly, const double* __restrict__ bbox, MfPoly* out) {
     const int P = blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= n_poly) return;
@@ -662,7 +672,7 @@ MfArgs mf_args(const lymph_ctx* c, const StepArgs& s) {
     MfArgs a;
     a.s = s;
     a.Kself = (const float*)c->d_K;
-    a.bf_ptr = c->d_bf_ptr;
+    a.range = (const longlong2*)c->d_mf_range;
     a.tri = (const MfTri*)c->d_mf_tri;
     a.poly = (const MfPoly*)c->d_mf_poly;
     a.u32 = (const float4*)c->d_mf_u32;
@@ -719,6 +729,9 @@ int lymph_mf_setup(lymph_ctx* c, const RefTables& R) {
         LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(float4) * (size_t)c->n_poly * c->Np));
         c->d_mf_u32 = p;
         c->device_bytes += (int64_t)(sizeof(float4) * c->n_poly * c->Np);
+        LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(longlong2) * (size_t)c->n_poly));
+        c->d_mf_range = p;
+        c->device_bytes += (int64_t)(sizeof(longlong2) * c->n_poly);
     }
     if (c->n_blocks > 0) {
         k_mf_tris<<<(unsigned)((c->n_blocks + 127) / 128), 128, 0, c->stream>>>(
@@ -728,6 +741,9 @@ int lymph_mf_setup(lymph_ctx* c, const RefTables& R) {
         c->launches++;
     }
     k_mf_polys<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->d_bbox, (MfPoly*)c->d_mf_poly);
+    c->launches++;
+    k_mf_range<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->d_row_ptr, c->d_bf_ptr,
+                                                              (longlong2*)c->d_mf_range);
     c->launches++;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
