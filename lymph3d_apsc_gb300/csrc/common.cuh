@@ -97,7 +97,7 @@ struct lymph_ctx {
     void* d_mf_tri = nullptr;
     void* d_mf_poly = nullptr;
     void* d_mf_u32 = nullptr;       // the operator input in FP32, [n_poly][Np] x 4
-    void* d_mf_range = nullptr;     // per polyhedron its neighbour triangles' range in d_mf_tri
+    void* d_mf_range = nullptr;     // per polyhedron: its triangles' range and neighbours (mf.cu k_mf_qrec)
     float mf_quad[3 * 25] = {};
     double *d_rhs_stat = nullptr, *d_rhs_dyn = nullptr;
     // state: two rotating step buffers + V0 + UEX

@@ -262,7 +262,7 @@ __device__ __forceinline__ void test_sf(float* acc, const float2* X, const float
 struct MfArgs {
     StepArgs s;                 // CSR pattern, M^-1, right-hand sides, state, status
     const float* Kself;         // [n_poly][ND * ND] column-major self blocks
-    const longlong2* range;     // per polyhedron: its neighbour triangles tri[x, y)
+    const int32_t* qrec;        // per polyhedron MF_REC ints: triangle range and neighbours (k_mf_qrec)
     const MfTri* tri;           // parallel to the block face lists
     const MfPoly* poly;         // [n_poly]
     const float4* u32;          // operator input in FP32: [n_poly][Np] (u_0, u_1, u_2, 0)
@@ -272,7 +272,12 @@ struct MfArgs {
     float theta;
 };
 
-constexpr int MF_MAXT = 64;   // triangles whose neighbour index is kept in shared memory
+// One record of MF_REC ints per polyhedron, read in one coalesced load at the
+// start of its pass: [0, 1] the first triangle fb (int64, low word first),
+// [2] the number of triangles, [4, 4 + MF_MAXT) the neighbour polyhedron of
+// its first MF_MAXT triangles (the rest are read from the triangle records).
+constexpr int MF_REC = 64;
+constexpr int MF_MAXT = MF_REC - 4;   // triangles whose neighbour index is kept in shared memory
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
@@ -322,7 +327,7 @@ template <int PD> struct MfSmem {
     double b[S::ND];
     float quad[3 * S::NQ2];
     float uP[S::ND];
-    int Q[MF_MAXT];
+    int rec[MF_REC];
 };
 
 // The pass of polyhedron P (every thread of the CTA calls it; it
@@ -339,13 +344,11 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     auto& s_uQ = sm.uQ;
     float* s_quad = sm.quad;
     float* s_uP = sm.uP;
-    int* s_Q = sm.Q;
     double* s_b = sm.b;
     const int tid = threadIdx.x;
-    const longlong2 rg = A.range[P];  // one load (the row's block range would be two dependent ones)
-    const int64_t fb = rg.x, fe = rg.y;
-    const int ntri = (int)(fe - fb);
-
+    // the polyhedron's record (triangle range and neighbours) in one load,
+    // so the first chunk's staging waits on one global round trip, not three
+    if (tid < MF_REC) sm.rec[tid] = A.qrec[(int64_t)P * MF_REC + tid];
     if (tid == 0) {
         const int64_t nb = (int64_t)ND * ND * 4, vb = (int64_t)ND * 8;
         prefetch_l2(A.Kself, A.kself_bytes, A.Kself + (int64_t)P * ND * ND, nb);
@@ -364,11 +367,12 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
         const int comp = i / NP;
         s_uP[i] = comp == 0 ? w.x : (comp == 1 ? w.y : w.z);
     }
-    for (int i = tid; i < ntri && i < MF_MAXT; i += MF_THREADS) s_Q[i] = A.tri[fb + i].Q;
     __syncthreads();
+    const int64_t fb = (int64_t)(uint32_t)sm.rec[0] | ((int64_t)sm.rec[1] << 32);
+    const int ntri = sm.rec[2];
 
     // neighbour of triangle i of P (shared memory for the first MF_MAXT)
-    auto getQ = [&](int i) -> int { return i < MF_MAXT ? s_Q[i] : A.tri[fb + i].Q; };
+    auto getQ = [&](int i) -> int { return i < MF_MAXT ? sm.rec[4 + i] : A.tri[fb + i].Q; };
     auto stage = [&](int c, int b) {  // chunk starting at triangle c into buffer b
         const int nt = (ntri - c) < CT ? ntri - c : CT;
         const char* src = (const char*)(A.tri + fb + c);
@@ -641,14 +645,20 @@ __global__ void k_mf_tris(int64_t n_blocks, const int32_t* __restrict__ blk_row,
     }
 }
 
-// range[P] = the neighbour triangles of row P: the blocks after the self
-// block (which comes first in every row), bf_ptr[row_ptr[P] + 1] to
-// bf_ptr[row_ptr[P + 1]].
-__global__ void k_mf_range(int n_poly, const int32_t* __restrict__ row_ptr, const int64_t* __restrict__ bf_ptr,
-                           longlong2* __restrict__ range) {
+// The per-polyhedron records of mf_poly (MF_REC ints each): the neighbour
+// triangles of row P are the blocks after the self block (which comes first
+// in every row), bf_ptr[row_ptr[P] + 1] to bf_ptr[row_ptr[P + 1]].
+__global__ void k_mf_qrec(int n_poly, const int32_t* __restrict__ row_ptr, const int64_t* __restrict__ bf_ptr,
+                          const MfTri* __restrict__ tri, int32_t* __restrict__ rec) {
     const int P = blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= n_poly) return;
-    range[P] = make_longlong2(bf_ptr[row_ptr[P] + 1], bf_ptr[row_ptr[P + 1]]);
+    const int64_t fb = bf_ptr[row_ptr[P] + 1], fe = bf_ptr[row_ptr[P + 1]];
+    int32_t* r = rec + (int64_t)P * MF_REC;
+    r[0] = (int32_t)(uint32_t)((uint64_t)fb & 0xffffffffu);
+    r[1] = (int32_t)(fb >> 32);
+    r[2] = (int32_t)(fe - fb);
+    r[3] = 0;
+    for (int i = 0; i < MF_MAXT; ++i) r[4 + i] = i < fe - fb ? tri[fb + i].Q : -1;
 }
 
 __global__ void k_mf_polys(int n_poly, const double* __restrict__ bbox, MfPoly* out) {
@@ -672,7 +682,7 @@ MfArgs mf_args(const lymph_ctx* c, const StepArgs& s) {
     MfArgs a;
     a.s = s;
     a.Kself = (const float*)c->d_K;
-    a.range = (const longlong2*)c->d_mf_range;
+    a.qrec = (const int32_t*)c->d_mf_range;
     a.tri = (const MfTri*)c->d_mf_tri;
     a.poly = (const MfPoly*)c->d_mf_poly;
     a.u32 = (const float4*)c->d_mf_u32;
@@ -729,9 +739,9 @@ int lymph_mf_setup(lymph_ctx* c, const RefTables& R) {
         LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(float4) * (size_t)c->n_poly * c->Np));
         c->d_mf_u32 = p;
         c->device_bytes += (int64_t)(sizeof(float4) * c->n_poly * c->Np);
-        LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(longlong2) * (size_t)c->n_poly));
+        LYMPH_CUDA_TRY(cudaMalloc(&p, sizeof(int32_t) * MF_REC * (size_t)c->n_poly));
         c->d_mf_range = p;
-        c->device_bytes += (int64_t)(sizeof(longlong2) * c->n_poly);
+        c->device_bytes += (int64_t)(sizeof(int32_t) * MF_REC * c->n_poly);
     }
     if (c->n_blocks > 0) {
         k_mf_tris<<<(unsigned)((c->n_blocks + 127) / 128), 128, 0, c->stream>>>(
@@ -742,8 +752,8 @@ int lymph_mf_setup(lymph_ctx* c, const RefTables& R) {
     }
     k_mf_polys<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->d_bbox, (MfPoly*)c->d_mf_poly);
     c->launches++;
-    k_mf_range<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->d_row_ptr, c->d_bf_ptr,
-                                                              (longlong2*)c->d_mf_range);
+    k_mf_qrec<<<(c->n_poly + 127) / 128, 128, 0, c->stream>>>(c->n_poly, c->d_row_ptr, c->d_bf_ptr,
+                                                             (const MfTri*)c->d_mf_tri, (int32_t*)c->d_mf_range);
     c->launches++;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
