@@ -32,6 +32,7 @@
 // update).  A step reads the self blocks (1/nb of the operator bytes) and the
 // per-triangle geometry instead of every block.
 
+#include <cstddef>
 #include <cstring>
 
 #include "step_body.cuh"
@@ -322,13 +323,21 @@ template <int PD> struct MfSmem {
     };
     Work w;
     float4 uQ[2][S::CT][S::NP];        // (u_0, u_1, u_2, 0) per basis function
-    MfTri tri[2][S::CT];
-    MfPoly polyQ[2][S::CT];
+    alignas(16) MfTri tri[2][S::CT];
+    alignas(16) MfPoly polyQ[2][S::CT];
     double b[S::ND];
     float quad[3 * S::NQ2];
     float uP[S::ND];
     int rec[MF_REC];
 };
+// every cp.async destination starts on a 16-byte boundary (with the shared
+// array itself 16-byte aligned)
+template <int PD> constexpr bool mf_smem_aligned() {
+    return offsetof(MfSmem<PD>, uQ) % 16 == 0 && offsetof(MfSmem<PD>, tri) % 16 == 0 &&
+           offsetof(MfSmem<PD>, polyQ) % 16 == 0 && sizeof(MfTri) % 16 == 0 && sizeof(MfPoly) % 16 == 0;
+}
+static_assert(mf_smem_aligned<1>() && mf_smem_aligned<2>() && mf_smem_aligned<3>() && mf_smem_aligned<4>(),
+              "cp.async destinations must be 16-byte aligned");
 
 // The pass of polyhedron P (every thread of the CTA calls it; it
 // synchronises): the per-problem tables come from A, the state, right-hand
