@@ -341,24 +341,24 @@ def pinned_array(n):
 
 def run_e2e(g, t, steps):
     """K steps through the reference-facing C ABI with host buffers in the
-    reference's u(ie, k) layout (TIME_STEP_MATRIX_FREE's u0_loc, un_loc in,
-    usol_loc out)."""
+    reference's u(ie, k) layout: lymph_time_step_host, TIME_STEP_MATRIX_FREE's
+    argument list (u0_loc, un_loc in, usol_loc out), the driver's rotation
+    u0_loc = un_loc, un_loc = usol_loc between calls."""
     from lymph3d_apsc_gb300 import _lib
     nv = g.n_poly * g.nd
     u0, p0 = pinned_array(nv)
     un, _ = pinned_array(nv)
+    us, _ = pinned_array(nv)
     fort = _lib.LAYOUT_FORTRAN
     u0[:] = g.get_state(_lib.SLOT_U0, fort).ravel()
     un[:] = g.get_state(_lib.SLOT_UN, fort).ravel()
     P = _lib.P_F64
     t0 = time.perf_counter()
     for _ in range(steps):
-        _lib.check(g.lib.lymph_set_state(g.ctx, _lib.SLOT_U0, u0.ctypes.data_as(P), fort), "set_state")
-        _lib.check(g.lib.lymph_set_state(g.ctx, _lib.SLOT_UN, un.ctypes.data_as(P), fort), "set_state")
-        g.TIME_STEP_MATRIX_FREE(t)
+        _lib.check(g.lib.lymph_time_step_host(g.ctx, t, u0.ctypes.data_as(P), un.ctypes.data_as(P),
+                                              us.ctypes.data_as(P), fort), "lymph_time_step_host")
         t += g.dt
-        u0, un = un, u0
-        _lib.check(g.lib.lymph_get_state(g.ctx, _lib.SLOT_UN, un.ctypes.data_as(P), fort), "get_state")
+        u0, un, us = un, us, u0
     el = time.perf_counter() - t0
     return {"value": g.n_poly * g.nd * steps / el, "seconds": el, "pinned": p0, "t": t,
             "h2d_bytes_per_step": 2 * nv * 8, "d2h_bytes_per_step": nv * 8}
@@ -708,7 +708,8 @@ def main():
         e = r["e2e"]
         line["e2e"] = {"value": info["sum"](e["value"]), "unit": "DOF-steps/s",
                        "h2d_bytes_per_step": e["h2d_bytes_per_step"], "d2h_bytes_per_step": e["d2h_bytes_per_step"],
-                       "pinned_host": e["pinned"], "host_layout": "reference u(ie, k), column-major"}
+                       "pinned_host": e["pinned"], "host_layout": "reference u(ie, k), column-major",
+                       "call": "lymph_time_step_host"}
     if info["rank"] == 0 and not args.no_cpu_baseline:
         cb = cpu_sample(cfg)
         line["cpu_baseline"] = {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",

@@ -184,6 +184,15 @@ int lymph_first_step(lymph_ctx* ctx, double t);
  * receives through MPI_EXCHANGE_DOF (src/exchange_data.f90:153-258) are
  * gathered on the device. */
 int lymph_step(lymph_ctx* ctx, double t);
+/* TIME_STEP_MATRIX_FREE with the reference's host arrays (src/matrix_free.f90
+ * :1230-1385, called at Lymph3D.f90:393 with the copies of :396-397 around
+ * it): u0 = u^{n-1} and un = u^n go up, one leapfrog step at time t runs,
+ * and usol = u^{n+1} comes back, in the given layout (LYMPH_LAYOUT_FORTRAN:
+ * the reference's u(ie, k)).  The same values as lymph_set_state(U0, u0),
+ * lymph_set_state(UN, un), lymph_step(t), lymph_get_state(UN, usol), with
+ * the two uploads on separate streams and one synchronisation.  Afterwards
+ * the context holds U0 = u^n and UN = u^{n+1}. */
+int lymph_time_step_host(lymph_ctx* ctx, double t, const double* u0, const double* un, double* usol, int layout);
 
 /* The two steps above with the time-function value g supplied by the caller
  * instead of sin(sqrt(2) pi t) (problem_data_and_properties.f90:14-23), for

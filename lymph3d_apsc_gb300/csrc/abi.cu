@@ -169,10 +169,10 @@ __global__ void k_transpose(const double* __restrict__ src, double* __restrict__
     }
 }
 
-int transpose(lymph_ctx* c, const double* src, double* dst, int64_t rows, int64_t cols) {
+int transpose(lymph_ctx* c, const double* src, double* dst, int64_t rows, int64_t cols, cudaStream_t st) {
     const int64_t tiles = ((rows + 31) / 32) * ((cols + 31) / 32);
     if (tiles <= 0) return LYMPH_OK;
-    k_transpose<<<(unsigned)tiles, dim3(32, 8), 0, c->stream>>>(src, dst, rows, cols);
+    k_transpose<<<(unsigned)tiles, dim3(32, 8), 0, st>>>(src, dst, rows, cols);
     c->launches++;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
@@ -197,10 +197,17 @@ double* lymph_slot_ptr(lymph_ctx* c, int slot) {
     }
 }
 
+int status_rc(lymph_ctx* c, int st, const char* where);
+
 int lymph_sync_status(lymph_ctx* c, const char* where) {
     LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
     int st = 0;
     LYMPH_CUDA_TRY(cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    return status_rc(c, st, where);
+}
+
+// The status word's meaning as a return code (and the word cleared).
+int status_rc(lymph_ctx* c, int st, const char* where) {
     if (st == 0) return LYMPH_OK;
     LYMPH_CUDA_TRY(cudaMemset(c->d_status, 0, sizeof(int)));
     std::string w(where);
@@ -230,6 +237,10 @@ int lymph_destroy(lymph_ctx* c) {
                     c->d_v0, c->d_uex, c->d_gvals, c->d_step_idx, c->d_partial, c->d_scalar, c->d_status,
                     c->d_mf_tri, c->d_mf_poly, c->d_mf_u32, c->d_mf_range, c->d_layout};
     for (void* p : ptrs) dfree(p);
+    dfree(c->d_layout2);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->ev_copy) cudaEventDestroy(c->ev_copy);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LYMPH_OK;
@@ -508,6 +519,46 @@ int lymph_step(lymph_ctx* c, double t) {
     return lymph_sync_status(c, "lymph_step");
 }
 
+int lymph_time_step_host(lymph_ctx* c, double t, const double* u0, const double* un, double* usol, int layout) {
+    if (!c || !u0 || !un || !usol) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_time_step_host: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    const size_t nv = (size_t)c->n_poly * c->nd, bytes = nv * sizeof(double);
+    const bool fort = layout == LYMPH_LAYOUT_FORTRAN;
+    if (!c->stream2) LYMPH_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    if (!c->ev_copy) LYMPH_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
+    if (!c->h_status) LYMPH_CUDA_TRY(cudaHostAlloc((void**)&c->h_status, sizeof(int), cudaHostAllocDefault));
+    if (fort) {
+        LYMPH_TRY(layout_buffer(c));
+        if (!c->d_layout2) LYMPH_TRY(dalloc(c, &c->d_layout2, nv));
+    }
+    double* d_u0 = lymph_slot_ptr(c, LYMPH_SLOT_U0);
+    double* d_un = lymph_slot_ptr(c, LYMPH_SLOT_UN);
+    // the second stream starts after what the context stream has queued
+    LYMPH_CUDA_TRY(cudaEventRecord(c->ev_copy, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamWaitEvent(c->stream2, c->ev_copy, 0));
+    // u^{n-1} up on the second stream, u^n on the context stream: two copy engines
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(fort ? c->d_layout2 : d_u0, u0, bytes, cudaMemcpyHostToDevice, c->stream2));
+    if (fort) LYMPH_TRY(transpose(c, c->d_layout2, d_u0, c->nd, c->n_poly, c->stream2));
+    LYMPH_CUDA_TRY(cudaEventRecord(c->ev_copy, c->stream2));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(fort ? c->d_layout : d_un, un, bytes, cudaMemcpyHostToDevice, c->stream));
+    if (fort) LYMPH_TRY(transpose(c, c->d_layout, d_un, c->nd, c->n_poly, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_copy, 0));
+    // TIME_STEP_MATRIX_FREE
+    LYMPH_TRY(set_g(c, time_function(t)));
+    LYMPH_TRY(lymph_dev_step(c, false));
+    c->cur ^= 1;
+    // u^{n+1} down and the status word, then one synchronisation
+    const double* d_out = lymph_slot_ptr(c, LYMPH_SLOT_UN);
+    if (fort) {
+        LYMPH_TRY(transpose(c, d_out, c->d_layout, c->n_poly, c->nd, c->stream));
+        d_out = c->d_layout;
+    }
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(usol, d_out, bytes, cudaMemcpyDeviceToHost, c->stream));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return status_rc(c, *c->h_status, "lymph_time_step_host");
+}
+
 int lymph_first_step_g(lymph_ctx* c, double g) {
     if (!c || !std::isfinite(g)) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_first_step_g: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
@@ -636,7 +687,7 @@ int lymph_get_state(lymph_ctx* c, int slot, double* host, int layout) {
     if (layout == LYMPH_LAYOUT_FORTRAN) {
         // transposed on the device, then one direct copy
         LYMPH_TRY(layout_buffer(c));
-        LYMPH_TRY(transpose(c, src, c->d_layout, c->n_poly, c->nd));
+        LYMPH_TRY(transpose(c, src, c->d_layout, c->n_poly, c->nd, c->stream));
         src = c->d_layout;
     }
     // a page-locked caller buffer moves by DMA
@@ -654,7 +705,7 @@ int lymph_set_state(lymph_ctx* c, int slot, const double* host, int layout) {
     } else {
         LYMPH_TRY(layout_buffer(c));
         LYMPH_CUDA_TRY(cudaMemcpyAsync(c->d_layout, host, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        LYMPH_TRY(transpose(c, c->d_layout, dst, c->nd, c->n_poly));
+        LYMPH_TRY(transpose(c, c->d_layout, dst, c->nd, c->n_poly, c->stream));
     }
     LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return LYMPH_OK;

@@ -111,6 +111,10 @@ struct lymph_ctx {
     double* d_partial = nullptr;    // per-polyhedron partial sums (error norms)
     double* d_scalar = nullptr;
     double* d_layout = nullptr;     // staging of a state in the reference's (ie, k) layout (allocated on first use)
+    double* d_layout2 = nullptr;    // a second staging buffer (lymph_time_step_host's u^{n-1})
+    cudaStream_t stream2 = nullptr; // lymph_time_step_host: the second upload runs on its own copy engine
+    cudaEvent_t ev_copy = nullptr;
+    int* h_status = nullptr;        // page-locked copy of d_status (read without a second round trip)
     int* d_status = nullptr;
     bool have_matrices = false, have_rhs_stat = false, have_rhs_dyn = false;
     int64_t launches = 0;

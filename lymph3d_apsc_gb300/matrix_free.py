@@ -92,6 +92,20 @@ class MatrixFree:
         """matrix_free.f90:1230-1385 + the rotation u0_loc = un_loc; un_loc = usol."""
         check(self.lib.lymph_step(self.ctx, t), "TIME_STEP_MATRIX_FREE")
 
+    def time_step_host(self, t: float, u0: np.ndarray, un: np.ndarray, usol: np.ndarray,
+                       layout: int = LAYOUT_POLY_MAJOR) -> np.ndarray:
+        """TIME_STEP_MATRIX_FREE with host arrays, the reference's argument list
+        (matrix_free.f90:1230-1385): u0 = u^{n-1}, un = u^n in, usol = u^{n+1}
+        out (filled in place), in the given layout; one C call
+        (lymph_time_step_host)."""
+        a = np.ascontiguousarray(u0, dtype=np.float64)
+        b = np.ascontiguousarray(un, dtype=np.float64)
+        if usol.dtype != np.float64 or not usol.flags.c_contiguous or usol.size != self.n_poly * self.nd:
+            raise ValueError("usol must be a C-contiguous float64 array of the state's size")
+        check(self.lib.lymph_time_step_host(self.ctx, t, ptr(a, c_double), ptr(b, c_double), ptr(usol, c_double), layout),
+              "TIME_STEP_MATRIX_FREE")
+        return usol
+
     def COMPUTE_ERROR_L2_MATRIX_FREE(self, slot_uh: int = SLOT_UN, slot_uex: int = SLOT_UEX) -> float:
         """matrix_free.f90:1388-1418: local sum of squares (no sqrt)."""
         out = c_double()

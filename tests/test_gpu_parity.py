@@ -293,6 +293,34 @@ def test_graph_loop_bitwise_equals_single_steps(require_gpu, p):
         x.close()
 
 
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED_MF])
+@pytest.mark.parametrize("layout", [_lib.LAYOUT_POLY_MAJOR, _lib.LAYOUT_FORTRAN])
+def test_time_step_host_equals_the_separate_calls(require_gpu, precision, layout):
+    """lymph_time_step_host (TIME_STEP_MATRIX_FREE with host u0, un in and
+    usol out) gives the bits of set_state, set_state, lymph_step, get_state,
+    and leaves the context in the same state."""
+    a = _prepared("bfs_ref_jitter", 3, precision=precision)
+    b = _prepared("bfs_ref_jitter", 3, precision=precision)
+    rng = np.random.default_rng(11)
+    shape = (a.n_poly, a.nd) if layout == _lib.LAYOUT_POLY_MAJOR else (a.nd, a.n_poly)
+    u0 = rng.standard_normal(shape) * 1e-3
+    un = rng.standard_normal(shape) * 1e-3
+    t = 5 * a.dt
+    for _ in range(3):
+        usol = np.empty(a.n_poly * a.nd)
+        a.time_step_host(t, u0, un, usol, layout)
+        b.set_state(_lib.SLOT_U0, u0, layout)
+        b.set_state(_lib.SLOT_UN, un, layout)
+        b.TIME_STEP_MATRIX_FREE(t)
+        ref = b.get_state(_lib.SLOT_UN, layout)
+        assert np.array_equal(usol.reshape(shape), ref)
+        assert np.array_equal(a.get_state(_lib.SLOT_U0), b.get_state(_lib.SLOT_U0))
+        u0, un = un, usol.reshape(shape)
+        t += a.dt
+    a.close()
+    b.close()
+
+
 def test_layout_roundtrip_and_fortran_order(require_gpu):
     g = _prepared("hex_dir", 2)
     u = g.get_state(_lib.SLOT_UN)
