@@ -192,6 +192,20 @@ def step_traffic_per_launch(cfg_name, n_blocks):
 # ---------------------------------------------------------------------------
 # CPU arm: the oracle (reference algorithm) on the host cores
 # ---------------------------------------------------------------------------
+def host_cpu():
+    """The host's CPU model (lscpu's "Model name", else the architecture)."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.machine()
+
+
 def cpu_sample(cfg, steps=None, warmup=1, target_s=12.0, threads=None):
     from oracle.oracle_py import Oracle, load as oracle_load
     lib = oracle_load()
@@ -711,9 +725,15 @@ def main():
                        "pinned_host": e["pinned"], "host_layout": "reference u(ie, k), column-major",
                        "call": "lymph_time_step_host"}
     if info["rank"] == 0 and not args.no_cpu_baseline:
-        cb = cpu_sample(cfg)
+        cores_all = os.cpu_count() or 1
+        cb = cpu_sample(cfg, threads=cores_all)
+        # the same sample on one thread (a shorter run), and what the host is
+        c1 = cpu_sample(cfg, target_s=5.0, threads=1)
+        from oracle.oracle_py import load as oracle_load
+        oracle_load().oracle_set_threads(cores_all)
         line["cpu_baseline"] = {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",
-                                "sample": cb["sample"]}
+                                "sample": cb["sample"], "single_thread_value": c1["value"],
+                                "host_cpu": host_cpu(), "nproc": cores_all}
     if info["rank"] == 0 and precision == 0 and not args.no_mixed:
         for key, prec in (("mixed", 1), ("mixed_mf", 2)):
             rm = run_gpu(cfg, prec, args.steps, args.warmup, {**info, "barrier": lambda: None, "max": lambda x: x},
