@@ -63,7 +63,9 @@ extern "C" {
                             matrix-free in FP32 at every step from the face
                             quadrature (Q's field and gradient at P's
                             quadrature points, tested against P's basis), so no
-                            neighbour block is stored or read; FP32
+                            neighbour block is stored or read; the triangle
+                            rule is exact to degree 2p with fewer nodes than
+                            the reference's (lymph_mf_face_rule); FP32
                             accumulation, FP64 combine, mass inverse, update
                             and error norms. */
 
