@@ -317,15 +317,20 @@ template <int PD> struct MfSmem {
         float2 leg[S::NPT][S::LEGW];   // P's (L, L') per point: direction-major, then degree
         float4 flux[S::NPT][3];        // (G_i0, G_i1, G_i2, s_i) per point, scaled by P's map
     };
+    struct Fin {                       // after the face loop
+        float red[MF_SLOTS][S::ND];    // the slots' partial rows
+        double b[S::ND];               // the right-hand side of the M^-1 apply (beside red: the
+                                       // last reads of red and the writes of b are not separated
+                                       // by a barrier)
+    };
     union Work {
         Loop loop;
-        float red[MF_SLOTS][S::ND];    // after the face loop: the slots' partial rows
+        Fin fin;
     };
     Work w;
     float4 uQ[2][S::CT][S::NP];        // (u_0, u_1, u_2, 0) per basis function
     alignas(16) MfTri tri[2][S::CT];
     alignas(16) MfPoly polyQ[2][S::CT];
-    double b[S::ND];
     float quad[3 * S::NQ2];
     float uP[S::ND];
     int rec[MF_REC];
@@ -353,7 +358,7 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     auto& s_uQ = sm.uQ;
     float* s_quad = sm.quad;
     float* s_uP = sm.uP;
-    double* s_b = sm.b;
+    double* s_b = sm.w.fin.b;
     const int tid = threadIdx.x;
     // the polyhedron's record (triangle range and neighbours) in one load,
     // so the first chunk's staging waits on one global round trip, not three
@@ -498,7 +503,7 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     __syncthreads();  // the loop buffers are free: reuse them for the slots' rows
     if (tact) {
 #pragma unroll
-        for (int i = 0; i < NP; ++i) s_w.red[slot][ci * NP + i] = acc[i];
+        for (int i = 0; i < NP; ++i) s_w.fin.red[slot][ci * NP + i] = acc[i];
     }
     // ---- self block (FP32, from L2; the test sums are parked, so the
     // registers go to loads in flight) ----
@@ -518,7 +523,7 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     if (tid < ND) {
         float t = 0.0f;
 #pragma unroll 6
-        for (int kk = 0; kk < MF_SLOTS; ++kk) t += s_w.red[kk][tid];
+        for (int kk = 0; kk < MF_SLOTS; ++kk) t += s_w.fin.red[kk][tid];
         y = (double)yself + (double)t;
     }
     finish_poly<PD, MODE>(sa, P, y, s_b);
