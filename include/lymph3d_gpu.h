@@ -224,6 +224,19 @@ int lymph_copy_state(lymph_ctx* ctx, int dst_slot, int src_slot);
 int lymph_get_state(lymph_ctx* ctx, int slot, double* host, int layout);
 int lymph_set_state(lymph_ctx* ctx, int slot, const double* host, int layout);
 
+/* Checkpoint / resume of the time loop (the reference parses RESTART and
+ * BKPFILE, src/Poly_readfile.f90:109-110, 129-131, but does not implement
+ * them).  _save writes u^{n-1}, u^n, the caller's time t and step count, and
+ * what identifies the run (a hash of the mesh descriptor's arrays, degree,
+ * precision, dt, alpha, theta) to path, through a temporary file renamed at
+ * the end.  _load, on a context built from the same mesh and parameters and
+ * set up (lymph_make_matrices, lymph_make_rhs), restores the two states and
+ * returns t and the step count; a file written for another run is refused
+ * (LYMPH_ERR_INVALID).  Stepping on from a loaded checkpoint gives the same
+ * bits as the uninterrupted run. */
+int lymph_checkpoint_save(lymph_ctx* ctx, const char* path, double t, int64_t steps);
+int lymph_checkpoint_load(lymph_ctx* ctx, const char* path, double* t, int64_t* steps);
+
 /* COMPUTE_ERROR_L2_MATRIX_FREE (src/matrix_free.f90:1388-1418): sum over
  * polyhedra and components of du^T M_modal du, du = slot_uh - slot_uex.
  * Returns the sum of squares; the caller takes the square root, as the

@@ -111,6 +111,8 @@ _SIGS = {
     "lymph_batch_schedule": (c_int, [c_void_p, P_I32, P_I32, P_I32]),
     "lymph_mf_face_rule": (c_int, [c_int32, P_I32, P_F64]),
     "lymph_time_step_host": (c_int, [c_void_p, c_double, P_F64, P_F64, P_F64, c_int]),
+    "lymph_checkpoint_save": (c_int, [c_void_p, c_char_p, c_double, c_int64]),
+    "lymph_checkpoint_load": (c_int, [c_void_p, c_char_p, POINTER(c_double), POINTER(c_int64)]),
     "lymph_batch_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_energy": (c_int, [c_void_p, c_int, c_int, P_F64]),
     "lymph_mpnn_create": (c_int, [c_int32, c_int32, c_int32, c_int32, c_int32, POINTER(c_void_p)]),

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
@@ -148,6 +149,44 @@ int set_g(lymph_ctx* c, double g) {
 }
 
 bool valid_slot(int s) { return s >= 0 && s < LYMPH_NUM_SLOTS; }
+
+// FNV-1a (64-bit) over byte ranges: identifies the mesh a checkpoint belongs to.
+struct Fnv64 {
+    uint64_t h = 1469598103934665603ull;
+    void add(const void* p, size_t n) {
+        const unsigned char* b = (const unsigned char*)p;
+        for (size_t i = 0; i < n; ++i) { h ^= b[i]; h *= 1099511628211ull; }
+    }
+    template <typename T> void add_value(T v) { add(&v, sizeof(v)); }
+};
+
+uint64_t mesh_hash(const lymph_mesh_desc* m) {
+    Fnv64 f;
+    f.add_value(m->n_node); f.add_value(m->n_tet); f.add_value(m->n_poly); f.add_value(m->n_mat);
+    f.add(m->coords, sizeof(double) * 3 * (size_t)m->n_node);
+    f.add(m->tet_vert, sizeof(int32_t) * 4 * (size_t)m->n_tet);
+    f.add(m->tet_poly, sizeof(int32_t) * (size_t)m->n_tet);
+    f.add(m->tet_mat, sizeof(int32_t) * (size_t)m->n_tet);
+    f.add(m->neigh, sizeof(int32_t) * 4 * (size_t)m->n_tet);
+    if (m->fun_tag) f.add(m->fun_tag, sizeof(int32_t) * 4 * (size_t)m->n_tet);
+    f.add(m->mat, sizeof(double) * 3 * (size_t)m->n_mat);
+    return f.h;
+}
+
+// The checkpoint file: this header, then u^{n-1} and u^n as [n_poly][3Np]
+// doubles (the device layout), all in the host's byte order.
+struct CheckpointHeader {
+    char magic[8];          // "LYMPHCK1"
+    int32_t version;        // 1
+    int32_t precision;
+    int32_t degree;
+    int32_t reserved;
+    uint64_t mesh_hash;
+    int64_t n_poly, nd;
+    double dt, alpha, theta;
+    double t;               // the caller's time (the next step's t)
+    int64_t steps;          // the caller's step count
+};
 
 // dst = src^T for a row-major rows x cols src (32 x 32 tiles through
 // shared memory, so both sides are read and written in full lines).  The
@@ -295,6 +334,7 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
     c->nq3 = (c->p + 1) * (c->p + 1) * (c->p + 1); c->nq2 = (c->p + 1) * (c->p + 1);
     c->precision = prm->precision; c->alpha = prm->alpha; c->theta = prm->theta; c->dt = prm->dt;
     c->n_node = m->n_node; c->n_tet = nt; c->n_poly = np; c->n_mat = m->n_mat;
+    c->mesh_hash = mesh_hash(m);
     int rc = LYMPH_OK;
     auto fail = [&](int code) { lymph_destroy(c); return code; };
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -708,6 +748,67 @@ int lymph_set_state(lymph_ctx* c, int slot, const double* host, int layout) {
         LYMPH_TRY(transpose(c, c->d_layout, dst, c->nd, c->n_poly, c->stream));
     }
     LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return LYMPH_OK;
+}
+
+int lymph_checkpoint_save(lymph_ctx* c, const char* path, double t, int64_t steps) {
+    if (!c || !path) return LYMPH_ERR_INVALID;
+    CheckpointHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, "LYMPHCK1", 8);
+    h.version = 1;
+    h.precision = c->precision;
+    h.degree = c->p;
+    h.mesh_hash = c->mesh_hash;
+    h.n_poly = c->n_poly;
+    h.nd = c->nd;
+    h.dt = c->dt; h.alpha = c->alpha; h.theta = c->theta;
+    h.t = t;
+    h.steps = steps;
+    const size_t nv = (size_t)c->n_poly * c->nd;
+    std::vector<double> u(2 * nv);
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(u.data(), lymph_slot_ptr(c, LYMPH_SLOT_U0), nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(u.data() + nv, lymph_slot_ptr(c, LYMPH_SLOT_UN), nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) { lymph_set_error(std::string("lymph_checkpoint_save: cannot write ") + tmp); return LYMPH_ERR_INVALID; }
+    const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(u.data(), sizeof(double), 2 * nv, f) == 2 * nv;
+    const bool closed = std::fclose(f) == 0;
+    if (!ok || !closed || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        lymph_set_error(std::string("lymph_checkpoint_save: write failed: ") + path);
+        return LYMPH_ERR_INVALID;
+    }
+    return LYMPH_OK;
+}
+
+int lymph_checkpoint_load(lymph_ctx* c, const char* path, double* t, int64_t* steps) {
+    if (!c || !path) return LYMPH_ERR_INVALID;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) { lymph_set_error(std::string("lymph_checkpoint_load: cannot read ") + path); return LYMPH_ERR_INVALID; }
+    CheckpointHeader h;
+    const size_t nv = (size_t)c->n_poly * c->nd;
+    std::vector<double> u;
+    auto bad = [&](const std::string& why) {
+        std::fclose(f);
+        lymph_set_error("lymph_checkpoint_load: " + why);
+        return LYMPH_ERR_INVALID;
+    };
+    if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, "LYMPHCK1", 8) != 0 || h.version != 1)
+        return bad("not a checkpoint of this library");
+    if (h.mesh_hash != c->mesh_hash || h.n_poly != c->n_poly) return bad("written for another mesh");
+    if (h.degree != c->p || h.nd != c->nd) return bad("written for another degree");
+    if (h.precision != c->precision) return bad("written for another precision mode");
+    if (h.dt != c->dt || h.alpha != c->alpha || h.theta != c->theta) return bad("written with another dt, alpha or theta");
+    u.resize(2 * nv);
+    if (std::fread(u.data(), sizeof(double), 2 * nv, f) != 2 * nv) return bad("truncated file");
+    std::fclose(f);
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(lymph_slot_ptr(c, LYMPH_SLOT_U0), u.data(), nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    LYMPH_CUDA_TRY(cudaMemcpyAsync(lymph_slot_ptr(c, LYMPH_SLOT_UN), u.data() + nv, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    LYMPH_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (t) *t = h.t;
+    if (steps) *steps = h.steps;
     return LYMPH_OK;
 }
 

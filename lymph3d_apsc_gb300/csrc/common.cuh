@@ -65,6 +65,7 @@ struct lymph_ctx {
     double alpha = 10.0, theta = -1.0, dt = 1e-3;
     // sizes
     int n_node = 0, n_tet = 0, n_poly = 0, n_mat = 0;
+    uint64_t mesh_hash = 0;         // FNV-1a of the mesh descriptor's arrays (checkpoints carry it)
     int64_t n_blocks = 0, n_face_sides = 0, n_block_faces = 0;
     cudaStream_t stream = nullptr;
     // host copies needed for set-up logic

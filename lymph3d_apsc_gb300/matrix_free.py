@@ -106,6 +106,17 @@ class MatrixFree:
               "TIME_STEP_MATRIX_FREE")
         return usol
 
+    def save_checkpoint(self, path, t: float, steps: int = 0):
+        """Writes u^{n-1}, u^n, t and the step count (lymph_checkpoint_save)."""
+        check(self.lib.lymph_checkpoint_save(self.ctx, str(path).encode(), t, steps), "save_checkpoint")
+
+    def load_checkpoint(self, path):
+        """Restores u^{n-1}, u^n from a checkpoint of the same run; returns
+        (t, steps) (lymph_checkpoint_load)."""
+        t, n = c_double(), c_int64()
+        check(self.lib.lymph_checkpoint_load(self.ctx, str(path).encode(), byref(t), byref(n)), "load_checkpoint")
+        return t.value, n.value
+
     def COMPUTE_ERROR_L2_MATRIX_FREE(self, slot_uh: int = SLOT_UN, slot_uex: int = SLOT_UEX) -> float:
         """matrix_free.f90:1388-1418: local sum of squares (no sqrt)."""
         out = c_double()

@@ -321,6 +321,36 @@ def test_time_step_host_equals_the_separate_calls(require_gpu, precision, layout
     b.close()
 
 
+@pytest.mark.parametrize("precision", [_lib.FP64, _lib.MIXED_MF])
+def test_checkpoint_resume_is_bitwise(require_gpu, tmp_path, precision):
+    """A run stopped after 17 steps, checkpointed, and resumed in a new
+    context gives the bits of the uninterrupted 40-step run; checkpoints of
+    another degree or mesh are refused."""
+    a = _prepared("bfs_ref_jitter", 3, precision=precision)
+    t, n, _, _ = a.run_steps(a.dt, 1.0, max_steps=40)
+    ref0, ref1 = a.get_state(_lib.SLOT_U0), a.get_state(_lib.SLOT_UN)
+    b = _prepared("bfs_ref_jitter", 3, precision=precision)
+    tb, nb, _, _ = b.run_steps(b.dt, 1.0, max_steps=17)
+    path = tmp_path / "run.ckpt"
+    b.save_checkpoint(path, tb, 1 + nb)
+    c = _prepared("bfs_ref_jitter", 3, precision=precision)
+    tc, steps = c.load_checkpoint(path)
+    assert tc == tb and steps == 18
+    assert np.array_equal(c.get_state(_lib.SLOT_UN), b.get_state(_lib.SLOT_UN))
+    tc, nc, _, _ = c.run_steps(tc, 1.0, max_steps=40 - 17)
+    assert tc == t
+    assert np.array_equal(c.get_state(_lib.SLOT_U0), ref0)
+    assert np.array_equal(c.get_state(_lib.SLOT_UN), ref1)
+    other_p = _prepared("bfs_ref_jitter", 2, precision=precision)
+    other_mesh = _prepared("hex_dir", 3, precision=precision)
+    for g in (other_p, other_mesh):
+        with pytest.raises(LymphError) as e:
+            g.load_checkpoint(path)
+        assert e.value.code == _lib.LYMPH_ERR_INVALID
+    for g in (a, b, c, other_p, other_mesh):
+        g.close()
+
+
 def test_layout_roundtrip_and_fortran_order(require_gpu):
     g = _prepared("hex_dir", 2)
     u = g.get_state(_lib.SLOT_UN)
