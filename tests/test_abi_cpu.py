@@ -137,6 +137,13 @@ def test_create_rejects_bad_input_with_status_codes():
     assert lib.lymph_create(None, byref(prm), byref(h)) == _lib.LYMPH_ERR_INVALID
     prm = _lib.Params(2, 7, 10.0, -1.0, 1e-3)  # unknown precision
     assert lib.lymph_create(byref(d), byref(prm), byref(h)) == _lib.LYMPH_ERR_INVALID
+    # calls on no context are refused, not dereferenced
+    x = np.zeros(4)
+    px = x.ctypes.data_as(_lib.P_F64)
+    assert lib.lymph_time_step_host(None, 0.0, px, px, px, _lib.LAYOUT_FORTRAN) == _lib.LYMPH_ERR_INVALID
+    assert lib.lymph_checkpoint_save(None, b"x.ckpt", 0.0, 0) == _lib.LYMPH_ERR_INVALID
+    assert lib.lymph_checkpoint_load(None, b"x.ckpt", None, None) == _lib.LYMPH_ERR_INVALID
+    assert lib.lymph_step(None, 0.0) == _lib.LYMPH_ERR_INVALID
 
 
 def test_create_without_device_fails_loudly():
