@@ -5,7 +5,9 @@
   face matching (symmetric, every interior face matched once), boundary
   conditions, BFS agglomeration (sizes, connectivity, determinism);
 * argument validation and the failure of lymph_create without a device come
-  back as status codes with a message, never as a crash.
+  back as status codes with a message, never as a crash;
+* the matrix-free path's triangle rules integrate every monomial of degree
+  <= 2p exactly (lymph_mf_face_rule needs no device).
 """
 import ctypes
 import re
