@@ -297,9 +297,11 @@ __device__ __forceinline__ void prefetch_l2(const void* base, int64_t total, con
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s), "r"((uint32_t)(e - s)) : "memory");
 }
 
-// One CTA per polyhedron P.  At the start one thread prefetches into L2 what
-// the end of the CTA reads (the FP32 self block, M^-1, the right-hand sides
-// and the state rows), so those reads do not wait on HBM.  Neighbour
+// One CTA per polyhedron P.  At the start the CTA reads P's record (its
+// triangles' range and neighbours, one coalesced load), and one thread
+// prefetches into L2 what the end of the CTA reads (the FP32 self block,
+// M^-1, the right-hand sides and the state rows), so those reads do not wait
+// on HBM.  Neighbour
 // triangles, CT triangles at a time, their geometry, Q's box and Q's FP32
 // coefficients copied into shared memory with cp.async one chunk ahead
 // (double-buffered): thread t evaluates point t -- Q's field and gradient,
