@@ -1069,6 +1069,80 @@ void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, in
     }
 }
 
+// face_points with a caller's triangle nodes node4 = (xi, eta, 1, 1) per node.
+void face_points_rule(const Oracle& o, int t, int e, int nq, const double* node4, std::vector<double>& pts) {
+    pts.assign(nq * 3, 0.0);
+    const double* fk = &o.fk[t * 12];
+    double temp[3][4];
+    for (int j = 0; j < 3; ++j)
+        for (int q = 0; q < 4; ++q) {
+            temp[j][q] = 0.0;
+            for (int l = 0; l < 4; ++l) temp[j][q] = temp[j][q] + fk[j * 4 + l] * o.nm[e][l][q];
+        }
+    for (int j = 0; j < 3; ++j)
+        for (int q = 0; q < nq; ++q) {
+            double s = 0.0;
+            for (int l = 0; l < 4; ++l) s = s + temp[j][l] * node4[q * 4 + l];
+            pts[q * 3 + j] = s;
+        }
+}
+
+// K_PQ u_Q point by point with a given triangle rule: nq nodes, node4 =
+// (xi, eta, 1, 1) per node as in nodtria2, weights w on the reference
+// triangle (summing to 1/2).
+int neighbour_apply_rule(const Oracle& o, int P, int Qp, const double* uq, int nq2, const double* node4,
+                         const double* wq, double* out) {
+    if (P < 0 || P >= o.n_poly || Qp < 0 || Qp >= o.n_poly || P == Qp) return LYMPH_ERR_INVALID;
+    const int Np = o.Np;
+    for (int r = 0; r < o.nd; ++r) out[r] = 0.0;
+    double bbP[3][2], bbQ[3][2];
+    get_bb(o, P, bbP);
+    get_bb(o, Qp, bbQ);
+    std::vector<double> pts, phP(Np), dP(3 * Np), phQ(Np), dQ(3 * Np);
+    for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1]; ++k) {
+        const int t = o.poly_tets[k];
+        const int mid = o.tet_mat[t];
+        const double lam = o.mat[mid * 3 + 1], mu = o.mat[mid * 3 + 2];
+        for (int f = 0; f < 4; ++f) {
+            const int E2 = o.neigh[t * 4 + f];
+            if (E2 < 0 || o.tet_poly[E2] != Qp) continue;
+            const double* n = &o.normal[t * 12 + f * 3];
+            const double ar = o.area[t * 4 + f];
+            const double sigma = o.alpha * (o.p * o.p) / std::min(o.hk[P], o.hk[Qp]) * (lam + 2 * mu);
+            const double T[3][3] = {{n[0] * n[0] + 0.5 * n[1] * n[1] + 0.5 * n[2] * n[2], 0.5 * n[0] * n[1], 0.5 * n[0] * n[2]},
+                                    {0.5 * n[1] * n[0], n[1] * n[1] + 0.5 * n[0] * n[0] + 0.5 * n[2] * n[2], 0.5 * n[1] * n[2]},
+                                    {0.5 * n[2] * n[0], 0.5 * n[2] * n[1], n[2] * n[2] + 0.5 * n[0] * n[0] + 0.5 * n[1] * n[1]}};
+            face_points_rule(o, t, f, nq2, node4, pts);
+            for (int q = 0; q < nq2; ++q) {
+                const double W = wq[q] * ar;
+                eval_basis_point(&pts[q * 3], bbQ, Np, o.blist.data(), phQ.data(), dQ.data());
+                eval_basis_point(&pts[q * 3], bbP, Np, o.blist.data(), phP.data(), dP.data());
+                double v[3] = {0, 0, 0}, D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                for (int j = 0; j < 3; ++j)
+                    for (int b = 0; b < Np; ++b) {
+                        const double c = uq[j * Np + b];
+                        v[j] += phQ[b] * c;
+                        for (int kk = 0; kk < 3; ++kk) D[j][kk] += dQ[kk * Np + b] * c;
+                    }
+                const double nv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
+                const double trD = D[0][0] + D[1][1] + D[2][2];
+                for (int i = 0; i < 3; ++i) {
+                    double G[3];
+                    for (int kk = 0; kk < 3; ++kk)
+                        G[kk] = -0.5 * o.theta * W * ((i == kk ? lam * nv : 0.0) + mu * (n[i] * v[kk] + v[i] * n[kk]));
+                    const double Tv = T[i][0] * v[0] + T[i][1] * v[1] + T[i][2] * v[2];
+                    const double hh = lam * (n[0] * D[0][i] + n[1] * D[1][i] + n[2] * D[2][i]) + mu * n[i] * trD +
+                                      mu * (n[0] * D[i][0] + n[1] * D[i][1] + n[2] * D[i][2]);
+                    const double si = -W * (sigma * Tv + 0.5 * hh);
+                    for (int a = 0; a < Np; ++a)
+                        out[i * Np + a] += dP[a] * G[0] + dP[Np + a] * G[1] + dP[2 * Np + a] * G[2] + phP[a] * si;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1361,57 +1435,26 @@ int oracle_nodal_values(void* h, int slot, double* out) {
 //   h_i  = lambda sum_j n_j D_ji + mu n_i tr D + mu sum_k n_k D_ik.
 // Test infrastructure: it checks that rearrangement against the assembled
 // block.
+// The point-wise form of the neighbour product with the reference's triangle
+// rule (nodtria2 / weitria2, mapping_quadrature_2D, Poly_ref_mappings.f90:137-186).
 int oracle_neighbour_apply_pointwise(void* h, int P, int Qp, const double* uq, double* out) {
     const Oracle& o = *(const Oracle*)h;
-    if (P < 0 || P >= o.n_poly || Qp < 0 || Qp >= o.n_poly || P == Qp) return LYMPH_ERR_INVALID;
-    const int Np = o.Np, nq2 = o.Q.nq2;
-    for (int r = 0; r < o.nd; ++r) out[r] = 0.0;
-    double bbP[3][2], bbQ[3][2];
-    get_bb(o, P, bbP);
-    get_bb(o, Qp, bbQ);
-    std::vector<double> pts, phP(Np), dP(3 * Np), phQ(Np), dQ(3 * Np);
-    for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1]; ++k) {
-        const int t = o.poly_tets[k];
-        const int mid = o.tet_mat[t];
-        const double lam = o.mat[mid * 3 + 1], mu = o.mat[mid * 3 + 2];
-        for (int f = 0; f < 4; ++f) {
-            const int E2 = o.neigh[t * 4 + f];
-            if (E2 < 0 || o.tet_poly[E2] != Qp) continue;
-            const double* n = &o.normal[t * 12 + f * 3];
-            const double ar = o.area[t * 4 + f];
-            const double sigma = o.alpha * (o.p * o.p) / std::min(o.hk[P], o.hk[Qp]) * (lam + 2 * mu);
-            const double T[3][3] = {{n[0] * n[0] + 0.5 * n[1] * n[1] + 0.5 * n[2] * n[2], 0.5 * n[0] * n[1], 0.5 * n[0] * n[2]},
-                                    {0.5 * n[1] * n[0], n[1] * n[1] + 0.5 * n[0] * n[0] + 0.5 * n[2] * n[2], 0.5 * n[1] * n[2]},
-                                    {0.5 * n[2] * n[0], 0.5 * n[2] * n[1], n[2] * n[2] + 0.5 * n[0] * n[0] + 0.5 * n[1] * n[1]}};
-            face_points(o, t, f, pts);
-            for (int q = 0; q < nq2; ++q) {
-                const double W = o.Q.weitria2[q] * ar;
-                eval_basis_point(&pts[q * 3], bbQ, Np, o.blist.data(), phQ.data(), dQ.data());
-                eval_basis_point(&pts[q * 3], bbP, Np, o.blist.data(), phP.data(), dP.data());
-                double v[3] = {0, 0, 0}, D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-                for (int j = 0; j < 3; ++j)
-                    for (int b = 0; b < Np; ++b) {
-                        const double c = uq[j * Np + b];
-                        v[j] += phQ[b] * c;
-                        for (int kk = 0; kk < 3; ++kk) D[j][kk] += dQ[kk * Np + b] * c;
-                    }
-                const double nv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
-                const double trD = D[0][0] + D[1][1] + D[2][2];
-                for (int i = 0; i < 3; ++i) {
-                    double G[3];
-                    for (int kk = 0; kk < 3; ++kk)
-                        G[kk] = -0.5 * o.theta * W * ((i == kk ? lam * nv : 0.0) + mu * (n[i] * v[kk] + v[i] * n[kk]));
-                    const double Tv = T[i][0] * v[0] + T[i][1] * v[1] + T[i][2] * v[2];
-                    const double hh = lam * (n[0] * D[0][i] + n[1] * D[1][i] + n[2] * D[2][i]) + mu * n[i] * trD +
-                                      mu * (n[0] * D[i][0] + n[1] * D[i][1] + n[2] * D[i][2]);
-                    const double si = -W * (sigma * Tv + 0.5 * hh);
-                    for (int a = 0; a < Np; ++a)
-                        out[i * Np + a] += dP[a] * G[0] + dP[Np + a] * G[1] + dP[2 * Np + a] * G[2] + phP[a] * si;
-                }
-            }
-        }
+    return neighbour_apply_rule(o, P, Qp, uq, o.Q.nq2, o.Q.nodtria2.data(), o.Q.weitria2.data(), out);
+}
+
+// The same with a caller's triangle rule: xyw holds (xi, eta, w) per node.
+int oracle_neighbour_apply_rule(void* h, int P, int Qp, const double* uq, int nq, const double* xyw, double* out) {
+    const Oracle& o = *(const Oracle*)h;
+    if (nq <= 0 || !xyw) return LYMPH_ERR_INVALID;
+    std::vector<double> node4(4 * (size_t)nq), w(nq);
+    for (int q = 0; q < nq; ++q) {
+        node4[4 * q + 0] = xyw[3 * q + 0];
+        node4[4 * q + 1] = xyw[3 * q + 1];
+        node4[4 * q + 2] = 1.0;
+        node4[4 * q + 3] = 1.0;
+        w[q] = xyw[3 * q + 2];
     }
-    return 0;
+    return neighbour_apply_rule(o, P, Qp, uq, nq, node4.data(), w.data(), out);
 }
 
 int oracle_get_pattern(void* h, int32_t* row_ptr, int32_t* col, int64_t* n_blocks_out) {

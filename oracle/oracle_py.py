@@ -70,6 +70,7 @@ def load():
             "oracle_time_function": (c_double, [c_double]),
             "oracle_match_faces": (c_int, [c_int, P_I32, P_I32, P_I32]),
             "oracle_neighbour_apply_pointwise": (c_int, [c_void_p, c_int, c_int, P_F64, P_F64]),
+            "oracle_neighbour_apply_rule": (c_int, [c_void_p, c_int, c_int, P_F64, c_int, P_F64, P_F64]),
         }
         for k, (r, a) in sigs.items():
             f = getattr(lib, k)
@@ -190,6 +191,16 @@ class Oracle:
         out = np.empty(self.nd)
         self._chk(self.lib.oracle_neighbour_apply_pointwise(self.h, int(P), int(Q), _p(uq), _p(out)),
                   "oracle_neighbour_apply_pointwise")
+        return out
+
+    def neighbour_apply_rule(self, P, Q, uq, xyw):
+        """The same with a caller's triangle rule: xyw = (xi, eta, w) per node
+        on the reference triangle (weights summing to 1/2)."""
+        uq = np.ascontiguousarray(uq, dtype=np.float64)
+        r = np.ascontiguousarray(xyw, dtype=np.float64)
+        out = np.empty(self.nd)
+        self._chk(self.lib.oracle_neighbour_apply_rule(self.h, int(P), int(Q), _p(uq), r.size // 3, _p(r), _p(out)),
+                  "oracle_neighbour_apply_rule")
         return out
 
     def block_dict(self, which=0):

@@ -9,6 +9,12 @@ from the oracle's assembled blocks: the two are the same sums in another
 order, so they agree to FP64 rounding (1e-12 normwise relative per block),
 with heterogeneous materials (lambda != mu per polyhedron), jittered
 tetrahedra and every interior-penalty variant theta = -1, 0, 1.
+
+The GPU path integrates each shared triangle with its own symmetric rule,
+exact to degree 2p with fewer nodes (lymph_mf_face_rule).  The second test
+evaluates the point-wise contraction in FP64 with that rule and checks it
+against the assembled block too: the face integrands have degree <= 2p, so
+both rules give the same integrals up to FP64 rounding (1e-12).
 """
 import numpy as np
 import pytest
@@ -43,4 +49,35 @@ def test_pointwise_neighbour_product_equals_the_block(p, theta):
     o.close()
     assert pairs >= 50
     print(f"p={p} theta={theta}: {pairs} neighbour blocks, worst relative difference {worst:.2e}")
+    assert worst <= 1e-12, worst
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_exact_degree_face_rule_gives_the_same_block(p):
+    from ctypes import POINTER, byref, c_double, c_int32
+    from lymph3d_apsc_gb300 import _lib
+    lib = _lib.load()
+    n = c_int32()
+    assert lib.lymph_mf_face_rule(p, byref(n), None) == 0
+    xyw = np.zeros(3 * n.value)
+    assert lib.lymph_mf_face_rule(p, byref(n), xyw.ctypes.data_as(POINTER(c_double))) == 0
+    assert n.value < (p + 1) ** 2
+    m = _mesh()
+    o = Oracle(m, p, 1e-3, theta=-1.0)
+    o.make_matrices()
+    blocks = o.block_dict(0)
+    rng = np.random.default_rng(10 + p)
+    worst, pairs = 0.0, 0
+    for (P, Q), K in blocks.items():
+        if P == Q:
+            continue
+        u = rng.standard_normal(o.nd)
+        want = K @ u
+        got = o.neighbour_apply_rule(P, Q, u, xyw)
+        worst = max(worst, float(np.linalg.norm(got - want) / np.linalg.norm(want)))
+        pairs += 1
+        if pairs >= 150:
+            break
+    o.close()
+    print(f"p={p}: {n.value}-node rule, {pairs} neighbour blocks, worst relative difference {worst:.2e}")
     assert worst <= 1e-12, worst
