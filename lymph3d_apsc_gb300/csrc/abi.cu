@@ -475,6 +475,7 @@ static int make_mf_matrices(lymph_ctx* c) {
 }
 
 int lymph_make_matrices(lymph_ctx* c) {
+    NvtxRange nvtx_("lymph_make_matrices");
     if (!c) return LYMPH_ERR_INVALID;
     if (c->precision == LYMPH_MIXED_MF) {
         if (!c->d_M) {
@@ -522,6 +523,7 @@ int lymph_make_matrices(lymph_ctx* c) {
 }
 
 int lymph_make_rhs(lymph_ctx* c, int which, int fid, int did, int nid) {
+    NvtxRange nvtx_("lymph_make_rhs");
     if (!c || (which != LYMPH_RHS_STAT && which != LYMPH_RHS_DYN)) return LYMPH_ERR_INVALID;
     if (fid < 0 || fid > 2 || did < 0 || did > 2 || nid < 0 || nid > 2) {
         lymph_set_error("lymph_make_rhs: unknown data function id");
@@ -536,6 +538,7 @@ int lymph_make_rhs(lymph_ctx* c, int which, int fid, int did, int nid) {
 }
 
 int lymph_modal_project(lymph_ctx* c, int fun_id, int slot, double scale) {
+    NvtxRange nvtx_("lymph_modal_project");
     if (!c || !valid_slot(slot) || fun_id < 0 || fun_id > 3) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_modal_project: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
     LYMPH_TRY(lymph_dev_vector(c, 1, fun_id, 0, 0, scale, lymph_slot_ptr(c, slot)));
@@ -543,6 +546,7 @@ int lymph_modal_project(lymph_ctx* c, int fun_id, int slot, double scale) {
 }
 
 int lymph_first_step(lymph_ctx* c, double t) {
+    NvtxRange nvtx_("lymph_first_step");
     if (!c) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_first_step: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
     LYMPH_TRY(set_g(c, time_function(t)));
@@ -551,6 +555,7 @@ int lymph_first_step(lymph_ctx* c, double t) {
 }
 
 int lymph_step(lymph_ctx* c, double t) {
+    NvtxRange nvtx_("lymph_step");
     if (!c) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_step: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
     LYMPH_TRY(set_g(c, time_function(t)));
@@ -560,6 +565,7 @@ int lymph_step(lymph_ctx* c, double t) {
 }
 
 int lymph_time_step_host(lymph_ctx* c, double t, const double* u0, const double* un, double* usol, int layout) {
+    NvtxRange nvtx_("lymph_time_step_host");
     if (!c || !u0 || !un || !usol) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_time_step_host: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
     const size_t nv = (size_t)c->n_poly * c->nd, bytes = nv * sizeof(double);
@@ -618,6 +624,7 @@ int lymph_step_g(lymph_ctx* c, double g) {
 
 int lymph_run_steps(lymph_ctx* c, double stop_time, int64_t max_steps, double* t_inout, int64_t* n_done,
                     float* ms_total, float* ms_kernel) {
+    NvtxRange nvtx_("lymph_run_steps");
     if (!c || !t_inout) return LYMPH_ERR_INVALID;
     if (!c->have_matrices) { lymph_set_error("lymph_run_steps: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
     // time values with the reference's accumulation (Lymph3D.f90:389-418)
@@ -699,6 +706,7 @@ int lymph_run_steps(lymph_ctx* c, double stop_time, int64_t max_steps, double* t
             // the graph holds the buffer pointers of parity cur0; R is even, so
             // the parity is the same after every launch
             for (; i + R <= n; i += R) {
+                NvtxRange nvtx_step("16 leapfrog steps (graph)");
                 LYMPH_CUDA_TRY(cudaGraphLaunch(c->graph_exec, c->stream));
                 c->launches += c->graph_launches;
             }

@@ -397,6 +397,7 @@ int lymph_batch_destroy(lymph_batch* b) {
 }
 
 int lymph_batch_run(lymph_batch* b, int64_t n_steps, const double* gvals, float* ms_total) {
+    NvtxRange nvtx_("lymph_batch_run");
     if (!b || n_steps < 0 || (n_steps > 0 && !gvals)) return LYMPH_ERR_INVALID;
     if (ms_total) *ms_total = 0.0f;
     if (n_steps == 0) return LYMPH_OK;

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <string>
 #include <vector>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/lymph3d_gpu.h"
 
@@ -124,6 +125,16 @@ struct lymph_ctx {
     int graph_steps = 0;
     int64_t graph_launches = 0;     // kernel launches one graph launch stands for
     int graph_parity = -1;
+};
+
+// A named NVTX range over the host-side extent of a C-ABI call or a graph
+// launch (visible to nsys and to ncu's --nvtx filters; no cost when no tool
+// is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 double* lymph_slot_ptr(lymph_ctx* c, int slot);
