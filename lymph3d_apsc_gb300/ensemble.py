@@ -1,5 +1,6 @@
 """Batched ensembles: many independent problems advanced by one persistent
-launch per step (lymph_batch_* in include/lymph3d_gpu.h).
+launch per step (lymph_batch_* in include/lymph3d_gpu.h; with matrix-free
+neighbour terms, one per degree present).
 
 `make_ensemble` builds the seeded ensemble of uneven problems (cube meshes of
 n^3 x 6 tetrahedra, BFS polyhedra, degree p per problem, a Ricker point
