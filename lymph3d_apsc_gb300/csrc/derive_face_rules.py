@@ -9,8 +9,10 @@ nodes) and (a, b, 1 - a - b) (S111, 6 nodes).  The orbit structures used
 (S21 for degree 2; 2 x S21 for 4; 2 x S21 + S111 for 6; S3 + 3 x S21 + S111
 for 8) are the classical ones with 3, 6, 12 and 16 nodes.  The script finds a
 solution with interior nodes and positive weights by least squares from
-random starts (double precision), refines it by Gauss-Newton at 40 digits
-(mpmath) and prints the table.  Run: python derive_face_rules.py
+seeded random starts (double precision), refines it by Gauss-Newton at 40
+digits (mpmath) and prints the table.  The degree-6 structure admits more
+than one such rule; the seeded search finds the one in mf.cu, and any of them
+would give the same integrals.  Run: python derive_face_rules.py
 """
 from math import factorial
 

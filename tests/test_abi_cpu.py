@@ -188,3 +188,28 @@ def test_matrix_free_face_rules_are_exact_to_degree_2p():
                 exact = factorial(i) * factorial(j) / factorial(i + j + 2)
                 assert abs(np.sum(w * xi ** i * eta ** j) - exact) <= 1e-15, (p, i, j)
     assert lib.lymph_mf_face_rule(5, byref(n), None) != 0
+
+
+def test_face_rules_are_what_their_derivation_script_gives():
+    """csrc/derive_face_rules.py (least squares from seeded starts, then
+    Gauss-Newton at 40 digits) reproduces the library's triangle rules: the
+    same nodes and weights, in any order, to 1e-15."""
+    import importlib.util
+    from ctypes import POINTER, byref, c_double, c_int32
+    spec = importlib.util.spec_from_file_location(
+        "derive_face_rules", ROOT / "lymph3d_apsc_gb300" / "csrc" / "derive_face_rules.py")
+    d = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(d)
+    lib = _lib.load()
+    for p in (1, 2, 3, 4):
+        x, res = d.refine(d.STRUCT[p], 2 * p, d.first_guess(d.STRUCT[p], 2 * p), iters=6)
+        assert float(res) < 1e-30
+        pts, ws = d.nodes(d.STRUCT[p], x, d.mp.mpf(1))
+        got = np.array(sorted((float(a), float(b), float(w)) for (a, b), w in zip(pts, ws)))
+        n = c_int32()
+        lib.lymph_mf_face_rule(p, byref(n), None)
+        xyw = np.zeros(3 * n.value)
+        lib.lymph_mf_face_rule(p, byref(n), xyw.ctypes.data_as(POINTER(c_double)))
+        want = np.array(sorted(map(tuple, xyw.reshape(-1, 3))))
+        assert got.shape == want.shape
+        assert np.abs(got - want).max() <= 1e-15, p
