@@ -267,6 +267,15 @@ int lymph_error_dg(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
 int lymph_error_l2_noalloc(const double* d_mass_modal, const double* d_uh, const double* d_uex, int32_t n_poly,
                            int32_t Np, double* sumsq);
 
+/* ku = K u: the operator apply of TIME_STEP_MATRIX_FREE alone, before the
+ * mass-matrix solve (the tp_KU mat-vecs over the self and neighbour blocks,
+ * src/matrix_free.f90:1292-1338), in the context's precision: FP64 blocks,
+ * FP32 blocks, or FP32 self blocks plus the matrix-free FP32 face terms
+ * (LYMPH_MIXED_MF), rows summed in FP64.  u and ku are host arrays
+ * [n_poly][3Np] (poly-major).  For parity checks of each precision's
+ * operator; the step kernels fuse this apply with the rest of the step. */
+int lymph_apply_operator(lymph_ctx* ctx, const double* u, double* ku);
+
 /* Discrete energy of the leapfrog pair (u^a = slot_a, u^b = slot_b, one step
  * apart): E = 1/2 |(u^b - u^a)/dt|^2_M + 1/2 u^b . K u^a, the quantity the
  * scheme conserves without forcing when K is symmetric (SIPG, lambda = mu).

@@ -115,6 +115,7 @@ _SIGS = {
     "lymph_checkpoint_load": (c_int, [c_void_p, c_char_p, POINTER(c_double), POINTER(c_int64)]),
     "lymph_batch_launch_count": (c_int, [c_void_p, POINTER(c_int64)]),
     "lymph_energy": (c_int, [c_void_p, c_int, c_int, P_F64]),
+    "lymph_apply_operator": (c_int, [c_void_p, P_F64, P_F64]),
     "lymph_mpnn_create": (c_int, [c_int32, c_int32, c_int32, c_int32, c_int32, POINTER(c_void_p)]),
     "lymph_mpnn_destroy": (c_int, [c_void_p]),
     "lymph_mpnn_num_params": (c_int64, [c_void_p]),

@@ -28,6 +28,7 @@ int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double s
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
 int lymph_dev_apply(lymph_ctx* c, const double* u, double* out);
+int lymph_dev_ku(lymph_ctx* c, const double* u, double* out);
 int lymph_dev_double_couple(lymph_ctx* c, int t, int P, const double moment[9], double* out);
 int lymph_dev_power_iteration(lymph_ctx* c, double* x, double* y, double* d_ss, int iters);
 int lymph_dev_point_source(lymph_ctx* c, int P, const double x0[3], const double dir[3], double* out);
@@ -865,6 +866,29 @@ int lymph_energy(lymph_ctx* c, int slot_a, int slot_b, double* energy) {
     LYMPH_TRY(lymph_sync_status(c, "lymph_energy"));
     *energy = 0.5 * t[0] / (c->dt * c->dt) + 0.5 * t[1];
     return LYMPH_OK;
+}
+
+int lymph_apply_operator(lymph_ctx* c, const double* u, double* ku) {
+    if (!c || !u || !ku) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_apply_operator: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    const size_t nv = (size_t)c->n_poly * c->nd;
+    double *du = nullptr, *dk = nullptr;
+    if (cudaMalloc(&du, nv * sizeof(double)) != cudaSuccess || cudaMalloc(&dk, nv * sizeof(double)) != cudaSuccess) {
+        if (du) cudaFree(du);
+        cudaGetLastError();
+        lymph_set_error("lymph_apply_operator: out of memory");
+        return LYMPH_ERR_OOM;
+    }
+    int rc = LYMPH_OK;
+    if (cudaMemcpyAsync(du, u, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+    if (rc == LYMPH_OK) rc = lymph_dev_ku(c, du, dk);
+    if (rc == LYMPH_OK && cudaMemcpyAsync(ku, dk, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+        rc = LYMPH_ERR_CUDA;
+    cudaStreamSynchronize(c->stream);
+    cudaFree(du);
+    cudaFree(dk);
+    LYMPH_TRY(rc);
+    return lymph_sync_status(c, "lymph_apply_operator");
 }
 
 int lymph_compute_error_l2_free(lymph_ctx* c, int s_uh, int s_uex, double* sumsq) { return lymph_error_l2(c, s_uh, s_uex, sumsq); }

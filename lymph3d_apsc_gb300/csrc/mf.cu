@@ -729,6 +729,7 @@ int launch_mf_p(lymph_ctx* c, int mode, const StepArgs& s) {
         case MODE_FIRST: return launch_mf_t<PD, MODE_FIRST>(c, s);
         case MODE_APPLY: return launch_mf_t<PD, MODE_APPLY>(c, s);
         case MODE_BILIN: return launch_mf_t<PD, MODE_BILIN>(c, s);
+        case MODE_KU: return launch_mf_t<PD, MODE_KU>(c, s);
         default: lymph_set_error("matrix-free neighbour terms: unsupported mode"); return LYMPH_ERR_INVALID;
     }
 }

@@ -169,6 +169,16 @@ int lymph_dev_apply(lymph_ctx* c, const double* u, double* out) {
     return launch_ctx<MODE_APPLY>(c, A);
 }
 
+// out = K u in the context's precision (the operator apply of
+// TIME_STEP_MATRIX_FREE before the mass-matrix solve).
+int lymph_dev_ku(lymph_ctx* c, const double* u, double* out) {
+    StepArgs A = base_args(c);
+    A.un = u;
+    A.u0 = u;
+    A.out = out;
+    return launch_ctx<MODE_KU>(c, A);
+}
+
 // out = M^-1 K u with the FP32 copy K32 of an FP64 context's blocks (the
 // surrogate's predictor term, whose own error is far above FP32 rounding).
 int lymph_dev_apply_fp32(lymph_ctx* c, const float* K32, const double* u, double* out) {

@@ -25,7 +25,8 @@ constexpr int NBB = 16;   // neighbour blocks staged in shared memory at once
 
 // MODE_APPLY: out = M^-1 K u (power iteration for the CFL bound)
 // MODE_BILIN: partial[P] = un_P . (K u0)_P (the bilinear form of the leapfrog energy)
-enum { MODE_STEP = 0, MODE_FIRST = 1, MODE_DG = 2, MODE_APPLY = 3, MODE_BILIN = 4 };
+// MODE_KU:    out = K u (the operator apply alone, before M^-1)
+enum { MODE_STEP = 0, MODE_FIRST = 1, MODE_DG = 2, MODE_APPLY = 3, MODE_BILIN = 4, MODE_KU = 5 };
 
 struct StepArgs {
     const int32_t* row_ptr;
@@ -38,7 +39,8 @@ struct StepArgs {
     const int64_t* step_idx;   // index into gvals (device counter)
     const double* u0;          // u^{n-1} (MODE_STEP), u^0 (MODE_FIRST), u_h (MODE_DG)
     const double* un;          // u^n (MODE_STEP, MODE_APPLY), v^0 (MODE_FIRST), u_ex (MODE_DG)
-    double* out;               // u^{n+1} (MODE_STEP: may alias u0), u^1 (MODE_FIRST), M^-1 K u (MODE_APPLY)
+    double* out;               // u^{n+1} (MODE_STEP: may alias u0), u^1 (MODE_FIRST), M^-1 K u (MODE_APPLY),
+                               // K u (MODE_KU)
     double* partial;           // MODE_DG: per-polyhedron du . (A du)
     double dt;
     int* status;
@@ -80,6 +82,13 @@ __device__ __forceinline__ void finish_poly(const StepArgs& A, int P, double y, 
                 e = e + (MODE == MODE_DG ? (A.u0[q] - A.un[q]) : A.un[q]) * s_b[rr];
             }
             A.partial[P] = e;
+        }
+        return;
+    }
+    if (MODE == MODE_KU) {
+        if (tid < ND) {
+            if (!isfinite(y)) atomicOr(A.status, ST_NONFINITE);
+            A.out[(int64_t)P * ND + tid] = y;
         }
         return;
     }
@@ -150,7 +159,7 @@ __device__ __forceinline__ void step_poly(const StepArgs& A, int P, char* smem) 
             const int bb = i / ND, c = i % ND;
             const int64_t q = (int64_t)A.col[b0 + bb] * ND + c;
             double v;
-            if (MODE == MODE_STEP || MODE == MODE_APPLY) v = A.un[q];
+            if (MODE == MODE_STEP || MODE == MODE_APPLY || MODE == MODE_KU) v = A.un[q];
             else if (MODE == MODE_FIRST || MODE == MODE_BILIN) v = A.u0[q];
             else v = A.u0[q] - A.un[q];
             s_u[i] = (AT)v;

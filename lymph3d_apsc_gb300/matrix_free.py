@@ -145,6 +145,14 @@ class MatrixFree:
                                        byref(mk) if kernel_timing else None), "run_steps")
         return tt.value, n.value, ms.value, (mk.value if kernel_timing else None)
 
+    def apply_operator(self, u: np.ndarray) -> np.ndarray:
+        """K u in the context's precision (lymph_apply_operator): the operator
+        apply of TIME_STEP_MATRIX_FREE before the mass-matrix solve."""
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(self.n_poly, self.nd)
+        out = np.empty_like(u)
+        check(self.lib.lymph_apply_operator(self.ctx, ptr(u, c_double), ptr(out, c_double)), "lymph_apply_operator")
+        return out
+
     def get_state(self, slot: int, layout: int = LAYOUT_POLY_MAJOR) -> np.ndarray:
         out = np.empty(self.n_poly * self.nd, np.float64)
         check(self.lib.lymph_get_state(self.ctx, slot, ptr(out, c_double), layout), "get_state")

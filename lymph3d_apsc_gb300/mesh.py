@@ -205,33 +205,53 @@ def read_mesh_file(path: Path):
             np.array(ttag, np.int32))
 
 
-def read_deck(deck_dir, override_materials: bool = True) -> tuple[Mesh, dict]:
-    """Reads a reference deck.  With override_materials the driver's
-    rho = lambda = mu = 1 override (Lymph3D.f90:196-203) is applied.
-    Returns the mesh (one polyhedron per tetrahedron) and Poly.input values."""
+def read_deck_arrays(deck_dir) -> dict:
+    """The raw contents of a reference deck: nodes, tetrahedra with their
+    material tags, tagged boundary triangles (0-based), the MATE table
+    (tag, degree, rho, lambda, mu) and the Poly.input time parameters."""
     d = Path(deck_dir)
     kw = _read_keywords(d / "Poly.input")
     mats, diri, neum = read_mate(d / (kw["MATFILE"] + ".mate"))
     coords, tv, tmat, tris, ttag = read_mesh_file(d / (kw["GRIDFILE"] + ".mesh"))
+    return {"coords": coords, "tet_vert": tv, "tet_mat_tag": tmat, "tria": tris, "tria_tag": ttag,
+            "mate": np.array(mats, np.float64).reshape(-1, 5),
+            "diri_tags": np.array(sorted(diri), np.int32), "neum_tags": np.array(sorted(neum), np.int32),
+            "dt": np.float64(kw.get("TIMESTEP", "1e-3")), "stop_time": np.float64(kw.get("STOPTIME", "1")),
+            "name": d.name}
+
+
+def deck_mesh(arrays: dict, override_materials: bool = True) -> tuple[Mesh, dict]:
+    """Mesh of a deck's raw arrays (read_deck_arrays, or a fixture saved from
+    it): boundary triangles tagged on the tetrahedra's faces, faces matched,
+    the decks' tag convention applied (2-4 Dirichlet, 5-7 Neumann,
+    MAKE_PARTITION_AND_MPI_FILES.f90:2105-2109), one polyhedron per
+    tetrahedron.  With override_materials the driver's rho = lambda = mu = 1
+    override (Lymph3D.f90:196-203) is applied."""
     lib = _lib.load()
+    tv = np.ascontiguousarray(arrays["tet_vert"], dtype=np.int32)
+    tris = np.ascontiguousarray(arrays["tria"], dtype=np.int32)
+    ttag = np.ascontiguousarray(arrays["tria_tag"], dtype=np.int32)
+    coords = np.ascontiguousarray(arrays["coords"], dtype=np.float64)
+    mats = np.asarray(arrays["mate"], dtype=np.float64).reshape(-1, 5)
     ftag = np.zeros_like(tv)
     nunf = c_int32(0)
-    tv = np.ascontiguousarray(tv, dtype=np.int32)
-    tris = np.ascontiguousarray(tris, dtype=np.int32)
-    ttag = np.ascontiguousarray(ttag, dtype=np.int32)
     check(lib.lymph_mesh_tag_boundary(tv.shape[0], ptr(tv, c_int32), tris.shape[0], ptr(tris, c_int32),
                                       ptr(ttag, c_int32), ptr(ftag, c_int32), byref(nunf)), "lymph_mesh_tag_boundary")
     neigh, _ = match_faces(tv)
     neigh, fun = apply_bc(ftag, neigh, _lib.BCMODE_REFERENCE)
-    tag_to_idx = {m[0]: i for i, m in enumerate(mats)}
-    tet_mat = np.array([tag_to_idx[t] for t in tmat], np.int32)
+    tag_to_idx = {int(m[0]): i for i, m in enumerate(mats)}
+    tet_mat = np.array([tag_to_idx[int(t)] for t in arrays["tet_mat_tag"]], np.int32)
     if override_materials:
-        mat = np.ones((len(mats), 3), np.float64)
+        mat = np.ones((mats.shape[0], 3), np.float64)
     else:
-        mat = np.array([[m[2], m[3], m[4]] for m in mats], np.float64)
-    degree = mats[0][1]
+        mat = np.ascontiguousarray(mats[:, 2:5])
     mesh = Mesh(coords, tv, np.arange(tv.shape[0], dtype=np.int32), tet_mat, neigh, fun, mat, ftag,
-                {"deck": str(d), "unfound_tria": nunf.value})
-    params = {"dt": float(kw.get("TIMESTEP", "1e-3")), "stop_time": float(kw.get("STOPTIME", "1")),
-              "degree": degree}
+                {"deck": str(arrays.get("name", "")), "unfound_tria": nunf.value})
+    params = {"dt": float(arrays["dt"]), "stop_time": float(arrays["stop_time"]), "degree": int(mats[0, 1])}
     return mesh, params
+
+
+def read_deck(deck_dir, override_materials: bool = True) -> tuple[Mesh, dict]:
+    """Reads a reference deck (Poly.input, *.mate, *.mesh).  Returns the mesh
+    (one polyhedron per tetrahedron) and the Poly.input values."""
+    return deck_mesh(read_deck_arrays(deck_dir), override_materials)

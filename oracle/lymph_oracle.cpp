@@ -75,6 +75,12 @@ int g_device_order = 0;
 // solves, the way the device kernel applies it.
 int g_explicit_inverse = 0;
 
+// Planted mistakes, for the tests that show a parity bar catches them (0 =
+// none).  Only the point-by-point neighbour product (neighbour_apply_rule)
+// reads it: 1 drops the penalty term, 2 flips the sign of the symmetry term,
+// 3 drops the consistency term, 4 drops the last shared triangle of the pair.
+int g_planted_mistake = 0;
+
 double perturb(double v, const double p[3], int comp) {
     if (g_perturb_ulps == 0 || v == 0.0) return v;
     uint64_t h = 1469598103934665603ull ^ (uint64_t)comp;
@@ -1099,6 +1105,13 @@ int neighbour_apply_rule(const Oracle& o, int P, int Qp, const double* uq, int n
     get_bb(o, P, bbP);
     get_bb(o, Qp, bbQ);
     std::vector<double> pts, phP(Np), dP(3 * Np), phQ(Np), dQ(3 * Np);
+    int n_shared = 0, i_shared = 0;
+    if (g_planted_mistake == 4)
+        for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1]; ++k)
+            for (int f = 0; f < 4; ++f) {
+                const int E2 = o.neigh[o.poly_tets[k] * 4 + f];
+                if (E2 >= 0 && o.tet_poly[E2] == Qp) ++n_shared;
+            }
     for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1]; ++k) {
         const int t = o.poly_tets[k];
         const int mid = o.tet_mat[t];
@@ -1106,6 +1119,7 @@ int neighbour_apply_rule(const Oracle& o, int P, int Qp, const double* uq, int n
         for (int f = 0; f < 4; ++f) {
             const int E2 = o.neigh[t * 4 + f];
             if (E2 < 0 || o.tet_poly[E2] != Qp) continue;
+            if (g_planted_mistake == 4 && ++i_shared == n_shared) continue;
             const double* n = &o.normal[t * 12 + f * 3];
             const double ar = o.area[t * 4 + f];
             const double sigma = o.alpha * (o.p * o.p) / std::min(o.hk[P], o.hk[Qp]) * (lam + 2 * mu);
@@ -1133,7 +1147,10 @@ int neighbour_apply_rule(const Oracle& o, int P, int Qp, const double* uq, int n
                     const double Tv = T[i][0] * v[0] + T[i][1] * v[1] + T[i][2] * v[2];
                     const double hh = lam * (n[0] * D[0][i] + n[1] * D[1][i] + n[2] * D[2][i]) + mu * n[i] * trD +
                                       mu * (n[0] * D[i][0] + n[1] * D[i][1] + n[2] * D[i][2]);
-                    const double si = -W * (sigma * Tv + 0.5 * hh);
+                    const double pen = g_planted_mistake == 1 ? 0.0 : sigma * Tv;
+                    const double sym = g_planted_mistake == 2 ? -0.5 * hh : 0.5 * hh;
+                    const double si = -W * (pen + sym);
+                    if (g_planted_mistake == 3) G[0] = G[1] = G[2] = 0.0;
                     for (int a = 0; a < Np; ++a)
                         out[i * Np + a] += dP[a] * G[0] + dP[Np + a] * G[1] + dP[2 * Np + a] * G[2] + phP[a] * si;
                 }
@@ -1159,6 +1176,8 @@ void oracle_set_reverse_sums(int on) { g_reverse_sums = on; }
 void oracle_set_explicit_inverse(int on) { g_explicit_inverse = on; }
 
 void oracle_set_device_order(int slices) { g_device_order = slices > 0 ? slices : 0; }
+
+void oracle_set_planted_mistake(int kind) { g_planted_mistake = kind; }
 
 int oracle_num_threads(void) {
 #ifdef _OPENMP

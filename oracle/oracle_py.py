@@ -39,6 +39,7 @@ def load():
             "oracle_set_reverse_sums": (None, [c_int]),
             "oracle_set_explicit_inverse": (None, [c_int]),
             "oracle_set_device_order": (None, [c_int]),
+            "oracle_set_planted_mistake": (None, [c_int]),
             "oracle_set_threads": (None, [c_int]),
             "oracle_create": (c_int, [c_void_p, c_int, c_double, c_double, c_double, POINTER(c_void_p)]),
             "oracle_destroy": (c_int, [c_void_p]),

@@ -6,13 +6,17 @@ product at each step from the face quadrature in FP32 (Q's field and gradient
 at P's quadrature points, tested against P's basis): the same sums as the
 assembled block in another order, rounded in FP32 at more places (basis
 values, geometry, the quadrature sums).  Bars (written in each assertion):
-  * one operator application, M^-1 (F - K u) through a leapfrog step from the
-    oracle's state: relative difference to the FP64 oracle <= 30 x the
-    FP32-block path's (both are FP32 evaluations of the FP64 operator; through
-    M^-1, whose condition number reaches ~1e7 at p = 4, the FP32-block path
-    itself differs by up to ~2e-1 from FP64 there, so no absolute bar);
-  * state after 20 leapfrog steps: relative difference to the FP64 oracle
-    <= 30 x the FP32-block path's + 1e-7;
+  * the operator apply alone, K u before M^-1 (lymph_apply_operator), with
+    random coefficients, every polyhedron row against the oracle's FP64 K u
+    from the assembled blocks: max_P ||(K u)_P - ref_P|| / ||ref_P|| <=
+    TOL_APPLY_FP32 (2e-6) for both FP32 forms, <= 1e-13 for FP64 blocks; one
+    dropped or mis-signed face term moves rows by > 100 x that bar
+    (tests/test_mf_formula.py plants each mistake in the oracle);
+  * the state after 20 leapfrog steps from the oracle's state, in the mass
+    norm (the L2 norm of the field): relative <= TOL_STEPS_FP32 (2e-5) for
+    both FP32 forms; the Euclidean differences of the coefficients (up to
+    ~1e-1 after one step at p = 4 for both FP32 forms, through M^-1 whose
+    condition number reaches ~1e7) are printed beside it;
   * L2 / DG errors against the manufactured solution after 0.1 s: <= 1.1 x
     the FP64 path's (the mixed-precision bar), on heterogeneous lognormal
     materials (an operator that is not symmetric);
@@ -29,6 +33,7 @@ import pytest
 from lymph3d_apsc_gb300 import MatrixFree, _lib
 from lymph3d_apsc_gb300._lib import LymphError
 from oracle.oracle_py import Oracle
+from parity_util import TOL_APPLY_FP32, TOL_APPLY_FP64, TOL_STEPS_FP32, mass_norm_rel, oracle_apply, row_rel_max
 from test_gpu_parity import KINDS, _mesh, rel
 
 pytestmark = pytest.mark.gpu
@@ -54,6 +59,27 @@ def _oracle(m, p, dt=1e-3):
     o.modal_project(1, 2)
     o.first_step(0.0)
     return o
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_operator_apply_against_fp64_oracle(require_gpu, kind, p):
+    """K u of every precision, row by row, against the oracle's FP64 K u."""
+    m = _mesh(kind)
+    o = Oracle(m, p, 1e-3)
+    o.make_matrices()
+    u = np.random.default_rng(100 + p).standard_normal((o.n_poly, o.nd))
+    want = oracle_apply(o, u)
+    o.close()
+    errs = {}
+    for name, prec, bar in (("fp64", _lib.FP64, TOL_APPLY_FP64), ("fp32_blocks", _lib.MIXED, TOL_APPLY_FP32),
+                            ("mixed_mf", _lib.MIXED_MF, TOL_APPLY_FP32)):
+        with MatrixFree(m, p, 1e-3, precision=prec) as g:
+            g.MAKE_MATRICES_FREE()
+            errs[name] = row_rel_max(g.apply_operator(u), want)
+        assert errs[name] <= bar, (name, errs[name])
+    print(f"p={p} {kind}: K u row error fp64 {errs['fp64']:.2e} fp32-blocks {errs['fp32_blocks']:.2e} "
+          f"mixed_mf {errs['mixed_mf']:.2e}")
 
 
 @pytest.mark.parametrize("kind", KINDS)
@@ -84,9 +110,11 @@ def test_mf_operator_and_steps_close_to_fp64(require_gpu, kind, p):
     uo = o.get_state(_lib.SLOT_UN)
     s_mf = rel(mf.get_state(_lib.SLOT_UN), uo)
     s_32 = rel(f32.get_state(_lib.SLOT_UN), uo)
-    print(f"p={p} {kind}: one apply mf {e_mf:.2e} fp32-blocks {e_32:.2e}; 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}")
-    assert e_mf <= 30.0 * e_32 + 1e-9
-    assert s_mf <= 30.0 * s_32 + 1e-7
+    m_mf = mass_norm_rel(o, mf.get_state(_lib.SLOT_UN), uo)
+    m_32 = mass_norm_rel(o, f32.get_state(_lib.SLOT_UN), uo)
+    print(f"p={p} {kind}: one apply mf {e_mf:.2e} fp32-blocks {e_32:.2e}; 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}"
+          f"; mass norm mf {m_mf:.2e} fp32-blocks {m_32:.2e}")
+    assert m_mf <= TOL_STEPS_FP32 and m_32 <= TOL_STEPS_FP32, (m_mf, m_32)
     for x in (mf, f32, o):
         x.close()
 
@@ -129,8 +157,11 @@ def test_mf_polyhedron_with_many_neighbour_triangles(require_gpu, p):
     uo = o.get_state(_lib.SLOT_UN)
     s_mf = rel(mf.get_state(_lib.SLOT_UN), uo)
     s_32 = rel(f32.get_state(_lib.SLOT_UN), uo)
-    print(f"p={p} big polyhedron: 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}")
-    assert s_mf <= 30.0 * s_32 + 1e-7
+    m_mf = mass_norm_rel(o, mf.get_state(_lib.SLOT_UN), uo)
+    m_32 = mass_norm_rel(o, f32.get_state(_lib.SLOT_UN), uo)
+    print(f"p={p} big polyhedron: 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}; mass norm mf {m_mf:.2e} "
+          f"fp32-blocks {m_32:.2e}")
+    assert m_mf <= TOL_STEPS_FP32 and m_32 <= TOL_STEPS_FP32, (m_mf, m_32)
     for x in (mf, f32, o):
         x.close()
 
@@ -161,8 +192,10 @@ def test_mf_other_interior_penalty_forms(require_gpu, theta, p):
     o.run_steps(1e-3, 1.0, max_steps=20)
     uo = o.get_state(_lib.SLOT_UN)
     s_mf, s_32 = (rel(g.get_state(_lib.SLOT_UN), uo) for g in runs)
-    print(f"p={p} theta={theta}: 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}")
-    assert s_mf <= 30.0 * s_32 + 1e-7
+    m_mf, m_32 = (mass_norm_rel(o, g.get_state(_lib.SLOT_UN), uo) for g in runs)
+    print(f"p={p} theta={theta}: 20 steps mf {s_mf:.2e} fp32-blocks {s_32:.2e}; mass norm mf {m_mf:.2e} "
+          f"fp32-blocks {m_32:.2e}")
+    assert m_mf <= TOL_STEPS_FP32 and m_32 <= TOL_STEPS_FP32, (m_mf, m_32)
     for x in runs + [o]:
         x.close()
 

@@ -34,6 +34,7 @@ import pytest
 from lymph3d_apsc_gb300 import MatrixFree, _lib, mesh as M
 from lymph3d_apsc_gb300._lib import LymphError
 from oracle.oracle_py import Oracle
+from parity_util import every_step_parity, mass_norm_rel, rel
 
 pytestmark = pytest.mark.gpu
 
@@ -61,13 +62,6 @@ def _mesh(kind):
 
 
 KINDS = ["one_poly", "tet_dir", "tet_ref_jitter", "hex_dir", "bfs_ref_jitter", "bfs_lognormal"]
-
-
-def rel(a, b):
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
-    den = np.linalg.norm(b)
-    return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
 
 
 @pytest.fixture(scope="module")
@@ -117,17 +111,6 @@ def test_setup_parity(require_gpu, pairs, kind, p):
         assert math.sqrt(num / den) <= TOL_SETUP, name
 
 
-def mass_norm_rel(o, a, b):
-    """||a - b||_M / ||b||_M with the oracle's modal mass matrices."""
-    Mm = o.mass(1)
-    Np = o.Np
-    d = (a - b).reshape(o.n_poly, 3, Np)
-    bb = b.reshape(o.n_poly, 3, Np)
-    num = np.einsum("pim,pmn,pin->", d, Mm, d)
-    den = np.einsum("pim,pmn,pin->", bb, Mm, bb)
-    return math.sqrt(max(num, 0.0) / den)
-
-
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("p", [1, 3, 4])
 def test_rhs_and_projection_parity(require_gpu, pairs, kind, p):
@@ -164,83 +147,22 @@ def test_mass_inverse(require_gpu, pairs, kind, p):
     assert np.abs(np.einsum("pij,pjk->pik", M_, Minv) - eye).max() <= 64 * cond * 2.2e-16
 
 
-def _start(g, o):
-    """Same RHS data on both sides; initial coefficients projected by the
-    oracle and copied to the device, so the comparison isolates the step."""
-    g.MAKE_RHS_FREE(_lib.RHS_STAT, _lib.F_NULL, _lib.GD_NULL, _lib.GN_NULL)
-    g.MAKE_RHS_FREE(_lib.RHS_DYN, _lib.F_TIME, _lib.GD, _lib.GN)
-    o.make_rhs(0, 0, 0, 0)
-    o.make_rhs(1, 1, 1, 1)
-    o.modal_project(0, 0)
-    o.modal_project(1, 2)
-    g.set_state(_lib.SLOT_U0, o.get_state(0))
-    g.set_state(_lib.SLOT_V0, o.get_state(2))
-
-
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("p", [1, 2, 3, 4])
 def test_step_parity_every_step(require_gpu, pairs, kind, p):
-    """u^n after every one of 25 steps (first step included)."""
-    from oracle.oracle_py import load as oracle_load
+    """u^n after every one of 25 steps (first step included).  Three more
+    oracle runs evaluate the same steps in other valid orders: (a) reversed
+    sums with FMA and M^-1 as an explicit inverse, (b) forward sums with the
+    explicit inverse, (c) the CUDA kernel's own order (column slices, two FMA
+    accumulators each, explicit inverse).  The floor is their largest spread
+    so far from the reference-order run (rounding noise accumulates over the
+    steps, and one sample of it can fall low).  (c) runs on the oracle's own
+    blocks and inverse, which differ from the device's set-up by rounding, so
+    it is a floor variant, not a bitwise emulation of the device."""
     m, g, o = pairs(kind, p)
-    _start(g, o)
-    # three more oracle runs evaluate the same steps in other valid orders:
-    # (a) reversed sums with FMA and M^-1 as an explicit inverse, (b) forward
-    # sums with the explicit inverse, (c) the CUDA kernel's own order (column
-    # slices, two FMA accumulators each, explicit inverse).  The floor is
-    # their largest spread so far from the reference-order run (rounding
-    # noise accumulates over the steps, and one sample of it can fall low).
-    # (c) runs on the oracle's own blocks and inverse, which differ from the
-    # device's set-up by rounding, so it is a floor variant, not a bitwise
-    # emulation of the device.
-    slices = {1: 8, 2: 8, 3: 4, 4: 3}[p]
-    variants = [(1, 1, 0), (0, 1, 0), (0, 0, slices)]
-    others = []
-    for _ in variants:
-        ox = Oracle(m, p, g.dt)
-        ox.make_matrices()
-        ox.make_rhs(0, 0, 0, 0)
-        ox.make_rhs(1, 1, 1, 1)
-        ox.set_state(0, o.get_state(0))
-        ox.set_state(2, o.get_state(2))
-        others.append(ox)
-    lib = oracle_load()
-    t = 0.0
-    worst = 0.0
-    floor = 0.0
-    worst_dev = 0.0
-    for k in range(25):
-        if k == 0:
-            g.FIRST_TIME_STEP_MATRIX_FREE(t)
-            o.first_step(t)
-        else:
-            g.TIME_STEP_MATRIX_FREE(t)
-            o.step(t)
-        for (rev, inv, dev), ox in zip(variants, others):
-            lib.oracle_set_reverse_sums(rev)
-            lib.oracle_set_explicit_inverse(inv)
-            lib.oracle_set_device_order(dev)
-            if k == 0:
-                ox.first_step(t)
-            else:
-                ox.step(t)
-            lib.oracle_set_reverse_sums(0)
-            lib.oracle_set_explicit_inverse(0)
-            lib.oracle_set_device_order(0)
-        t += g.dt
-        ref = o.get_state(_lib.SLOT_UN)
-        got = g.get_state(_lib.SLOT_UN)
-        floor = max([floor] + [rel(ox.get_state(_lib.SLOT_UN), ref) for ox in others])
-        e = rel(got, ref)
-        worst = max(worst, e / max(TOL_STATE, 4.0 * floor))
-        assert e <= max(TOL_STATE, 4.0 * floor), (k, e, floor)
-        assert mass_norm_rel(o, got, ref) <= TOL_STATE
-        worst_dev = max(worst_dev, rel(got, others[2].get_state(_lib.SLOT_UN)))
-    for ox in others:
-        ox.close()
+    e, floor, worst = every_step_parity(m, p, g, o, n_steps=25)
     assert worst <= 1.0
-    print(f"p={p} {kind}: device vs reference order {e:.2e}, floor {floor:.2e}, "
-          f"device vs its order on the CPU {worst_dev:.2e}")
+    print(f"p={p} {kind}: device vs reference order {e:.2e}, floor {floor:.2e}, bar ratio {worst:.2f}")
 
 
 @pytest.mark.parametrize("kind", ["tet_ref_jitter", "bfs_ref_jitter", "bfs_lognormal"])

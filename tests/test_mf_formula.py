@@ -81,3 +81,50 @@ def test_exact_degree_face_rule_gives_the_same_block(p):
     o.close()
     print(f"p={p}: {n.value}-node rule, {pairs} neighbour blocks, worst relative difference {worst:.2e}")
     assert worst <= 1e-12, worst
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_planted_face_mistakes_exceed_the_operator_bar(p):
+    """The GPU bar on the operator apply (TOL_APPLY_FP32, per polyhedron row,
+    tests/test_gpu_mf.py) is far below what any single face-term mistake
+    does: with one mistake planted in the oracle's point-wise neighbour
+    product (the penalty term dropped, the symmetry term's sign flipped, the
+    consistency term dropped, one shared triangle left out), the rows of
+    K u move by more than 100 x the bar (2e-2 and more against 2e-6)."""
+    from ctypes import POINTER, byref, c_double, c_int32
+    from lymph3d_apsc_gb300 import _lib
+    from oracle.oracle_py import load as oracle_load
+    from parity_util import TOL_APPLY_FP32, oracle_apply, row_rel_max
+    lib = _lib.load()
+    n = c_int32()
+    lib.lymph_mf_face_rule(p, byref(n), None)
+    xyw = np.zeros(3 * n.value)
+    lib.lymph_mf_face_rule(p, byref(n), xyw.ctypes.data_as(POINTER(c_double)))
+    m = _mesh()
+    o = Oracle(m, p, 1e-3)
+    o.make_matrices()
+    rp, col = o.pattern()
+    vals = o.blocks(0)
+    u = np.random.default_rng(5).standard_normal((o.n_poly, o.nd))
+    want = oracle_apply(o, u, vals)
+    olib = oracle_load()
+
+    def rows(plant):
+        olib.oracle_set_planted_mistake(plant)
+        try:
+            out = np.zeros_like(u)
+            for P in range(o.n_poly):
+                for k in range(rp[P], rp[P + 1]):
+                    Q = int(col[k])
+                    out[P] += vals[k] @ u[Q] if Q == P else o.neighbour_apply_rule(P, Q, u[Q], xyw)
+            return out
+        finally:
+            olib.oracle_set_planted_mistake(0)
+
+    clean = row_rel_max(rows(0), want)
+    assert clean <= 1e-12, clean
+    for plant in (1, 2, 3, 4):
+        e = row_rel_max(rows(plant), want)
+        print(f"p={p} planted mistake {plant}: rows move by {e:.2e} (bar {TOL_APPLY_FP32:.0e})")
+        assert e >= 100 * TOL_APPLY_FP32, (plant, e)
+    o.close()

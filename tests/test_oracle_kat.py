@@ -236,17 +236,59 @@ def test_golden_driver_values():
         assert abs(float(np.sum(u * u)) - case["sumsq_un"]) <= 1e-12 * case["sumsq_un"]
 
 
-DECKS = Path("/root/reference/src/tests/analytical")
+DECKS = GOLDEN / "decks"
 
 
-@pytest.mark.skipif(not DECKS.exists(), reason="reference decks not mounted")
-@pytest.mark.parametrize("deck", ["tet_5", "tet_25"])
+def _deck(name):
+    a = dict(np.load(DECKS / f"{name}.npz"))
+    a["name"] = name
+    return M.deck_mesh(a)
+
+
+@pytest.mark.parametrize("deck", ["tet_5", "tet_25", "tet_100", "tet_125"])
 def test_reference_deck_reads_and_runs(deck):
-    mesh, prm = M.read_deck(DECKS / deck)
+    """The reference's decks (committed fixtures of src/tests/analytical/*):
+    every boundary triangle found on a tetrahedron face, every face matched,
+    the decks' tags giving Dirichlet and Neumann faces, and the oracle's
+    driver run reproducing its committed values."""
+    mesh, prm = _deck(deck)
     assert mesh.info["unfound_tria"] == 0
     assert np.all(mesh.neigh != M._lib.MESH_UNMATCHED)
     # the decks mark z=0, z=1, x=1 Dirichlet and y=1, x=0, y=0 Neumann
     assert (mesh.neigh == -1).sum() > 0 and (mesh.neigh == -2).sum() > 0
+    gold = next(x for x in json.loads((DECKS / "deck_driver.json").read_text())["decks"] if x["deck"] == deck)
+    assert mesh.n_tet == gold["n_tet"] and prm["degree"] == gold["p"]
     o = O.Oracle(mesh, prm["degree"], prm["dt"])
-    r = O.run_reference_driver(o, 20 * prm["dt"])
-    assert r["n_steps"] in (20, 21) and math.isfinite(r["err_L2"]) and math.isfinite(r["err_DG"])
+    stop = prm["stop_time"] if deck != "tet_100" else 0.2
+    r = O.run_reference_driver(o, stop)
+    o.close()
+    assert math.isfinite(r["err_L2"]) and math.isfinite(r["err_DG"])
+    if deck != "tet_100":  # the full 3,183-step tet_100 run is left to the GPU test
+        assert r["n_steps"] == gold["n_steps"] and r["t"] == gold["t_final"]
+        assert abs(r["err_L2"] - gold["err_L2"]) <= 1e-12 * gold["err_L2"]
+        assert abs(r["err_DG"] - gold["err_DG"]) <= 1e-12 * gold["err_DG"]
+
+
+def test_agglomeration_fixtures():
+    """elem_in_poly of the benchmark meshes equals the committed arrays: the
+    125 hexahedra of the 5^3 cube and the seeded BFS grouping of the 40^3
+    cube into 46,767 polyhedra of 4..15 tetrahedra."""
+    fx = np.load(GOLDEN / "elem_in_poly.npz")
+    c0 = M.cube(5, bc="dirichlet", agglomeration="hex")
+    assert np.array_equal(c0.tet_poly, fx["c0"]) and c0.n_poly == 125
+    c1 = M.cube(40, bc="dirichlet", agglomeration="bfs", seed=0, group=(4, 12))
+    assert np.array_equal(c1.tet_poly, fx["c1"]) and c1.n_poly == 46767
+    sizes = np.bincount(c1.tet_poly)
+    assert sizes.min() >= 4 and sizes.max() <= 16
+
+
+def test_c0_golden_driver():
+    """The 125-polyhedron p = 2 run to T = 0.1 (1,000 steps) reproduces the
+    committed oracle values."""
+    gold = json.loads((GOLDEN / "c0_driver.json").read_text())
+    o = O.Oracle(M.cube(5, bc="dirichlet", agglomeration="hex"), 2, 1e-4)
+    r = O.run_reference_driver(o, 0.1)
+    o.close()
+    assert r["n_steps"] == gold["n_steps"] == 1000 and r["t"] == gold["t_final"]
+    assert abs(r["err_L2"] - gold["err_L2"]) <= 1e-12 * gold["err_L2"]
+    assert abs(r["err_DG"] - gold["err_DG"]) <= 1e-12 * gold["err_DG"]
