@@ -2,28 +2,35 @@
 """Benchmark of the PolyDG elastodynamics time loop (DOF-steps/s).
 
 Workload (default, one GPU): the 40^3 x 6 = 384,000-tetrahedron unit cube
-agglomerated by seeded BFS into ~48,000 polyhedra of 4..12 tetrahedra,
-degree p = 3 (60 DOFs per polyhedron), rho = 1, lambda = 2, mu = 1, SIPG
-(alpha = 10, theta = -1), manufactured solution, dt = 2e-5.  A "step" is one
-leapfrog step (TIME_STEP_MATRIX_FREE) over the whole mesh.
+agglomerated by seeded BFS into 46,767 polyhedra of 4..15 tetrahedra, degree
+p = 4 (105 DOFs per polyhedron), rho = 1, lambda and mu lognormal per
+polyhedron (median 1, sigma 0.5, seed 1), SIPG (alpha = 10, theta = -1), the
+manufactured solution, dt = 2e-5.  A "step" is one leapfrog step
+(TIME_STEP_MATRIX_FREE) over the whole mesh.
 
-  value    DOF-steps/s of K graph-launched steps, inputs resident in HBM,
-           CUDA events on the library stream.  Inputs (the operator blocks,
-           15 GB) are far larger than L2, so no flush is needed.
+  value    DOF-steps/s of K graph-launched plain FP64 steps, inputs resident
+           in HBM, CUDA events on the library stream.  Inputs (the operator
+           blocks, 45 GB) are far larger than L2, so no flush is needed.
+  mixed, mixed_mf  the same workload with FP32 operator blocks, and with
+           FP32 self blocks plus matrix-free FP32 face terms, with their L2 /
+           DG errors after 1,000 steps beside the FP64 run's.
   e2e      the same metric through the reference-facing C ABI with host
            buffers: every step uploads u^{n-1}, u^n from page-locked host
-           memory, calls lymph_step and reads u^{n+1} back.
-  roofline the step kernel: algorithmic bytes per launch / average launch
-           duration (per-launch CUDA events), against the measured HBM copy
-           bandwidth; the FP64-ALU view is reported beside it.
+           memory, calls lymph_time_step_host and reads u^{n+1} back.
+  roofline the step kernel: FLOPs per launch / average launch duration
+           (per-launch CUDA events) against the GB300's FP64 rate (the pipe
+           that binds it); the HBM view (algorithmic bytes, measured copy
+           bandwidth, ncu DRAM traffic) beside it.
   cpu_baseline  the CPU oracle (restatement of the reference algorithm:
-           assembled element blocks + Cholesky solves) on all host cores,
-           on a bounded sample of the same workload (smaller cube, same
-           degree, grouping and material), per DOF-step.
+           assembled element blocks + Cholesky solves, built -O3) on all
+           host cores, on a bounded sample of the same workload (smaller
+           cube, same degree, grouping and material law), per DOF-step.
 
-`--impl reference` times that CPU implementation alone (the reference arm).
-`--gpus N` runs N independent replicas (the path has no data-path exchange
-on one GPU per problem; see the design notes), value = sum over ranks.
+`--impl reference` times that CPU implementation on the whole configured
+workload (the same mesh, degree, materials and steps), on all host cores, in
+a process that never loads the GPU library (the mesh comes from
+oracle/mesh_py.py).  `--gpus N` runs N independent replicas (the path has no
+data-path exchange on one GPU per problem), value = sum over ranks.
 """
 from __future__ import annotations
 
@@ -206,20 +213,37 @@ def host_cpu():
     return platform.machine()
 
 
-def cpu_sample(cfg, steps=None, warmup=1, target_s=12.0, threads=None):
+def oracle_mesh(cfg, n=None):
+    """The configuration's mesh from oracle/mesh_py.py: the same arrays as
+    the library's cube(), built without loading the GPU library."""
+    from oracle import mesh_py as MP
+    return MP.cube(n or cfg["n"], bc="dirichlet", agglomeration=cfg["agglomeration"], seed=cfg["seed"],
+                   group=cfg["group"], material=cfg["material"], lognormal_seed=1 if cfg["lognormal"] else None)
+
+
+def oracle_prepared(cfg, m, threads=None):
+    """The oracle's driver set-up (Lymph3D.f90:262-368: operator, right-hand
+    sides, initial projections, first step) with the timing build; the A_dg
+    blocks (used only by the DG error) are not assembled."""
     from oracle.oracle_py import Oracle, load as oracle_load
-    lib = oracle_load()
+    lib = oracle_load(timing=True)
     if threads:
         lib.oracle_set_threads(threads)
-    cores = lib.oracle_num_threads()
-    m = make_mesh(cfg, cfg["sample_n"])
-    o = Oracle(m, cfg["p"], cfg["dt"])
+    lib.oracle_set_assemble_dg(0)
+    o = Oracle(m, cfg["p"], cfg["dt"], timing=True)
     o.make_matrices()
+    lib.oracle_set_assemble_dg(1)
     o.make_rhs(0, 0, 0, 0)
     o.make_rhs(1, 1, 1, 1)
     o.modal_project(0, 0)
     o.modal_project(1, 2)
     o.first_step(0.0)
+    return o, lib.oracle_num_threads()
+
+
+def cpu_sample(cfg, steps=None, warmup=1, target_s=12.0, threads=None):
+    m = oracle_mesh(cfg, cfg["sample_n"])
+    o, cores = oracle_prepared(cfg, m, threads)
     t = cfg["dt"]
     for _ in range(warmup):
         o.step(t)
@@ -237,7 +261,48 @@ def cpu_sample(cfg, steps=None, warmup=1, target_s=12.0, threads=None):
     o.close()
     return {"value": dofs * n / el, "unit": "DOF-steps/s", "cores": cores, "steps": n, "seconds": el,
             "sample": f"{cfg['sample_n']}^3 x 6 = {m.n_tet} tets, {m.n_poly} polyhedra, p={cfg['p']}, "
-                      f"{n} leapfrog steps, assembled blocks + Cholesky solves, FP64, {cores} threads"}
+                      f"{n} leapfrog steps, assembled blocks + Cholesky solves, FP64, {cores} threads; "
+                      f"per DOF-step, extrapolated to the full workload"}
+
+
+def run_reference_arm(cfg, steps, warmup):
+    """The CPU implementation on the whole configured workload: the oracle's
+    set-up, `warmup` steps, then `steps` timed leapfrog steps."""
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    m = oracle_mesh(cfg)
+    t1 = time.perf_counter()
+    o, cores = oracle_prepared(cfg, m, threads)
+    rp, col = o.pattern()
+    t2 = time.perf_counter()
+    log(f"[bench] reference arm: mesh {m.n_tet} tets / {m.n_poly} polyhedra in {t1 - t0:.1f}s; oracle set-up "
+        f"{t2 - t1:.1f}s on {cores} threads, {col.size} blocks")
+    t = cfg["dt"]
+    t, _ = o.run_steps(t, 1e30, warmup)
+    a = time.perf_counter()
+    t, n = o.run_steps(t, 1e30, steps)
+    el = time.perf_counter() - a
+    import resource
+    log(f"[bench] reference arm: {n} steps in {el:.2f}s; peak host memory "
+        f"{resource.getrusage(resource.RUSAGE_SELF).ru_maxrss / 1e6:.1f} GB")
+    out = {"dofs": 3 * o.Np * m.n_poly, "steps": n, "seconds": el, "cores": cores, "n_tet": m.n_tet,
+           "n_poly": m.n_poly, "n_blocks": int(col.size), "Np": o.Np, "setup_s": t2 - t1}
+    o.close()
+    return out
+
+
+def workload_config(cfg, n_tet, n_poly, Np, n_blocks, precision_name, world):
+    """The `config` object of the JSON line, the same for both arms."""
+    nd = 3 * Np
+    fp64_bytes = n_blocks * nd * nd * 8 + n_poly * (3 * nd * 8 + 2 * Np * Np * 8 + 2 * nd * 8)
+    mat = "lognormal lambda, mu per polyhedron (median 1, sigma 0.5, seed 1), rho=1" if cfg["lognormal"] else \
+        f"rho={cfg['material'][0]:g}, lambda={cfg['material'][1]:g}, mu={cfg['material'][2]:g}"
+    return {"workload": f"{cfg['n']}^3x6 tets, BFS polyhedra {cfg['group'][0]}-{cfg['group'][1]} tets "
+                        f"(seed {cfg['seed']}), p={cfg['p']}, {mat}, SIPG alpha=10, dt={cfg['dt']}",
+            "n_tet": n_tet, "n_poly": n_poly, "dofs": 3 * Np * n_poly, "n_blocks": n_blocks,
+            "precision": precision_name,
+            "l2_flush": "inputs larger than L2 (FP64 operator blocks %.1f GB per step)" % (fp64_bytes / 1e9),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 # ---------------------------------------------------------------------------
@@ -577,7 +642,7 @@ def main():
                     help="timed steps (default 200; 2000 for the surrogate configuration c4)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_mf"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison run")
@@ -588,22 +653,28 @@ def main():
         args.steps = 2000 if cfg.get("surrogate") else 200
     info = rank_setup(args)
     metric = "DOF-steps/s (PolyDG elastodynamics leapfrog, 3*Np*N_poly*steps / loop time)"
-    workload = (f"{cfg['n']}^3x6 tets, BFS polyhedra {cfg['group'][0]}-{cfg['group'][1]} tets (seed {cfg['seed']}), "
-                f"p={cfg['p']}, SIPG alpha=10, dt={cfg['dt']}")
 
     if args.impl == "reference":
         if info["rank"] != 0:
             return
-        threads = os.cpu_count()
-        cb = cpu_sample(cfg, steps=args.steps, warmup=args.warmup, threads=threads)
-        line = {"impl": "reference", "metric": metric, "value": cb["value"], "unit": "DOF-steps/s",
-                "n_gpus": args.gpus, "steps": cb["steps"], "warmup": args.warmup,
-                "ms_per_step": 1e3 * cb["seconds"] / cb["steps"], "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated cube mesh, manufactured solution)",
-                "config": {"workload": workload, "sample": cb["sample"], "l2_flush": "not needed (CPU)"},
-                "cpu_baseline": {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",
-                                 "sample": cb["sample"]},
-                "e2e": {"value": cb["value"], "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if cfg.get("ensemble") or cfg.get("surrogate") or cfg.get("mpnn_forward"):
+            print(json.dumps({"impl": "reference", "unavailable": f"config {args.config}: the reference has no "
+                              "batched, learned or network path; its arm times the single-problem configurations"}))
+            return
+        r = run_reference_arm(cfg, args.steps, args.warmup)
+        value = r["dofs"] * r["steps"] / r["seconds"]
+        sample = (f"the whole workload: {r['n_tet']} tets, {r['n_poly']} polyhedra, p={cfg['p']}, {r['steps']} "
+                  f"timed leapfrog steps after {args.warmup}, assembled blocks + Cholesky solves, FP64, "
+                  f"{r['cores']} threads (oracle set-up {r['setup_s']:.0f} s, untimed)")
+        line = {"impl": "reference", "metric": metric, "value": value, "unit": "DOF-steps/s",
+                "n_gpus": args.gpus, "steps": r["steps"], "warmup": args.warmup,
+                "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (generated cube mesh, manufactured solution; no public dataset)",
+                "config": workload_config(cfg, r["n_tet"], r["n_poly"], r["Np"], r["n_blocks"], "fp64", 1),
+                "cpu_baseline": {"value": value, "unit": "DOF-steps/s", "cores": r["cores"], "kind": "port",
+                                 "sample": sample, "host_cpu": host_cpu()},
+                "e2e": {"value": value, "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
 
@@ -696,28 +767,34 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = r["bytes"] / (r["kernel_ms_avg"] / 1e3) / 1e9
     traffic = step_traffic_per_launch(args.config + {0: "", 1: "_mixed", 2: "_mixed_mf"}[precision], r["n_blocks"])
+    fp64_tf = r["flops"] / (r["kernel_ms_avg"] / 1e3) / 1e12
+    hbm = {"achieved_gbs": achieved, "peak_gbs": peak, "frac": achieved / peak, "peak_source": peak_kind,
+           "bytes_per_launch": r["bytes"]}
+    if precision == 0:
+        # the FP64 block kernel keeps the FP64 pipe busy (ncu: 96 %) below the
+        # HBM rate, so its roofline is the FP64 rate
+        roof = {"bound": "fp64", "achieved": fp64_tf, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                "frac": fp64_tf / FP64_NOMINAL_TFLOPS, "traffic": traffic,
+                "peak_source": "nominal GB300 dense FP64 (152 SMs x 2 FMA/clock x 2.07 GHz); no measured FP64 "
+                               "figure exists for this pool, and the library's FMA-chain probe (fp64_probe_tflops) "
+                               "measures less than the kernel itself",
+                "flops_per_launch": r["flops"], "kernel_ms": r["kernel_ms_avg"], "hbm": hbm,
+                "fp64_probe_tflops": fp64_peak()}
+    else:
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_kind, "bytes_per_launch": r["bytes"],
+                "kernel_ms": r["kernel_ms_avg"]}
     line = {
         "metric": metric, "value": value, "unit": "DOF-steps/s", "n_gpus": info["world"], "steps": r["steps"],
         "warmup": args.warmup, "ms_per_step": r["ms"] / r["steps"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[precision],
         "data": "synthetic (generated cube mesh, manufactured solution; no public dataset)",
-        "config": {"workload": workload, "n_tet": r["n_tet"], "n_poly": r["n_poly"], "dofs": r["dofs"],
-                   "n_blocks": r["n_blocks"], "precision": args.precision,
-                   "l2_flush": "inputs larger than L2 (operator blocks %.1f GB per step)" % (r["bytes"] / 1e9),
-                   "parallelism": "replicas" if info["world"] > 1 else "single GPU"},
+        "config": workload_config(cfg, r["n_tet"], r["n_poly"], r["Np"], r["n_blocks"], args.precision, info["world"]),
         "err_L2": r["err_L2"], "err_DG": r["err_DG"], "error_after_steps": r["error_steps"],
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_kind,
-                     "bytes_per_launch": r["bytes"], "kernel_ms": r["kernel_ms_avg"],
-                     "fp64_tflops": r["flops"] / (r["kernel_ms_avg"] / 1e3) / 1e12,
-                     "fp64_peak_tflops": FP64_NOMINAL_TFLOPS,
-                     "fp64_peak_source": "nominal GB300 dense FP64 (the probe below measures less than the kernel)",
-                     "fp64_probe_tflops": fp64_peak()},
+        "roofline": roof,
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
     }
-    rf = line["roofline"]
-    rf["fp64_frac"] = rf["fp64_tflops"] / rf["fp64_peak_tflops"]
     if "e2e" in r:
         e = r["e2e"]
         line["e2e"] = {"value": info["sum"](e["value"]), "unit": "DOF-steps/s",
@@ -730,10 +807,11 @@ def main():
         # the same sample on one thread (a shorter run), and what the host is
         c1 = cpu_sample(cfg, target_s=5.0, threads=1)
         from oracle.oracle_py import load as oracle_load
-        oracle_load().oracle_set_threads(cores_all)
+        oracle_load(timing=True).oracle_set_threads(cores_all)
         line["cpu_baseline"] = {"value": cb["value"], "unit": "DOF-steps/s", "cores": cb["cores"], "kind": "port",
                                 "sample": cb["sample"], "single_thread_value": c1["value"],
-                                "host_cpu": host_cpu(), "nproc": cores_all}
+                                "host_cpu": host_cpu(), "nproc": cores_all,
+                                "build": "oracle/_build/liblymph_oracle_timing.so (-O3, OpenMP over polyhedra)"}
     if info["rank"] == 0 and precision == 0 and not args.no_mixed:
         for key, prec in (("mixed", 1), ("mixed_mf", 2)):
             rm = run_gpu(cfg, prec, args.steps, args.warmup, {**info, "barrier": lambda: None, "max": lambda x: x},

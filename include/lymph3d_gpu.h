@@ -5,8 +5,10 @@
  * (src/matrix_free.f90).  Every entry point below replaces one subroutine the
  * Fortran driver src/Lymph3D.f90 calls; the citation next to each declaration
  * names the reference interface it stands for.  All arguments are plain C
- * types and host pointers; no device pointer, torch type or C++ type crosses
- * this boundary.  Device memory, streams and kernels live behind the opaque
+ * types and pointers; no torch type or C++ type crosses this boundary.  Data
+ * pointers are host pointers, with one exception: lymph_error_l2_noalloc
+ * takes device pointers to the caller's own device arrays.  Everything else
+ * in device memory, the streams and the kernels live behind the opaque
  * context handle.
  *
  * Conventions
@@ -260,10 +262,16 @@ int lymph_error_dg(lymph_ctx* ctx, int slot_uh, int slot_uex, double* sumsq);
  * (2 MiB) that every GPU loading the library holds until the process exits;
  * n_poly above 262,144 is rejected with LYMPH_ERR_INVALID.  The first call on
  * a device looks up the array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture.  Kernels run on the legacy
- * default stream and the result is copied back synchronously.  All calls
- * share the one array: calls that overlap on the GPU (from several host
- * threads, or concurrently with other work on the same device array) race. */
+ * make that first call before any stream capture.  With lazy module loading
+ * (CUDA_MODULE_LOADING=LAZY, the CUDA default) that first call is also when
+ * the 2 MiB are allocated on the device, so a caller that fills device
+ * memory to a cap should make it before doing so.  The address is cached
+ * per device ordinal for the life of the process: after a cudaDeviceReset
+ * the cached address is stale, so do not call this again in that process.
+ * Kernels run on the legacy default stream and the result is copied back
+ * synchronously.  All calls share the one array: calls that overlap on the
+ * GPU (from several host threads, or concurrently with other work on the
+ * same device array) race. */
 int lymph_error_l2_noalloc(const double* d_mass_modal, const double* d_uh, const double* d_uex, int32_t n_poly,
                            int32_t Np, double* sumsq);
 

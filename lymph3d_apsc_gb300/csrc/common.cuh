@@ -199,5 +199,48 @@ __host__ __device__ inline void basis_eval(const double pt[3], const double* bb,
 
 inline int np_of(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }
 
+// ---------------------------------------------------------------------------
+// the L2-norm bodies shared by the context path (step.cu) and the
+// allocation-free entry point (noalloc.cu), so both give the same bits
+// ---------------------------------------------------------------------------
+// COMPUTE_ERROR_L2_MATRIX_FREE's body for polyhedron P
+// (src/matrix_free.f90:1388-1418): sum_i du_i^T M du_i with du = uh - uex,
+// M the Np x Np modal mass matrix, rows and columns in the reference's order.
+__device__ __forceinline__ double l2_partial_poly(int P, int NP, const double* __restrict__ Mm,
+                                                  const double* __restrict__ uh, const double* __restrict__ uex) {
+    const int ND = 3 * NP;
+    double err = 0.0;
+    const double* M = Mm + (int64_t)P * NP * NP;
+    for (int i = 0; i < 3; ++i) {
+        double e = 0.0;
+        for (int rr = 0; rr < NP; ++rr) {
+            double t = 0.0;
+            for (int c = 0; c < NP; ++c) {
+                const int64_t qc = (int64_t)P * ND + i * NP + c;
+                t = t + M[rr * NP + c] * (uh[qc] - uex[qc]);
+            }
+            const int64_t qr = (int64_t)P * ND + i * NP + rr;
+            e = e + (uh[qr] - uex[qr]) * t;
+        }
+        err = err + e;
+    }
+    return err;
+}
+
+// Deterministic sum of v[0..n) by one CTA of 1024 threads: a fixed strided
+// order per thread, then a fixed shared-memory tree; thread 0 writes *out.
+__device__ __forceinline__ void sum_fixed_order_1024(int64_t n, const double* __restrict__ v, double* out) {
+    __shared__ double red[1024];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += v[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
 // launch helpers (defined in abi.cu)
 int lymph_sync_status(lymph_ctx* c, const char* where);

@@ -36,38 +36,12 @@ __global__ void k_l2_partial(int n_poly, int NP, const double* __restrict__ Mm, 
                              const double* __restrict__ uex, double* partial) {
     const int P = blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= n_poly) return;
-    const int ND = 3 * NP;
-    double err = 0.0;
-    const double* M = Mm + (int64_t)P * NP * NP;
-    for (int i = 0; i < 3; ++i) {
-        double e = 0.0;
-        for (int rr = 0; rr < NP; ++rr) {
-            double t = 0.0;
-            for (int c = 0; c < NP; ++c) {
-                const int64_t qc = (int64_t)P * ND + i * NP + c;
-                t = t + M[rr * NP + c] * (uh[qc] - uex[qc]);
-            }
-            const int64_t qr = (int64_t)P * ND + i * NP + rr;
-            e = e + (uh[qr] - uex[qr]) * t;
-        }
-        err = err + e;
-    }
-    partial[P] = err;
+    partial[P] = l2_partial_poly(P, NP, Mm, uh, uex);
 }
 
-// Deterministic sum of n values: fixed per-thread strided order, then a
-// fixed shared-memory tree.
-__global__ void k_sum(int64_t n, const double* __restrict__ v, double* out) {
-    __shared__ double red[1024];
-    double s = 0.0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += v[i];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *out = red[0];
+// Deterministic sum of n values (one CTA of 1024 threads).
+__global__ void __launch_bounds__(1024) k_sum(int64_t n, const double* __restrict__ v, double* out) {
+    sum_fixed_order_1024(n, v, out);
 }
 
 // Sum of squares of v into *out (one CTA, fixed order).

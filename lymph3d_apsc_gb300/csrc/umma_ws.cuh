@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
     uint64_t* acc = empty + WS_STAGES;
     uint32_t* tmem_slot = (uint32_t*)(acc + 1);
     __shared__ int s_abort;
+    __shared__ int s_issued[WS_STAGES];  // per stage the last k-step whose TMA loads were issued (-1: none)
     const int t = threadIdx.x, warp = t / 32, lane = t % 32;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * WS_BN;
     const int nb = (a.Npad - n0) < WS_BN ? (a.Npad - n0) : WS_BN;  // this CTA's columns (multiple of 16)
@@ -112,6 +113,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
 
     if (t == 0) {
         s_abort = 0;
+        for (int s = 0; s < WS_STAGES; ++s) s_issued[s] = -1;
         for (int s = 0; s < WS_STAGES; ++s) {
             mbar_init(smem_u32(&full[s]), 1);
             mbar_init(smem_u32(&split[s]), WS_SPLIT);
@@ -144,6 +146,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
                     mbar_expect_tx(smem_u32(&full[st]), bytes);
                     tma_load_2d(sp, &a.mapA[sg], k0, m0, smem_u32(&full[st]));
                     tma_load_2d(sp + 2 * (uint32_t)WS_TILE_A, &a.mapB, koff + k0, n0, smem_u32(&full[st]));
+                    ((volatile int*)s_issued)[st] = kt;
                 }
                 koff += a.segK[sg];
             }
@@ -256,12 +259,18 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
         }
     }
     // teardown: after an abort, let the work in flight finish (bounded) before
-    // the tensor memory and the shared memory go away
+    // the tensor memory and the shared memory go away: the MMAs (the "acc"
+    // commit, issued after the MMA loop however it ended) and the last TMA
+    // loads of every stage (no later load was issued on a stage, so the
+    // phase of its last one is the one still pending, if any)
     __syncthreads();
     if (t == 0 && *abort) {
         atomicOr(a.status, 1);
         mbar_wait(smem_u32(acc), 0u);
-        for (int s = 0; s < WS_STAGES; ++s) mbar_try_wait(smem_u32(&full[s]), 0u);
+        for (int s = 0; s < WS_STAGES; ++s) {
+            const int kt = ((volatile int*)s_issued)[s];
+            if (kt >= 0) mbar_wait(smem_u32(&full[s]), (uint32_t)((kt / WS_STAGES) & 1));
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();

@@ -81,6 +81,11 @@ int g_explicit_inverse = 0;
 // 3 drops the consistency term, 4 drops the last shared triangle of the pair.
 int g_planted_mistake = 0;
 
+// When 0, MAKE_MATRICES_FREE skips the A_dg blocks (the DG-norm operator): the
+// timed CPU runs of the benchmark need only K, and at 46,767 polyhedra and
+// p = 4 each operator holds 44 GB.  COMPUTE_ERROR_DG then reports an error.
+int g_assemble_dg = 1;
+
 double perturb(double v, const double p[3], int comp) {
     if (g_perturb_ulps == 0 || v == 0.0) return v;
     uint64_t h = 1469598103934665603ull ^ (uint64_t)comp;
@@ -504,6 +509,7 @@ struct Oracle {
     std::vector<double> rhs_stat, rhs_dyn;    // [n_poly][nd]
     std::vector<double> slot[4];              // [n_poly][nd]
     bool have_matrices = false;
+    bool have_dg = false;      // A_dg assembled (g_assemble_dg when the matrices were made)
     int status = 0;
 };
 
@@ -759,7 +765,7 @@ int block_of(Oracle& o, int P, int Qp) {
         if (v[b] == Qp) return (int)b;
     v.push_back(Qp);
     o.K[P].resize(v.size() * o.nd * o.nd, 0.0);
-    o.A[P].resize(v.size() * o.nd * o.nd, 0.0);
+    if (o.have_dg) o.A[P].resize(v.size() * o.nd * o.nd, 0.0);
     return (int)v.size() - 1;
 }
 
@@ -772,11 +778,14 @@ int make_matrices(Oracle& o) {
     o.A.assign(o.n_poly, std::vector<double>());
     o.M.assign((size_t)o.n_poly * N2, 0.0); o.Mm.assign((size_t)o.n_poly * N2, 0.0);
     o.R.assign((size_t)o.n_poly * N2, 0.0); o.Rm.assign((size_t)o.n_poly * N2, 0.0);
+    o.have_dg = g_assemble_dg != 0;
+    const bool dg = o.have_dg;
     int bad = 0;
 #pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
     for (int P = 0; P < o.n_poly; ++P) {
         o.nbr[P].push_back(P);
-        o.K[P].assign(nd * nd, 0.0); o.A[P].assign(nd * nd, 0.0);
+        o.K[P].assign(nd * nd, 0.0);
+        if (dg) o.A[P].assign(nd * nd, 0.0);
         std::vector<double> phi, dphi, V, Mv, phib, gradb;
         FaceMats F;
         for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1]; ++k) {
@@ -796,7 +805,7 @@ int make_matrices(Oracle& o) {
                         for (int n = 0; n < Np; ++n) {
                             double v = V[((i * 3 + j) * Np + m) * Np + n];
                             o.K[P][(i * Np + m) * nd + j * Np + n] += v;
-                            o.A[P][(i * Np + m) * nd + j * Np + n] += v;
+                            if (dg) o.A[P][(i * Np + m) * nd + j * Np + n] += v;
                         }
             for (int f = 0; f < 4; ++f) {
                 int E2 = o.neigh[t * 4 + f];
@@ -812,14 +821,14 @@ int make_matrices(Oracle& o) {
                 stiffness_face(o.alpha, o.p, Np, E2, o.hk[P], hk2, nn, o.area[t * 4 + f], o.Q, lambda, mu, phib, gradb, F);
                 auto IDX = [&](int i, int j, int m, int n) { return ((i * 3 + j) * Np + m) * Np + n; };
                 double* K1 = &o.K[P][0];
-                double* A1 = &o.A[P][0];
+                double* A1 = dg ? &o.A[P][0] : nullptr;
                 for (int i = 0; i < 3; ++i)
                     for (int j = 0; j < 3; ++j)
                         for (int m = 0; m < Np; ++m)
                             for (int n = 0; n < Np; ++n) {
                                 int rc = (i * Np + m) * nd + j * Np + n;
                                 K1[rc] += F.S1[IDX(i, j, m, n)];
-                                A1[rc] += F.S1[IDX(i, j, m, n)];
+                                if (dg) A1[rc] += F.S1[IDX(i, j, m, n)];
                             }
                 if (E2 == BC_DIRI) {
                     for (int i = 0; i < 3; ++i)
@@ -833,7 +842,7 @@ int make_matrices(Oracle& o) {
                     int b = block_of(o, P, Qp);
                     K1 = &o.K[P][0];
                     double* Kb = &o.K[P][(size_t)b * nd * nd];
-                    double* Ab = &o.A[P][(size_t)b * nd * nd];
+                    double* Ab = dg ? &o.A[P][(size_t)b * nd * nd] : nullptr;
                     for (int i = 0; i < 3; ++i)
                         for (int j = 0; j < 3; ++j)
                             for (int m = 0; m < Np; ++m)
@@ -841,7 +850,7 @@ int make_matrices(Oracle& o) {
                                     int rc = (i * Np + m) * nd + j * Np + n;
                                     K1[rc] = K1[rc] + o.theta * F.I1[IDX(i, j, m, n)] - F.I1[IDX(j, i, n, m)];
                                     Kb[rc] = Kb[rc] + o.theta * F.I2[IDX(i, j, m, n)] + F.S2[IDX(i, j, m, n)];
-                                    Ab[rc] = Ab[rc] + F.S2[IDX(i, j, m, n)];
+                                    if (dg) Ab[rc] = Ab[rc] + F.S2[IDX(i, j, m, n)];
                                     Kb[rc] = Kb[rc] - F.IT2[IDX(i, j, m, n)];
                                 }
                 }
@@ -1179,6 +1188,8 @@ void oracle_set_device_order(int slices) { g_device_order = slices > 0 ? slices 
 
 void oracle_set_planted_mistake(int kind) { g_planted_mistake = kind; }
 
+void oracle_set_assemble_dg(int on) { g_assemble_dg = on; }
+
 int oracle_num_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();
@@ -1336,6 +1347,7 @@ int oracle_error_l2(void* h, int s_uh, int s_uex, double* out) {
 // COMPUTE_ERROR_DG_MATRIX_FREE, matrix_free.f90:1421-1504.
 int oracle_error_dg(void* h, int s_uh, int s_uex, double* out) {
     Oracle& o = *(Oracle*)h;
+    if (!o.have_dg) { g_err = "oracle: the A_dg blocks were not assembled"; return LYMPH_ERR_ORDER; }
     int nd = o.nd;
     std::vector<double> du(o.slot[s_uh].size());
     for (size_t k = 0; k < du.size(); ++k) du[k] = o.slot[s_uh][k] - o.slot[s_uex][k];
@@ -1493,6 +1505,7 @@ int oracle_get_pattern(void* h, int32_t* row_ptr, int32_t* col, int64_t* n_block
 
 int oracle_get_blocks(void* h, int which, double* vals) {
     Oracle& o = *(Oracle*)h;
+    if (which != LYMPH_BLOCKS_K && !o.have_dg) { g_err = "oracle: the A_dg blocks were not assembled"; return LYMPH_ERR_ORDER; }
     size_t off = 0, bs = (size_t)o.nd * o.nd;
     for (int P = 0; P < o.n_poly; ++P) {
         const std::vector<double>& src = (which == LYMPH_BLOCKS_K) ? o.K[P] : o.A[P];
@@ -1529,6 +1542,7 @@ int oracle_get_poly_geometry(void* h, double* bbox, double* hk) {
 int oracle_get_kloc_reference_layout(void* h, int which, double* out) {
     Oracle& o = *(Oracle*)h;
     if (o.n_poly != o.n_tet) { g_err = "reference layout needs one tet per polyhedron"; return LYMPH_ERR_INVALID; }
+    if (which != LYMPH_BLOCKS_K && !o.have_dg) { g_err = "oracle: the A_dg blocks were not assembled"; return LYMPH_ERR_ORDER; }
     int nd = o.nd;
     size_t ne = o.n_poly;
     std::fill(out, out + 5 * (size_t)nd * nd * ne, 0.0);

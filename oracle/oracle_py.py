@@ -15,22 +15,28 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liblymph_oracle.so"
+# the same source built -O3 with FMA contraction: the timed CPU runs only
+LIB_TIMING = HERE / "_build" / "liblymph_oracle_timing.so"
 
-_lib = None
+_libs = {}
 
 
 def build() -> Path:
     src = HERE / "lymph_oracle.cpp"
-    if not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+    hdr = HERE.parent / "include" / "lymph3d_gpu.h"
+    newest = max(src.stat().st_mtime, hdr.stat().st_mtime)
+    if any(not p.exists() or p.stat().st_mtime < newest for p in (LIB, LIB_TIMING)):
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB
 
 
-def load():
-    global _lib
-    if _lib is None:
+def load(timing: bool = False):
+    """The checker library (FP contraction off), or with timing=True the
+    -O3 build used only to time the CPU baseline."""
+    key = "timing" if timing else "parity"
+    if key not in _libs:
         build()
-        lib = ctypes.CDLL(str(LIB))
+        lib = ctypes.CDLL(str(LIB_TIMING if timing else LIB))
         P_I32, P_F64 = POINTER(c_int32), POINTER(c_double)
         sigs = {
             "oracle_last_error": (c_char_p, []),
@@ -40,6 +46,7 @@ def load():
             "oracle_set_explicit_inverse": (None, [c_int]),
             "oracle_set_device_order": (None, [c_int]),
             "oracle_set_planted_mistake": (None, [c_int]),
+            "oracle_set_assemble_dg": (None, [c_int]),
             "oracle_set_threads": (None, [c_int]),
             "oracle_create": (c_int, [c_void_p, c_int, c_double, c_double, c_double, POINTER(c_void_p)]),
             "oracle_destroy": (c_int, [c_void_p]),
@@ -77,8 +84,8 @@ def load():
             f = getattr(lib, k)
             f.restype = r
             f.argtypes = a
-        _lib = lib
-    return _lib
+        _libs[key] = lib
+    return _libs[key]
 
 
 def _p(a, t=c_double):
@@ -88,8 +95,8 @@ def _p(a, t=c_double):
 class Oracle:
     """CPU FP64 restatement of the reference path for one problem."""
 
-    def __init__(self, mesh, degree: int, dt: float, alpha: float = 10.0, theta: float = -1.0):
-        self.lib = load()
+    def __init__(self, mesh, degree: int, dt: float, alpha: float = 10.0, theta: float = -1.0, timing: bool = False):
+        self.lib = load(timing)
         self.mesh = mesh
         self._desc = mesh.desc()
         h = c_void_p()

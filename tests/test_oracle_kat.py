@@ -292,3 +292,26 @@ def test_c0_golden_driver():
     assert r["n_steps"] == gold["n_steps"] == 1000 and r["t"] == gold["t_final"]
     assert abs(r["err_L2"] - gold["err_L2"]) <= 1e-12 * gold["err_L2"]
     assert abs(r["err_DG"] - gold["err_DG"]) <= 1e-12 * gold["err_DG"]
+
+
+@pytest.mark.parametrize("n,bc,agg,seed,group", [(3, "dirichlet", "bfs", 0, (4, 12)), (4, "reference", "bfs", 3, (4, 16)),
+                                                 (5, "reference", "hex", 0, (6, 6)), (2, "dirichlet", "tet", 0, (1, 1))])
+def test_oracle_mesh_builder_equals_the_library(n, bc, agg, seed, group):
+    """oracle/mesh_py.py (the meshes of the CPU reference arm, built without
+    the GPU library) gives the library's arrays bit for bit."""
+    from oracle import mesh_py as MP
+    a = M.cube(n, bc=bc, agglomeration=agg, seed=seed, group=group)
+    b = MP.cube(n, bc=bc, agglomeration=agg, seed=seed, group=group)
+    for k in ("coords", "tet_vert", "tet_poly", "tet_mat", "neigh", "fun_tag", "mat"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    m0 = M.cube(n, bc=bc, agglomeration=agg, seed=seed, group=group)
+    c = M.cube(n, bc=bc, agglomeration=agg, seed=seed, group=group,
+               poly_materials=M.lognormal_materials(m0.n_poly, seed=1))
+    d = MP.cube(n, bc=bc, agglomeration=agg, seed=seed, group=group, lognormal_seed=1)
+    assert np.array_equal(c.mat, d.mat) and np.array_equal(c.tet_mat, d.tet_mat)
+
+
+def test_oracle_mesh_builder_reproduces_the_benchmark_grouping():
+    from oracle import mesh_py as MP
+    b = MP.cube(40, bc="dirichlet", agglomeration="bfs", seed=0, group=(4, 12))
+    assert np.array_equal(b.tet_poly, np.load(GOLDEN / "elem_in_poly.npz")["c1"])

@@ -5,10 +5,10 @@ It is meant for callers that cannot allocate device memory when they need
 the norm.  The test gives it device copies of a real problem's modal mass
 matrices and coefficients (allocated here by the test through the CUDA
 runtime, as such a caller would hold them) and checks that two calls in a
-row agree with the context path lymph_error_l2 on the same data, within
-the relative 1e-13 this file uses (both paths run the same arithmetic in the
-same order, so they agree to the last bit in practice).  It also checks the
-size limit.  The file is named to be collected last.
+row agree with the context path lymph_error_l2 on the same data: both
+paths call the same device functions (the per-polyhedron body and the
+fixed-order sum in common.cuh), so they must agree to the last bit.  It also
+checks the size limit.  The file is named to be collected last.
 """
 import ctypes
 import glob
@@ -20,8 +20,6 @@ import pytest
 from lymph3d_apsc_gb300 import MatrixFree, _lib, mesh as M
 
 pytestmark = pytest.mark.gpu
-
-TOL = 1e-13
 
 
 def _cudart():
@@ -72,7 +70,7 @@ def test_noalloc_l2_matches_context_path_twice(require_gpu, p):
             out = c_double(-1.0)
             rc = lib.lymph_error_l2_noalloc(bufs[0].ptr, bufs[1].ptr, bufs[2].ptr, n_poly, Np, byref(out))
             assert rc == 0, lib.lymph_last_error()
-            assert expected > 0 and abs(out.value - expected) <= TOL * expected, (out.value, expected)
+            assert expected > 0 and out.value == expected, (out.value, expected)
         # sizes beyond the static scratch are refused with a message
         out = c_double()
         rc = lib.lymph_error_l2_noalloc(bufs[0].ptr, bufs[1].ptr, bufs[2].ptr, 262145, Np, byref(out))
