@@ -4,7 +4,10 @@
 EXPORT_SOLUTION, src/solution_processing.f90:62-194, on the device); the
 writers restate the formats of src/export_file_formats.f90 in host code:
 legacy ASCII VTK (VTK_WRITE_SOLUTION :16-212), VTU mesh + solution files
-(VTU_WRITE_SOLUTION :257-480) and the PVD collection (PVD_SETUP :215-251).
+(VTU_WRITE_SOLUTION :257-480), the PVD collection (PVD_SETUP :215-251) and
+the EnSight Gold ASCII set (ENSIGHT_WRITE_MESH :580-686,
+ENSIGHT_WRITE_BOUNDARY :688-822, ENSIGHT_WRITE_SOLUTION :824-905,
+ENSIGHT_WRITE_CASE :907-988).
 Like the reference, every tetrahedron gets its own four points (the field
 is discontinuous across elements), cells are VTK_TETRA (10), and the cell
 data carry the polyhedron index of each tetrahedron (1-based, as the
@@ -106,6 +109,146 @@ def write_pvd(directory, steps) -> Path:
             f.write(f'    <DataSet timestep="{s}" part="1" file="solution_{s}.vtu"/>\n')
         f.write("  </Collection>\n</VTKFile>\n")
     return p
+
+
+# ---------------------------------------------------------------------------
+# EnSight Gold, ASCII (fixed-width fields: floats E12.5, integers I10)
+# ---------------------------------------------------------------------------
+def _e12(values) -> str:
+    """One E12.5 field per line, the EnSight ASCII float format."""
+    return "".join(f"{v:12.5E}\n" for v in np.asarray(values, np.float64).ravel())
+
+
+def _i10(values) -> str:
+    return "".join(f"{int(v):10d}\n" for v in np.asarray(values).ravel())
+
+
+def write_ensight_mesh(directory, mesh: Mesh):
+    """mesh.geo (one part of tetra4 cells, every tetrahedron with its own four
+    nodes, numbered 1..4 n_tet) and poly.sca (the polyhedron index of each
+    tetrahedron, 1-based, as a per-element scalar): ENSIGHT_WRITE_MESH.  The
+    node and element ids are written and declared "given" (the reference
+    lists ids under "assign", where EnSight readers expect none).  Returns
+    the paths written."""
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    n = mesh.n_tet
+    pts = _points(mesh)
+    geo = d / "mesh.geo"
+    with open(geo, "w") as f:
+        f.write("Ensight Gold\nUnstructured mesh part\nnode id given\nelement id given\n")
+        f.write(f"part\n{1:10d}\nStatic mesh file\ncoordinates\n{4 * n:10d}\n")
+        f.write(_i10(np.arange(1, 4 * n + 1)))
+        for k in range(3):
+            f.write(_e12(pts[:, k]))
+        f.write(f"tetra4\n{n:10d}\n")
+        f.write(_i10(np.arange(1, n + 1)))
+        conn = np.arange(1, 4 * n + 1).reshape(n, 4)
+        f.write("".join("".join(f"{v:10d}" for v in row) + "\n" for row in conn))
+    sca = d / "poly.sca"
+    with open(sca, "w") as f:
+        f.write(f"scalar per element\npart\n{1:10d}\ntetra4\n")
+        f.write(_e12(mesh.tet_poly + 1))
+    return [geo, sca]
+
+
+def write_ensight_boundary(directory, mesh: Mesh):
+    """boundaries.geo (every boundary triangle, tria3, with its own three
+    nodes), boundaries_tag.sca (the triangle's boundary tag from the mesh
+    file, as a per-element scalar) and boundaries.case tying them together:
+    ENSIGHT_WRITE_BOUNDARY.  Returns the paths written."""
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    t, f_ = np.nonzero(mesh.neigh < 0)
+    face_v = np.array([[0, 1, 2], [0, 1, 3], [1, 2, 3], [2, 0, 3]])  # MAKE_PARTITION_AND_MPI_FILES.f90:1087-1096
+    tri = mesh.tet_vert[t[:, None], face_v[f_]]
+    pts = mesh.coords[tri].reshape(-1, 3)
+    nb = int(t.size)
+    if mesh.face_tag is not None:
+        tags = mesh.face_tag[t, f_]
+    else:
+        tags = -mesh.neigh[t, f_]
+    geo = d / "boundaries.geo"
+    with open(geo, "w") as f:
+        f.write("Ensight Gold\nUnstructured mesh part\nnode id given\nelement id given\n")
+        f.write(f"part\n{1:10d}\nboundary faces\ncoordinates\n{3 * nb:10d}\n")
+        f.write(_i10(np.arange(1, 3 * nb + 1)))
+        for k in range(3):
+            f.write(_e12(pts[:, k]))
+        f.write(f"tria3\n{nb:10d}\n")
+        f.write(_i10(np.arange(1, nb + 1)))
+        conn = np.arange(1, 3 * nb + 1).reshape(nb, 3)
+        f.write("".join("".join(f"{v:10d}" for v in row) + "\n" for row in conn))
+    sca = d / "boundaries_tag.sca"
+    with open(sca, "w") as f:
+        f.write(f"scalar per element\npart\n{1:10d}\ntria3\n")
+        f.write(_e12(tags))
+    case = d / "boundaries.case"
+    case.write_text("FORMAT\ntype: ensight gold\nGEOMETRY\nmodel: boundaries.geo\nVARIABLE\n"
+                    "scalar per element: tag boundaries_tag.sca\n")
+    return [geo, sca, case]
+
+
+def write_ensight_solution(directory, u_nod: np.ndarray, step: int, name: str = "u") -> Path:
+    """sol_tet_<step, 6 digits>.vec: the nodal vectors of every tetrahedron's
+    four nodes, x components, then y, then z (ENSIGHT_WRITE_SOLUTION)."""
+    if not 0 <= step < 1000000:
+        raise ValueError("step must fit the six-digit file number")
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    u = np.asarray(u_nod, np.float64).reshape(-1, 3)
+    p = d / f"sol_tet_{step:06d}.vec"
+    with open(p, "w") as f:
+        f.write(f"vector per node\npart\n{1:10d}\ncoordinates\n")
+        for k in range(3):
+            f.write(_e12(u[:, k]))
+    return p
+
+
+def write_ensight_case(directory, dt: float, stop_time: float, increment: int, name: str = "u") -> Path:
+    """solution.case: the mesh, the nodal vector u in sol_tet_******.vec
+    every `increment` steps from step 0, the per-element polyhedron index,
+    and the time values (ENSIGHT_WRITE_CASE: floor(stop_time / dt) /
+    increment + 1 steps at times i * increment * dt)."""
+    d = Path(directory)
+    d.mkdir(parents=True, exist_ok=True)
+    nsteps = int(np.floor(stop_time / dt)) // increment + 1
+    times = [i * increment * dt for i in range(nsteps)]
+    lines = ["FORMAT", "type: ensight gold", "GEOMETRY", "model: mesh.geo", "VARIABLE",
+             f"vector per node: {1:10d} {name} sol_tet_******.vec", f"scalar per element: {1:10d} poly poly.sca",
+             "TIME", f"time set: {1:10d}", f"number of steps: {nsteps:10d}", f"filename start number: {0:10d}",
+             f"filename increment: {increment:10d}", "time values:"]
+    for i in range(0, nsteps, 10):
+        lines.append("".join(f"{t:12.5E}" for t in times[i:i + 10]))
+    p = d / "solution.case"
+    p.write_text("\n".join(lines) + "\n")
+    return p
+
+
+def read_ensight_geo(path):
+    """(node coordinates [n, 3], connectivity [n_cells, k] 1-based, cell
+    type) of a one-part file written by write_ensight_mesh /
+    write_ensight_boundary (for tests and tools)."""
+    lines = Path(path).read_text().splitlines()
+    i = lines.index("coordinates")
+    nn = int(lines[i + 1])
+    ids_given = lines[2].strip() == "node id given"
+    o = i + 2 + (nn if ids_given else 0)
+    xyz = np.array([[float(lines[o + k * nn + j][:12]) for k in range(3)] for j in range(nn)])
+    j = o + 3 * nn
+    ctype, nc = lines[j].strip(), int(lines[j + 1])
+    o = j + 2 + (nc if lines[3].strip() == "element id given" else 0)
+    w = {"tetra4": 4, "tria3": 3}[ctype]
+    conn = np.array([[int(lines[o + c][10 * q:10 * q + 10]) for q in range(w)] for c in range(nc)])
+    return xyz, conn, ctype
+
+
+def read_ensight_values(path, ncomp: int = 1):
+    """The values of a per-node vector or per-element scalar file, shape
+    [n, ncomp]."""
+    lines = Path(path).read_text().splitlines()
+    vals = np.array([float(ln[:12]) for ln in lines[4:]])
+    return vals.reshape(ncomp, -1).T
 
 
 def read_vtk_point_vectors(path) -> np.ndarray:
