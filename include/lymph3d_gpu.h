@@ -51,10 +51,22 @@ extern "C" {
 #define LYMPH_ERR_TIMEOUT            104   /* a bounded device-side wait expired */
 #define LYMPH_ERR_INDEX              105   /* device-side index check failed */
 
-/* ---- boundary markers in lymph_mesh_desc.neigh (BC_DIRI / BC_NEUM,
- *      src/Poly_global.f90:420-421) ------------------------------------- */
+/* ---- boundary markers in lymph_mesh_desc.neigh (BC_DIRI / BC_NEUM /
+ *      BC_ABSO, src/Poly_global.f90:420-422) ----------------------------- */
 #define LYMPH_BC_DIRI (-1)
 #define LYMPH_BC_NEUM (-2)
+/* Absorbing face: no stiffness or load term (traction-free like a Neumann
+ * face), plus the damping block of MAKE_DAMPING_FACE
+ * (src/assemble_element.f90:666-731) on its polyhedron,
+ *   D_P[(i,m),(j,n)] = sum_q w_q |face| phi_m phi_n (c_t (t1_i t1_j + t2_i t2_j) + c_n n_i n_j),
+ * with the first-order impedances c_t = rho c_s = sqrt(rho mu) and
+ * c_n = rho c_p = sqrt(rho (lambda + 2 mu)) of the face's tetrahedron (the
+ * reference's c1, c2, c3; its matrix-free path leaves the call commented
+ * out, src/matrix_free.f90:279-287).  The leapfrog step then solves
+ *   (M + dt/2 D) u^{n+1} = dt^2 (F - K u^n) + 2 M u^n - (M - dt/2 D) u^{n-1}
+ * on polyhedra with absorbing faces, and the first step subtracts D v^0 from
+ * the load. */
+#define LYMPH_BC_ABSO (-3)
 
 /* ---- precision of the operator apply ----------------------------------- */
 #define LYMPH_FP64   0   /* every operation in FP64 (the plain path) */
@@ -127,7 +139,7 @@ typedef struct lymph_mesh_desc {
     const int32_t* tet_poly;  /* [n_tet] polyhedron id (elem_in_poly)          */
     const int32_t* tet_mat;   /* [n_tet] material id (Elem_loc%mat_prop)       */
     const int32_t* neigh;     /* [n_tet][4] tet across face f, or LYMPH_BC_DIRI /
-                                 LYMPH_BC_NEUM (neigh_el(f,2)); face f joins
+                                 LYMPH_BC_NEUM / LYMPH_BC_ABSO (neigh_el(f,2)); face f joins
                                  vertices {1,2,3},{1,2,4},{2,3,4},{3,1,4}
                                  (1-based, MAKE_PARTITION_AND_MPI_FILES.f90:1087-1096) */
     const int32_t* fun_tag;   /* [n_tet][4] boundary space-function tag

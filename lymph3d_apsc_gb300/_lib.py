@@ -30,6 +30,7 @@ LYMPH_ERR_INDEX = 105
 
 BC_DIRI = -1
 BC_NEUM = -2
+BC_ABSO = -3  # absorbing: no stiffness or load term, a damping block on its polyhedron
 MESH_UNMATCHED = -9
 
 FP64 = 0

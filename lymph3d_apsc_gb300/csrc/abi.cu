@@ -24,6 +24,7 @@ int lymph_dev_assemble_list(lymph_ctx* c, int which, void* out, int out_fp32, bo
                             int64_t n_list, int64_t out_stride);
 int lymph_mf_setup(lymph_ctx* c, const RefTables& R);
 int lymph_dev_cholesky(lymph_ctx* c);
+int lymph_dev_damping(lymph_ctx* c, bool assemble);
 int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scale, double* out);
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
@@ -278,6 +279,9 @@ int lymph_destroy(lymph_ctx* c) {
                     c->d_mf_tri, c->d_mf_poly, c->d_mf_u32, c->d_mf_range, c->d_layout};
     for (void* p : ptrs) dfree(p);
     dfree(c->d_layout2);
+    void* absp[] = {c->d_abs_idx, c->d_abs_poly, c->d_abs_ptr, c->d_abs_faces, c->d_Dabs, c->d_Wabs, c->d_Rw, c->d_RwT,
+                    c->d_Winv};
+    for (void* p : absp) dfree(p);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->ev_copy) cudaEventDestroy(c->ev_copy);
     if (c->stream2) cudaStreamDestroy(c->stream2);
@@ -324,7 +328,7 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
     for (int t = 0; t < nt; ++t)
         for (int f = 0; f < 4; ++f) {
             int e = m->neigh[t * 4 + f];
-            if (e == LYMPH_BC_DIRI || e == LYMPH_BC_NEUM) continue;
+            if (e == LYMPH_BC_DIRI || e == LYMPH_BC_NEUM || e == LYMPH_BC_ABSO) continue;
             if (e < 0 || e >= nt || e == t) { lymph_set_error("lymph_create: bad neighbour entry"); return LYMPH_EXIT_NEIGHBOUR_EL_ERROR; }
             bool back = false;
             for (int g = 0; g < 4; ++g) back |= (m->neigh[e * 4 + g] == t);
@@ -353,6 +357,7 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
     }
     std::vector<int32_t> row_ptr(np + 1, 0), col, blk_row, bf;
     std::vector<int64_t> bf_ptr(1, 0);
+    std::vector<int32_t> abs_idx(np, -1), abs_poly, abs_ptr(1, 0), abs_faces;
     int64_t n_sides = 0;
     for (int P = 0; P < np; ++P) {
         std::vector<int32_t> self_faces;
@@ -361,6 +366,7 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
             int t = ptets[k];
             for (int f = 0; f < 4; ++f) {
                 int e = m->neigh[t * 4 + f];
+                if (e == LYMPH_BC_ABSO) { abs_faces.push_back(t * 4 + f); continue; }  // damping only
                 if (e == LYMPH_BC_NEUM) continue;
                 if (e == LYMPH_BC_DIRI) { self_faces.push_back(t * 4 + f); continue; }
                 int Q = m->tet_poly[e];
@@ -368,6 +374,11 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
                 self_faces.push_back(t * 4 + f);
                 nb[Q].push_back(t * 4 + f);
             }
+        }
+        if ((int32_t)abs_faces.size() > abs_ptr.back()) {
+            abs_idx[P] = (int32_t)abs_poly.size();
+            abs_poly.push_back(P);
+            abs_ptr.push_back((int32_t)abs_faces.size());
         }
         n_sides += (int64_t)self_faces.size();
         row_ptr[P] = (int32_t)col.size();
@@ -406,6 +417,19 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
     if ((rc = upload(c, &c->d_blk_row, blk_row.data(), blk_row.size()))) return fail(rc);
     if ((rc = upload(c, &c->d_bf_ptr, bf_ptr.data(), bf_ptr.size()))) return fail(rc);
     if ((rc = upload(c, &c->d_bf, bf.data(), bf.size()))) return fail(rc);
+    c->n_abs = (int)abs_poly.size();
+    if (c->n_abs > 0) {
+        const size_t nd2 = (size_t)c->n_abs * c->nd * c->nd;
+        if ((rc = upload(c, &c->d_abs_idx, abs_idx.data(), abs_idx.size()))) return fail(rc);
+        if ((rc = upload(c, &c->d_abs_poly, abs_poly.data(), abs_poly.size()))) return fail(rc);
+        if ((rc = upload(c, &c->d_abs_ptr, abs_ptr.data(), abs_ptr.size()))) return fail(rc);
+        if ((rc = upload(c, &c->d_abs_faces, abs_faces.data(), abs_faces.size()))) return fail(rc);
+        if ((rc = dalloc(c, &c->d_Dabs, nd2))) return fail(rc);
+        if ((rc = dalloc(c, &c->d_Wabs, nd2))) return fail(rc);
+        if ((rc = dalloc(c, &c->d_Rw, nd2))) return fail(rc);
+        if ((rc = dalloc(c, &c->d_RwT, nd2))) return fail(rc);
+        if ((rc = dalloc(c, &c->d_Winv, nd2))) return fail(rc);
+    }
     if ((rc = dalloc(c, &c->d_fk, 12 * (size_t)nt))) return fail(rc);
     if ((rc = dalloc(c, &c->d_jdet, (size_t)nt))) return fail(rc);
     if ((rc = dalloc(c, &c->d_normal, 12 * (size_t)nt))) return fail(rc);
@@ -491,6 +515,7 @@ int lymph_make_matrices(lymph_ctx* c) {
         }
         LYMPH_TRY(make_mf_matrices(c));
         LYMPH_TRY(lymph_dev_cholesky(c));
+        LYMPH_TRY(lymph_dev_damping(c, true));
         LYMPH_TRY(lymph_sync_status(c, "lymph_make_matrices"));
         c->have_matrices = true;
         return LYMPH_OK;
@@ -518,6 +543,7 @@ int lymph_make_matrices(lymph_ctx* c) {
     c->k32_valid = false;  // an FP32 copy made from earlier blocks is stale
     LYMPH_TRY(lymph_dev_assemble(c, LYMPH_BLOCKS_K, c->d_K, c->precision == LYMPH_MIXED, true));
     LYMPH_TRY(lymph_dev_cholesky(c));
+    LYMPH_TRY(lymph_dev_damping(c, true));
     LYMPH_TRY(lymph_sync_status(c, "lymph_make_matrices"));
     c->have_matrices = true;
     return LYMPH_OK;
@@ -1030,6 +1056,11 @@ int lymph_set_dt(lymph_ctx* c, double dt) {
     if (!c || !(dt > 0.0) || !std::isfinite(dt)) return LYMPH_ERR_INVALID;
     c->dt = dt;
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    if (c->n_abs > 0 && c->have_matrices && c->winv_dt != dt) {
+        // the absorbing polyhedra's M (x) I + dt/2 D depends on dt
+        LYMPH_TRY(lymph_dev_damping(c, false));
+        return lymph_sync_status(c, "lymph_set_dt");
+    }
     return LYMPH_OK;
 }
 

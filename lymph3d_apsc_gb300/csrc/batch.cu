@@ -210,6 +210,9 @@ int refresh_problems(lymph_batch* b) {
         P.a.rhs_stat = c->d_rhs_stat;
         P.a.rhs_dyn = c->d_rhs_dyn;
         P.a.partial = nullptr;
+        P.a.abs_idx = c->n_abs > 0 ? c->d_abs_idx : nullptr;
+        P.a.Dabs = c->d_Dabs;
+        P.a.Winv = c->d_Winv;
         P.a.dt = c->dt;
         P.a.status = b->d_status;
         P.a.n_poly = c->n_poly;

@@ -92,6 +92,14 @@ struct lymph_ctx {
     bool surrogate_apply_fp32 = false;  // lymph_surrogate_apply_fp32
     double *d_M = nullptr, *d_Mm = nullptr, *d_R = nullptr, *d_Rm = nullptr, *d_RT = nullptr, *d_RmT = nullptr;
     double* d_Minv = nullptr;       // [n_poly][Np][Np] column-major inverse of M_loc
+    // absorbing faces (LYMPH_BC_ABSO): the n_abs polyhedra that have some,
+    // their faces (CSR over d_abs_ptr, codes t*4+f), each polyhedron's index
+    // among them (-1 for the others), the damping block D (symmetric) and the
+    // column-major inverse of W = M (x) I + dt/2 D of each, [n_abs][nd][nd]
+    int n_abs = 0;
+    int32_t *d_abs_idx = nullptr, *d_abs_poly = nullptr, *d_abs_ptr = nullptr, *d_abs_faces = nullptr;
+    double *d_Dabs = nullptr, *d_Winv = nullptr, *d_Wabs = nullptr, *d_Rw = nullptr, *d_RwT = nullptr;
+    double winv_dt = 0.0;           // the dt the W inverses were made for
     // matrix-free neighbour terms (LYMPH_MIXED_MF): d_K holds the n_poly FP32
     // self blocks; d_mf_tri the FP32 geometry of every neighbour-block
     // triangle (parallel to d_bf), d_mf_poly the Legendre map of every

@@ -819,6 +819,9 @@ void lymph_mf_batch_problem(const lymph_ctx* c, int* status, void* out) {
     s.u0 = s.un = nullptr;
     s.out = nullptr;
     s.partial = nullptr;
+    s.abs_idx = c->n_abs > 0 ? c->d_abs_idx : nullptr;
+    s.Dabs = c->d_Dabs;
+    s.Winv = c->d_Winv;
     s.dt = c->dt;
     s.status = status;
     s.n_poly = c->n_poly;

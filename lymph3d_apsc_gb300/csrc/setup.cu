@@ -685,6 +685,75 @@ __global__ void __launch_bounds__(VEC_THREADS) k_vector(VecArgs A) {
     for (int r = tid; r < ND; r += VEC_THREADS) A.out[(int64_t)P * ND + r] = s_acc[r] * A.scale;
 }
 
+// MAKE_DAMPING_FACE (assemble_element.f90:666-731) summed over the absorbing
+// faces of each polyhedron that has some: one CTA per such polyhedron, the
+// face's quadrature points and P's basis values in shared memory, each thread
+// owning fixed entries of the ND x ND block D (row (i, m), column (j, n)):
+//   D += |face| w_q (phi_m phi_n) C_ij,
+//   C = c_t (t1 t1^T + t2 t2^T) + c_n n n^T = c_t (I - n n^T) + c_n n n^T,
+// c_t = sqrt(rho mu), c_n = sqrt(rho (lambda + 2 mu)) of the face's
+// tetrahedron.  phi_m phi_n is formed before the weight, so D is exactly
+// symmetric.
+template <int PD>
+__global__ void __launch_bounds__(VEC_THREADS) k_damping(const int32_t* __restrict__ abs_poly,
+                                                       const int32_t* __restrict__ abs_ptr,
+                                                       const int32_t* __restrict__ abs_faces, const double* __restrict__ fk,
+                                                       const double* __restrict__ nrm, const double* __restrict__ area,
+                                                       const double* __restrict__ bbox, const int32_t* __restrict__ tet_mat,
+                                                       const double* __restrict__ mat, const RefTables* __restrict__ ref,
+                                                       double* __restrict__ D) {
+    using Dg = Deg<PD>;
+    constexpr int NP = Dg::NP, ND = Dg::ND, NQ2 = Dg::NQ2;
+    __shared__ double s_phi[NQ2 * NP];
+    __shared__ double s_pt[NQ2 * 3];
+    const int a = blockIdx.x, tid = threadIdx.x, P = abs_poly[a];
+    const double* bb = &bbox[P * 6];
+    double* Da = D + (int64_t)a * ND * ND;
+    for (int e = tid; e < ND * ND; e += VEC_THREADS) Da[e] = 0.0;
+    for (int k = abs_ptr[a]; k < abs_ptr[a + 1]; ++k) {
+        const int code = abs_faces[k], t = code >> 2, f = code & 3;
+        __syncthreads();
+        for (int q = tid; q < NQ2; q += VEC_THREADS) face_point(&fk[t * 12], ref, f, q, &s_pt[q * 3]);
+        __syncthreads();
+        for (int it = tid; it < NQ2 * NP; it += VEC_THREADS) {
+            const int q = it / NP, fb = it % NP;
+            double dp[3];
+            basis_eval(&s_pt[q * 3], bb, &ref->blist[fb * 3], &s_phi[q * NP + fb], dp);
+        }
+        __syncthreads();
+        const double* n = &nrm[t * 12 + f * 3];
+        const int mid = tet_mat[t];
+        const double rho = mat[mid * 3 + 0], lam = mat[mid * 3 + 1], mu = mat[mid * 3 + 2];
+        const double ct = sqrt(rho * mu), cn = sqrt(rho * (lam + 2.0 * mu));
+        const double ar = area[t * 4 + f];
+        for (int e = tid; e < ND * ND; e += VEC_THREADS) {
+            const int r = e / ND, cc = e - r * ND;
+            const int i = r / NP, m = r - i * NP, j = cc / NP, nn = cc - j * NP;
+            const double nij = n[i] * n[j];
+            const double C = ct * ((i == j ? 1.0 : 0.0) - nij) + cn * nij;
+            double s = 0.0;
+            for (int q = 0; q < NQ2; ++q) s = s + ref->weitria2[q] * (s_phi[q * NP + m] * s_phi[q * NP + nn]);
+            Da[e] += ar * C * s;
+        }
+    }
+}
+
+// W = M (x) I + dt/2 D for each polyhedron with absorbing faces (M: the
+// rho-weighted mass matrix M_loc of the polyhedron, the same for each
+// component).
+__global__ void k_damping_w(int n_abs, int NP, const int32_t* __restrict__ abs_poly, const double* __restrict__ M,
+                            const double* __restrict__ D, double half_dt, double* __restrict__ W) {
+    const int ND = 3 * NP;
+    const int64_t total = (int64_t)n_abs * ND * ND;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = e / ((int64_t)ND * ND);
+        const int rc = (int)(e - a * ND * ND), r = rc / ND, cc = rc - r * ND;
+        const int i = r / NP, m = r - i * NP, j = cc / NP, nn = cc - j * NP;
+        const double mv = (i == j) ? M[(int64_t)abs_poly[a] * NP * NP + m * NP + nn] : 0.0;
+        W[e] = mv + half_dt * D[e];
+    }
+}
+
 // Point source: rhs[P][i*Np + m] = dir_i phi_m(x0) for the polyhedron P
 // that contains x0 (one block of Np threads); the rest of rhs was zeroed by
 // the caller.  The spatial part of a Ricker source f = dir delta(x - x0) R(t),
@@ -819,6 +888,40 @@ int lymph_dev_cholesky(lymph_ctx* c) {
     k_cholesky<<<grid, 32 * warps_per_block, smem, c->stream>>>(c->n_poly, c->Np, c->d_Mm, c->d_Rm, c->d_RmT, c->d_status);
     k_mass_inverse<<<grid, 32 * warps_per_block, 0, c->stream>>>(c->n_poly, c->Np, c->d_R, c->d_Minv);
     c->launches += 3;
+    LYMPH_CUDA_TRY(cudaGetLastError());
+    return LYMPH_OK;
+}
+
+// The damping blocks of the absorbing faces (once per assembly) and the
+// inverses of M (x) I + dt/2 D for the context's dt: W, its Cholesky factor
+// (cholesky, one warp per polyhedron) and the explicit column-major inverse
+// (solve_LU per column), as for the mass matrix.
+int lymph_dev_damping(lymph_ctx* c, bool assemble) {
+    if (c->n_abs <= 0) return LYMPH_OK;
+    const int ND = c->nd;
+    if (assemble) {
+        switch (c->p) {
+            case 1: k_damping<1><<<c->n_abs, VEC_THREADS, 0, c->stream>>>(c->d_abs_poly, c->d_abs_ptr, c->d_abs_faces, c->d_fk, c->d_normal, c->d_area, c->d_bbox, c->d_tet_mat, c->d_mat, c->d_ref, c->d_Dabs); break;
+            case 2: k_damping<2><<<c->n_abs, VEC_THREADS, 0, c->stream>>>(c->d_abs_poly, c->d_abs_ptr, c->d_abs_faces, c->d_fk, c->d_normal, c->d_area, c->d_bbox, c->d_tet_mat, c->d_mat, c->d_ref, c->d_Dabs); break;
+            case 3: k_damping<3><<<c->n_abs, VEC_THREADS, 0, c->stream>>>(c->d_abs_poly, c->d_abs_ptr, c->d_abs_faces, c->d_fk, c->d_normal, c->d_area, c->d_bbox, c->d_tet_mat, c->d_mat, c->d_ref, c->d_Dabs); break;
+            case 4: k_damping<4><<<c->n_abs, VEC_THREADS, 0, c->stream>>>(c->d_abs_poly, c->d_abs_ptr, c->d_abs_faces, c->d_fk, c->d_normal, c->d_area, c->d_bbox, c->d_tet_mat, c->d_mat, c->d_ref, c->d_Dabs); break;
+            default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
+        }
+        c->launches++;
+        LYMPH_CUDA_TRY(cudaGetLastError());
+    }
+    const int64_t total = (int64_t)c->n_abs * ND * ND;
+    const unsigned gw = (unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+    k_damping_w<<<gw, 256, 0, c->stream>>>(c->n_abs, c->Np, c->d_abs_poly, c->d_M, c->d_Dabs, 0.5 * c->dt, c->d_Wabs);
+    const size_t smem = sizeof(double) * (size_t)ND * ND;  // one warp per block: its ND x ND factor
+    // raise (never lower) k_cholesky's dynamic shared-memory limit: the mass
+    // factorisation launches it with up to 4 Np^2 doubles per block
+    const size_t lim = smem > (size_t)48 * 1024 ? smem : (size_t)48 * 1024;
+    LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_cholesky, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim));
+    k_cholesky<<<c->n_abs, 32, smem, c->stream>>>(c->n_abs, ND, c->d_Wabs, c->d_Rw, c->d_RwT, c->d_status);
+    k_mass_inverse<<<(unsigned)((c->n_abs + 3) / 4), 128, 0, c->stream>>>(c->n_abs, ND, c->d_Rw, c->d_Winv);
+    c->launches += 3;
+    c->winv_dt = c->dt;
     LYMPH_CUDA_TRY(cudaGetLastError());
     return LYMPH_OK;
 }

@@ -108,6 +108,9 @@ StepArgs base_args(lymph_ctx* c) {
     A.rhs_stat = c->d_rhs_stat; A.rhs_dyn = c->d_rhs_dyn; A.gvals = c->d_gvals; A.step_idx = c->d_step_idx;
     A.u0 = nullptr; A.un = nullptr; A.out = nullptr; A.partial = c->d_partial; A.dt = c->dt; A.status = c->d_status;
     A.n_poly = c->n_poly;
+    A.abs_idx = c->n_abs > 0 ? c->d_abs_idx : nullptr;
+    A.Dabs = c->d_Dabs;
+    A.Winv = c->d_Winv;
     return A;
 }
 

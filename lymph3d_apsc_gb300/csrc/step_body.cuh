@@ -42,6 +42,10 @@ struct StepArgs {
     double* out;               // u^{n+1} (MODE_STEP: may alias u0), u^1 (MODE_FIRST), M^-1 K u (MODE_APPLY),
                                // K u (MODE_KU)
     double* partial;           // MODE_DG: per-polyhedron du . (A du)
+    const int32_t* abs_idx;    // per polyhedron its index among those with absorbing faces, -1 for the
+                               // others; null when the mesh has no absorbing face
+    const double* Dabs;        // [n_abs][ND][ND] damping blocks (symmetric)
+    const double* Winv;        // [n_abs][ND][ND] column-major inverse of M (x) I + dt/2 D
     double dt;
     int* status;
     int n_poly;
@@ -102,6 +106,44 @@ __device__ __forceinline__ void finish_poly(const StepArgs& A, int P, double y, 
         }
     }
     __syncthreads();
+    // polyhedra with absorbing faces (the index is the same for the whole CTA)
+    const int ai = (MODE == MODE_STEP || MODE == MODE_FIRST) && A.abs_idx ? A.abs_idx[P] : -1;
+    if (ai >= 0) {
+        const double* Db = A.Dabs + (int64_t)ai * ND * ND;
+        const int64_t base = (int64_t)P * ND;
+        double dv = 0.0;
+        if (tid < ND) {
+            // MODE_STEP: D (u^n - u^{n-1}); MODE_FIRST: D v^0 (v^0 is in un)
+#pragma unroll 1
+            for (int c = 0; c < ND; ++c) {
+                const double w = (MODE == MODE_STEP) ? A.un[base + c] - A.u0[base + c] : A.un[base + c];
+                dv += Db[(int64_t)c * ND + tid] * w;
+            }
+        }
+        double bn = 0.0;
+        if (tid < ND) bn = (MODE == MODE_STEP) ? A.dt * A.dt * s_b[tid] - A.dt * dv : s_b[tid] - dv;
+        __syncthreads();
+        if (tid < ND) s_b[tid] = bn;
+        __syncthreads();
+        if (MODE == MODE_STEP) {
+            // u^{n+1} = 2 u^n - u^{n-1} + W^-1 (dt^2 (F - K u^n) - dt D (u^n - u^{n-1}))
+            if (tid < ND) {
+                const double* Wi = A.Winv + (int64_t)ai * ND * ND + tid;
+                double x0 = 0.0, x1 = 0.0;
+#pragma unroll 1
+                for (int c = 0; c < ND; c += 2) {
+                    x0 += Wi[(int64_t)c * ND] * s_b[c];
+                    if (c + 1 < ND) x1 += Wi[(int64_t)(c + 1) * ND] * s_b[c + 1];
+                }
+                const int64_t q = base + tid;
+                const double v = (x0 + x1) + 2.0 * A.un[q] - A.u0[q];
+                if (!isfinite(v)) atomicOr(A.status, ST_NONFINITE);
+                A.out[q] = v;
+            }
+            return;
+        }
+        // MODE_FIRST continues with M^-1 (F - K u^0 - D v^0) below
+    }
     if (tid < ND) {
         const int i = tid / NP, m = tid % NP;
         const double* Mi = A.Minv + (int64_t)P * NP * NP + m;

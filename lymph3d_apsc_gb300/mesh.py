@@ -105,8 +105,10 @@ def cube(n: int, bc: str = "dirichlet", agglomeration: str = "tet", seed: int = 
          jitter_seed: int = 7) -> Mesh:
     """Structured [0,1]^3 mesh of n^3 hexahedra x 6 tetrahedra.
 
-    bc: "dirichlet" (every boundary face Dirichlet) or "reference" (the decks'
-    convention: z=0, z=1, x=1 Dirichlet; y=1, x=0, y=0 Neumann).
+    bc: "dirichlet" (every boundary face Dirichlet), "reference" (the decks'
+    convention: z=0, z=1, x=1 Dirichlet; y=1, x=0, y=0 Neumann) or
+    "absorbing" (z=1 a free surface, i.e. Neumann; every other boundary face
+    absorbing, LYMPH_BC_ABSO).
     agglomeration: "tet" (one polyhedron per tetrahedron, the reference's only
     consistent mode), "hex" (6 tets per polyhedron) or "bfs" (seeded groups of
     group[0]..group[1] tets).
@@ -129,6 +131,11 @@ def cube(n: int, bc: str = "dirichlet", agglomeration: str = "tet", seed: int = 
     matched = neigh.copy()
     mode = _lib.BCMODE_ALL_DIRICHLET if bc == "dirichlet" else _lib.BCMODE_REFERENCE
     neigh, fun = apply_bc(ftag, neigh, mode)
+    if bc == "absorbing":
+        neigh = set_absorbing(neigh, ftag, tags=(2, 4, 5, 6, 7))
+        neigh[(neigh < 0) & (ftag == 3)] = _lib.BC_NEUM
+    elif bc not in ("dirichlet", "reference"):
+        raise ValueError(f"unknown boundary condition set {bc!r}")
     if agglomeration == "tet":
         tp = np.arange(nt.value, dtype=np.int32)
     elif agglomeration == "hex":
@@ -145,6 +152,15 @@ def cube(n: int, bc: str = "dirichlet", agglomeration: str = "tet", seed: int = 
         tmat = np.zeros(nt.value, np.int32)
     return Mesh(coords, tv, tp, tmat, neigh, fun, mat, ftag,
                 {"n": n, "bc": bc, "agglomeration": agglomeration, "seed": seed, "group": tuple(group)})
+
+
+def set_absorbing(neigh: np.ndarray, face_tag: np.ndarray, tags) -> np.ndarray:
+    """The boundary faces whose tag is in `tags` become absorbing
+    (LYMPH_BC_ABSO), the reference's ABSO records (Poly_readfile.f90:521)."""
+    nb = np.array(neigh, dtype=np.int32, copy=True)
+    sel = (nb < 0) & np.isin(face_tag, np.asarray(list(tags), dtype=np.int32))
+    nb[sel] = _lib.BC_ABSO
+    return nb
 
 
 def lognormal_materials(n_poly: int, seed: int, sigma: float = 0.5, rho: float = 1.0) -> np.ndarray:
@@ -167,10 +183,11 @@ def _read_keywords(path: Path) -> dict:
     return out
 
 
-def read_mate(path: Path):
-    """MATE / DIRI / NEUM records (Poly_readfile.f90:327-707).
-    lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2 (:393-412)."""
-    mats, diri, neum = [], {}, {}
+def read_mate(path: Path, with_abso: bool = False):
+    """MATE / DIRI / NEUM (and ABSO) records (Poly_readfile.f90:327-707).
+    lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2 (:393-412).  Returns
+    (mats, diri, neum), and the ABSO tags as a fourth item with with_abso."""
+    mats, diri, neum, abso = [], {}, {}, []
     for line in Path(path).read_text().splitlines():
         p = line.split()
         if not p:
@@ -182,7 +199,9 @@ def read_mate(path: Path):
             diri[int(p[1])] = int(p[2])
         elif p[0] == "NEUM":
             neum[int(p[1])] = int(p[2])
-    return mats, diri, neum
+        elif p[0] == "ABSO":
+            abso.append(int(p[1]))
+    return (mats, diri, neum, abso) if with_abso else (mats, diri, neum)
 
 
 def read_mesh_file(path: Path):
@@ -211,11 +230,12 @@ def read_deck_arrays(deck_dir) -> dict:
     (tag, degree, rho, lambda, mu) and the Poly.input time parameters."""
     d = Path(deck_dir)
     kw = _read_keywords(d / "Poly.input")
-    mats, diri, neum = read_mate(d / (kw["MATFILE"] + ".mate"))
+    mats, diri, neum, abso = read_mate(d / (kw["MATFILE"] + ".mate"), with_abso=True)
     coords, tv, tmat, tris, ttag = read_mesh_file(d / (kw["GRIDFILE"] + ".mesh"))
     return {"coords": coords, "tet_vert": tv, "tet_mat_tag": tmat, "tria": tris, "tria_tag": ttag,
             "mate": np.array(mats, np.float64).reshape(-1, 5),
             "diri_tags": np.array(sorted(diri), np.int32), "neum_tags": np.array(sorted(neum), np.int32),
+            "abso_tags": np.array(sorted(abso), np.int32),
             "dt": np.float64(kw.get("TIMESTEP", "1e-3")), "stop_time": np.float64(kw.get("STOPTIME", "1")),
             "name": d.name}
 
@@ -225,8 +245,9 @@ def deck_mesh(arrays: dict, override_materials: bool = True) -> tuple[Mesh, dict
     it): boundary triangles tagged on the tetrahedra's faces, faces matched,
     the decks' tag convention applied (2-4 Dirichlet, 5-7 Neumann,
     MAKE_PARTITION_AND_MPI_FILES.f90:2105-2109), one polyhedron per
-    tetrahedron.  With override_materials the driver's rho = lambda = mu = 1
-    override (Lymph3D.f90:196-203) is applied."""
+    tetrahedron; faces whose tag has an ABSO record are absorbing.  With
+    override_materials the driver's rho = lambda = mu = 1 override
+    (Lymph3D.f90:196-203) is applied."""
     lib = _lib.load()
     tv = np.ascontiguousarray(arrays["tet_vert"], dtype=np.int32)
     tris = np.ascontiguousarray(arrays["tria"], dtype=np.int32)
@@ -239,6 +260,9 @@ def deck_mesh(arrays: dict, override_materials: bool = True) -> tuple[Mesh, dict
                                       ptr(ttag, c_int32), ptr(ftag, c_int32), byref(nunf)), "lymph_mesh_tag_boundary")
     neigh, _ = match_faces(tv)
     neigh, fun = apply_bc(ftag, neigh, _lib.BCMODE_REFERENCE)
+    abso = arrays.get("abso_tags")
+    if abso is not None and len(abso):
+        neigh = set_absorbing(neigh, ftag, abso)
     tag_to_idx = {int(m[0]): i for i, m in enumerate(mats)}
     tet_mat = np.array([tag_to_idx[int(t)] for t in arrays["tet_mat_tag"]], np.int32)
     if override_materials:

@@ -510,6 +510,11 @@ struct Oracle {
     std::vector<double> slot[4];              // [n_poly][nd]
     bool have_matrices = false;
     bool have_dg = false;      // A_dg assembled (g_assemble_dg when the matrices were made)
+    // absorbing faces: per polyhedron its index among those with some (-1
+    // otherwise), their damping blocks D [nd][nd] and the Cholesky factors of
+    // W = M (x) I + dt/2 D (row-major, as cholesky writes them)
+    std::vector<int> abs_idx;
+    std::vector<std::vector<double>> Dabs, RW;
     int status = 0;
 };
 
@@ -769,6 +774,88 @@ int block_of(Oracle& o, int P, int Qp) {
     return (int)v.size() - 1;
 }
 
+// MAKE_DAMPING_FACE (assemble_element.f90:666-731) on every absorbing face
+// of a polyhedron, summed into the polyhedron's damping block D:
+//   val = phi_m (t1_i b1 + t2_i b2 + n_i b3),  b = (c1 phi_n t1_j, c2 phi_n t2_j, c3 phi_n n_j),
+//   D[(i,m),(j,n)] += w_q |face| val,
+// over all (i, j, m, n).  The reference leaves c1 = c2 = c3 = 1 as
+// placeholders, takes its two tangents straight from two face edges
+// (CREATE_NORMAL_FACE, MAKE_PARTITION_AND_MPI_FILES.f90:1486-1498, not
+// orthogonal to each other), loops over the upper triangle adding each term
+// to both halves (so the diagonal counts twice) and writes row (i-1)*DIM + m;
+// here the frame is orthonormal (t1 the first edge direction, t2 = n x t1),
+// c1 = c2 = rho c_s = sqrt(rho mu) and c3 = rho c_p = sqrt(rho (lambda + 2 mu))
+// (the first-order absorbing impedances of the face's tetrahedron), and every
+// term is added once at row i*Np + m.  Then W = M (x) I + dt/2 D and its
+// Cholesky factor.
+bool make_damping(Oracle& o) {
+    const int Np = o.Np, nd = o.nd, nq2 = o.Q.nq2;
+    o.abs_idx.assign(o.n_poly, -1);
+    o.Dabs.clear();
+    o.RW.clear();
+    for (int P = 0; P < o.n_poly; ++P) {
+        bool any = false;
+        for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1] && !any; ++k)
+            for (int f = 0; f < 4; ++f) any |= (o.neigh[o.poly_tets[k] * 4 + f] == BC_ABSO);
+        if (any) {
+            o.abs_idx[P] = (int)o.Dabs.size();
+            o.Dabs.emplace_back((size_t)nd * nd, 0.0);
+            o.RW.emplace_back((size_t)nd * nd, 0.0);
+        }
+    }
+    bool ok = true;
+#pragma omp parallel for schedule(dynamic, 1) reduction(&& : ok)
+    for (int P = 0; P < o.n_poly; ++P) {
+        const int a = o.abs_idx[P];
+        if (a < 0) continue;
+        std::vector<double>& D = o.Dabs[a];
+        std::vector<double> phib, gradb;
+        for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1]; ++k) {
+            const int t = o.poly_tets[k];
+            const int mid = o.tet_mat[t];
+            const double rho = o.mat[mid * 3 + 0], lam = o.mat[mid * 3 + 1], mu = o.mat[mid * 3 + 2];
+            const double c1 = std::sqrt(rho * mu), c2 = c1, c3 = std::sqrt(rho * (lam + 2 * mu));
+            for (int f = 0; f < 4; ++f) {
+                if (o.neigh[t * 4 + f] != BC_ABSO) continue;
+                const double* nv = &o.normal[t * 12 + f * 3];
+                // first tangent: the edge from the face's second vertex to its third
+                const int* fv = FACE_VERTS[f];
+                double e[3], t1[3], t2[3];
+                for (int d = 0; d < 3; ++d)
+                    e[d] = o.coords[o.tet_vert[t * 4 + fv[2]] * 3 + d] - o.coords[o.tet_vert[t * 4 + fv[1]] * 3 + d];
+                const double en = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+                for (int d = 0; d < 3; ++d) t1[d] = e[d] / en;
+                t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
+                t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
+                t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
+                basis_boundary(o, t, f, P, -1, phib, gradb);
+                const double ar = o.area[t * 4 + f];
+                for (int q = 0; q < nq2; ++q) {
+                    const double w = o.Q.weitria2[q];
+                    for (int i = 0; i < 3; ++i)
+                        for (int j = 0; j < 3; ++j)
+                            for (int m = 0; m < Np; ++m)
+                                for (int n = 0; n < Np; ++n) {
+                                    const double phn = phib[q * Np + n];
+                                    const double b1 = c1 * phn * t1[j], b2 = c2 * phn * t2[j], b3 = c3 * phn * nv[j];
+                                    const double val = phib[q * Np + m] * (t1[i] * b1 + t2[i] * b2 + nv[i] * b3);
+                                    D[(size_t)(i * Np + m) * nd + j * Np + n] += w * ar * val;
+                                }
+                }
+            }
+        }
+        std::vector<double> W((size_t)nd * nd);
+        for (int r = 0; r < nd; ++r)
+            for (int c = 0; c < nd; ++c) {
+                const int i = r / Np, m = r % Np, j = c / Np, n = c % Np;
+                const double mv = (i == j) ? o.M[(size_t)P * Np * Np + (size_t)m * Np + n] : 0.0;
+                W[(size_t)r * nd + c] = mv + 0.5 * o.dt * D[(size_t)r * nd + c];
+            }
+        if (!cholesky(W.data(), nd, o.RW[a].data())) ok = false;
+    }
+    return ok;
+}
+
 // MAKE_MATRICES_FREE, matrix_free.f90:27-464, polyhedron-accumulated; then
 // the Cholesky factors of the driver (Lymph3D.f90:264-271).
 int make_matrices(Oracle& o) {
@@ -814,7 +901,7 @@ int make_matrices(Oracle& o) {
                     Qp = o.tet_poly[E2];
                     if (Qp == P) continue;  // face_flag: same polyhedron
                 }
-                if (E2 == BC_NEUM) continue;  // no stiffness contribution
+                if (E2 == BC_NEUM || E2 == BC_ABSO) continue;  // no stiffness contribution (absorbing: damping only)
                 const double* nn = &o.normal[t * 12 + f * 3];
                 basis_boundary(o, t, f, P, Qp, phib, gradb);
                 double hk2 = (Qp >= 0) ? o.hk[Qp] : o.hk[0];
@@ -860,6 +947,7 @@ int make_matrices(Oracle& o) {
         if (!cholesky(&o.Mm[(size_t)P * N2], Np, &o.Rm[(size_t)P * N2])) bad |= 1;
     }
     if (bad) { g_err = "oracle: mass matrix is not positive definite"; return LYMPH_EXIT_SINGULARMTX; }
+    if (!make_damping(o)) { g_err = "oracle: M + dt/2 D is not positive definite"; return LYMPH_EXIT_SINGULARMTX; }
     o.have_matrices = true;
     return 0;
 }
@@ -1042,6 +1130,109 @@ void apply_and_solve_device_order(const Oracle& o, const std::vector<double>& u,
             }
             out[i * Np + m] = x0 + x1;
         }
+}
+
+// tmp = -K u + rhs_stat + rhs_dyn g(t) for polyhedron P, the reference's
+// order (blocks in stored order, each row summed forward).
+void apply_rhs(const Oracle& o, const std::vector<double>& u, double t, int P, std::vector<double>& tmp) {
+    const int nd = o.nd;
+    tmp.assign(nd, 0.0);
+    const double g = time_function(t);
+    for (size_t b = 0; b < o.nbr[P].size(); ++b) {
+        const double* Kb = &o.K[P][b * nd * nd];
+        const double* uq = &u[(size_t)o.nbr[P][b] * nd];
+        for (int r = 0; r < nd; ++r) {
+            double s = 0.0;
+            for (int c = 0; c < nd; ++c) s = s + Kb[r * nd + c] * uq[c];
+            tmp[r] = tmp[r] + s;
+        }
+    }
+    for (int r = 0; r < nd; ++r) tmp[r] = -tmp[r] + o.rhs_stat[(size_t)P * nd + r] + o.rhs_dyn[(size_t)P * nd + r] * g;
+}
+
+// The damped leapfrog step of a polyhedron with absorbing faces:
+//   (M + dt/2 D) u^{n+1} = dt^2 (F - K u^n) + 2 M u^n - (M - dt/2 D) u^{n-1},
+// solved as u^{n+1} = 2 u^n - u^{n-1} + W^-1 (dt^2 (F - K u^n) - dt D (u^n - u^{n-1})),
+// W = M (x) I + dt/2 D by its Cholesky factor (solve_LU(R^T, R)).
+void absorbing_step(const Oracle& o, double t, int P, double* out) {
+    const int nd = o.nd, a = o.abs_idx[P];
+    const std::vector<double>& un = o.slot[LYMPH_SLOT_UN];
+    const std::vector<double>& u0 = o.slot[LYMPH_SLOT_U0];
+    std::vector<double> tmp, b(nd), x(nd);
+    apply_rhs(o, un, t, P, tmp);
+    const double* D = o.Dabs[a].data();
+    const size_t base = (size_t)P * nd;
+    for (int r = 0; r < nd; ++r) {
+        double dv = 0.0;
+        for (int c = 0; c < nd; ++c) dv = dv + D[(size_t)r * nd + c] * (un[base + c] - u0[base + c]);
+        b[r] = o.dt * o.dt * tmp[r] - o.dt * dv;
+    }
+    if (g_explicit_inverse || g_device_order) {
+        // floor variants: W^-1 as an explicit inverse (columns by solve_LU),
+        // applied with fused multiply-adds, the way the device applies it
+        std::vector<double> e(nd), col(nd), inv((size_t)nd * nd);
+        for (int k = 0; k < nd; ++k) {
+            for (int r = 0; r < nd; ++r) e[r] = (r == k) ? 1.0 : 0.0;
+            solve_LU_RT_R(o.RW[a].data(), e.data(), nd, col.data());
+            for (int r = 0; r < nd; ++r) inv[(size_t)r * nd + k] = col[r];
+        }
+        for (int r = 0; r < nd; ++r) {
+            double s = 0.0;
+            for (int c = 0; c < nd; ++c) s = std::fma(inv[(size_t)r * nd + c], b[c], s);
+            x[r] = s;
+        }
+    } else {
+        solve_LU_RT_R(o.RW[a].data(), b.data(), nd, x.data());
+    }
+    for (int r = 0; r < nd; ++r) out[r] = x[r] + 2.0 * un[base + r] - u0[base + r];
+}
+
+// The first step of a polyhedron with absorbing faces:
+//   u^1 = u^0 + dt v^0 + dt^2/2 M^-1 (F - K u^0 - D v^0).
+void absorbing_first_step(const Oracle& o, double t, int P, double* out) {
+    const int nd = o.nd, Np = o.Np, a = o.abs_idx[P];
+    const std::vector<double>& u0 = o.slot[LYMPH_SLOT_U0];
+    const std::vector<double>& v0 = o.slot[LYMPH_SLOT_V0];
+    std::vector<double> tmp, v(Np), x(Np);
+    apply_rhs(o, u0, t, P, tmp);
+    const double* D = o.Dabs[a].data();
+    const size_t base = (size_t)P * nd;
+    for (int r = 0; r < nd; ++r) {
+        double dv = 0.0;
+        for (int c = 0; c < nd; ++c) dv = dv + D[(size_t)r * nd + c] * v0[base + c];
+        tmp[r] = tmp[r] - dv;
+    }
+    const double half_dt2 = 0.5 * (o.dt * o.dt);
+    std::vector<double> inv;
+    if (g_explicit_inverse || g_device_order) explicit_inverse(o, P, inv);
+    for (int i = 0; i < 3; ++i) {
+        for (int m = 0; m < Np; ++m) v[m] = tmp[i * Np + m];
+        if (g_device_order) {
+            // floor variant: the device's order (explicit inverse, two
+            // accumulators over even and odd columns, fused multiply-adds)
+            for (int m = 0; m < Np; ++m) {
+                double x0 = 0.0, x1 = 0.0;
+                for (int c = 0; c < Np; c += 2) {
+                    x0 = std::fma(inv[(size_t)m * Np + c], v[c], x0);
+                    if (c + 1 < Np) x1 = std::fma(inv[(size_t)m * Np + c + 1], v[c + 1], x1);
+                }
+                const size_t q = base + i * Np + m;
+                out[i * Np + m] = std::fma(o.dt, v0[q], std::fma(half_dt2, x0 + x1, u0[q]));
+            }
+            continue;
+        }
+        if (g_explicit_inverse) {
+            for (int m = 0; m < Np; ++m) {
+                double xx = 0.0;
+                for (int c = 0; c < Np; ++c) xx = std::fma(inv[(size_t)m * Np + c], v[c], xx);
+                x[m] = xx;
+            }
+        } else {
+            solve_LU_RT_R(&o.R[(size_t)P * Np * Np], v.data(), Np, x.data());
+        }
+        for (int m = 0; m < Np; ++m)
+            out[i * Np + m] = half_dt2 * x[m] + u0[base + i * Np + m] + o.dt * v0[base + i * Np + m];
+    }
 }
 
 void apply_and_solve(const Oracle& o, const std::vector<double>& u, double t, int P, std::vector<double>& out) {
@@ -1256,6 +1447,10 @@ int oracle_first_step(void* h, double t) {
     std::vector<double> un((size_t)o.n_poly * nd);
 #pragma omp parallel for schedule(static)
     for (int P = 0; P < o.n_poly; ++P) {
+        if (!o.abs_idx.empty() && o.abs_idx[P] >= 0) {
+            absorbing_first_step(o, t, P, &un[(size_t)P * nd]);
+            continue;
+        }
         std::vector<double> x;
         apply_and_solve(o, o.slot[LYMPH_SLOT_U0], t, P, x);
         for (int r = 0; r < nd; ++r) {
@@ -1278,6 +1473,10 @@ int oracle_step(void* h, double t) {
     std::vector<double> us((size_t)o.n_poly * nd);
 #pragma omp parallel for schedule(static)
     for (int P = 0; P < o.n_poly; ++P) {
+        if (!o.abs_idx.empty() && o.abs_idx[P] >= 0) {
+            absorbing_step(o, t, P, &us[(size_t)P * nd]);
+            continue;
+        }
         std::vector<double> x;
         apply_and_solve(o, o.slot[LYMPH_SLOT_UN], t, P, x);
         for (int r = 0; r < nd; ++r) {
