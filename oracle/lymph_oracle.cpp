@@ -515,6 +515,9 @@ struct Oracle {
     // W = M (x) I + dt/2 D (row-major, as cholesky writes them)
     std::vector<int> abs_idx;
     std::vector<std::vector<double>> Dabs, RW;
+    // the same blocks summed in the device kernel's arrangement
+    // (|face| C_ij sum_q w_q (phi_m phi_n)), for the device-order floor variant
+    std::vector<std::vector<double>> Dabs_dev, RW_dev;
     int status = 0;
 };
 
@@ -793,6 +796,8 @@ bool make_damping(Oracle& o) {
     o.abs_idx.assign(o.n_poly, -1);
     o.Dabs.clear();
     o.RW.clear();
+    o.Dabs_dev.clear();
+    o.RW_dev.clear();
     for (int P = 0; P < o.n_poly; ++P) {
         bool any = false;
         for (int k = o.poly_ptr[P]; k < o.poly_ptr[P + 1] && !any; ++k)
@@ -801,6 +806,8 @@ bool make_damping(Oracle& o) {
             o.abs_idx[P] = (int)o.Dabs.size();
             o.Dabs.emplace_back((size_t)nd * nd, 0.0);
             o.RW.emplace_back((size_t)nd * nd, 0.0);
+            o.Dabs_dev.emplace_back((size_t)nd * nd, 0.0);
+            o.RW_dev.emplace_back((size_t)nd * nd, 0.0);
         }
     }
     bool ok = true;
@@ -842,16 +849,33 @@ bool make_damping(Oracle& o) {
                                     D[(size_t)(i * Np + m) * nd + j * Np + n] += w * ar * val;
                                 }
                 }
+                // the device kernel's arrangement: C = c_t (I - n n^T) + c_n n n^T
+                std::vector<double>& Dd = o.Dabs_dev[a];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) {
+                        const double nij = nv[i] * nv[j];
+                        const double C = c1 * ((i == j ? 1.0 : 0.0) - nij) + c3 * nij;
+                        for (int m = 0; m < Np; ++m)
+                            for (int n = 0; n < Np; ++n) {
+                                double sq = 0.0;
+                                for (int q = 0; q < nq2; ++q)
+                                    sq = sq + o.Q.weitria2[q] * (phib[q * Np + m] * phib[q * Np + n]);
+                                Dd[(size_t)(i * Np + m) * nd + j * Np + n] += ar * C * sq;
+                            }
+                    }
             }
         }
         std::vector<double> W((size_t)nd * nd);
-        for (int r = 0; r < nd; ++r)
-            for (int c = 0; c < nd; ++c) {
-                const int i = r / Np, m = r % Np, j = c / Np, n = c % Np;
-                const double mv = (i == j) ? o.M[(size_t)P * Np * Np + (size_t)m * Np + n] : 0.0;
-                W[(size_t)r * nd + c] = mv + 0.5 * o.dt * D[(size_t)r * nd + c];
-            }
-        if (!cholesky(W.data(), nd, o.RW[a].data())) ok = false;
+        for (int v = 0; v < 2; ++v) {
+            const std::vector<double>& Dv = v == 0 ? D : o.Dabs_dev[a];
+            for (int r = 0; r < nd; ++r)
+                for (int c = 0; c < nd; ++c) {
+                    const int i = r / Np, m = r % Np, j = c / Np, n = c % Np;
+                    const double mv = (i == j) ? o.M[(size_t)P * Np * Np + (size_t)m * Np + n] : 0.0;
+                    W[(size_t)r * nd + c] = mv + 0.5 * o.dt * Dv[(size_t)r * nd + c];
+                }
+            if (!cholesky(W.data(), nd, (v == 0 ? o.RW[a] : o.RW_dev[a]).data())) ok = false;
+        }
     }
     return ok;
 }
@@ -1160,7 +1184,8 @@ void absorbing_step(const Oracle& o, double t, int P, double* out) {
     const std::vector<double>& u0 = o.slot[LYMPH_SLOT_U0];
     std::vector<double> tmp, b(nd), x(nd);
     apply_rhs(o, un, t, P, tmp);
-    const double* D = o.Dabs[a].data();
+    const double* D = (g_device_order ? o.Dabs_dev[a] : o.Dabs[a]).data();
+    const std::vector<double>& RW = g_device_order ? o.RW_dev[a] : o.RW[a];
     const size_t base = (size_t)P * nd;
     for (int r = 0; r < nd; ++r) {
         double dv = 0.0;
@@ -1173,7 +1198,7 @@ void absorbing_step(const Oracle& o, double t, int P, double* out) {
         std::vector<double> e(nd), col(nd), inv((size_t)nd * nd);
         for (int k = 0; k < nd; ++k) {
             for (int r = 0; r < nd; ++r) e[r] = (r == k) ? 1.0 : 0.0;
-            solve_LU_RT_R(o.RW[a].data(), e.data(), nd, col.data());
+            solve_LU_RT_R(RW.data(), e.data(), nd, col.data());
             for (int r = 0; r < nd; ++r) inv[(size_t)r * nd + k] = col[r];
         }
         for (int r = 0; r < nd; ++r) {
@@ -1195,7 +1220,7 @@ void absorbing_first_step(const Oracle& o, double t, int P, double* out) {
     const std::vector<double>& v0 = o.slot[LYMPH_SLOT_V0];
     std::vector<double> tmp, v(Np), x(Np);
     apply_rhs(o, u0, t, P, tmp);
-    const double* D = o.Dabs[a].data();
+    const double* D = (g_device_order ? o.Dabs_dev[a] : o.Dabs[a]).data();
     const size_t base = (size_t)P * nd;
     for (int r = 0; r < nd; ++r) {
         double dv = 0.0;
