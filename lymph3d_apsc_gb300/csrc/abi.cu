@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <string>
 #include <vector>
@@ -340,6 +341,10 @@ int lymph_create(const lymph_mesh_desc* m, const lymph_params* prm, lymph_ctx** 
     c->precision = prm->precision; c->alpha = prm->alpha; c->theta = prm->theta; c->dt = prm->dt;
     c->n_node = m->n_node; c->n_tet = nt; c->n_poly = np; c->n_mat = m->n_mat;
     c->mesh_hash = mesh_hash(m);
+    {
+        static std::atomic<uint64_t> next_uid{1};
+        c->uid = next_uid++;
+    }
     int rc = LYMPH_OK;
     auto fail = [&](int code) { lymph_destroy(c); return code; };
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -513,6 +518,7 @@ int lymph_make_matrices(lymph_ctx* c) {
             LYMPH_TRY(dalloc(c, &c->d_RmT, nm));
             LYMPH_TRY(dalloc(c, &c->d_Minv, nm));
         }
+        c->rhs_version++;
         LYMPH_TRY(make_mf_matrices(c));
         LYMPH_TRY(lymph_dev_cholesky(c));
         LYMPH_TRY(lymph_dev_damping(c, true));
@@ -541,6 +547,7 @@ int lymph_make_matrices(lymph_ctx* c) {
         LYMPH_TRY(dalloc(c, &c->d_Minv, nm));
     }
     c->k32_valid = false;  // an FP32 copy made from earlier blocks is stale
+    c->rhs_version++;      // and so is any cached M^-1 F
     LYMPH_TRY(lymph_dev_assemble(c, LYMPH_BLOCKS_K, c->d_K, c->precision == LYMPH_MIXED, true));
     LYMPH_TRY(lymph_dev_cholesky(c));
     LYMPH_TRY(lymph_dev_damping(c, true));
@@ -558,6 +565,7 @@ int lymph_make_rhs(lymph_ctx* c, int which, int fid, int did, int nid) {
     }
     if (!c->have_matrices) { lymph_set_error("lymph_make_rhs: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
     double* out = (which == LYMPH_RHS_STAT) ? c->d_rhs_stat : c->d_rhs_dyn;
+    c->rhs_version++;
     LYMPH_TRY(lymph_dev_vector(c, 0, fid, did, nid, 1.0, out));
     LYMPH_TRY(lymph_sync_status(c, "lymph_make_rhs"));
     if (which == LYMPH_RHS_STAT) c->have_rhs_stat = true; else c->have_rhs_dyn = true;
@@ -1004,6 +1012,7 @@ int lymph_make_rhs_point(lymph_ctx* c, int which, int32_t tet, const double* x0,
     int32_t P = 0;
     LYMPH_CUDA_TRY(cudaMemcpy(&P, c->d_tet_poly + tet, sizeof(int32_t), cudaMemcpyDeviceToHost));
     double* out = (which == LYMPH_RHS_STAT) ? c->d_rhs_stat : c->d_rhs_dyn;
+    c->rhs_version++;
     LYMPH_TRY(lymph_dev_point_source(c, P, x0, dir, out));
     LYMPH_TRY(lymph_sync_status(c, "lymph_make_rhs_point"));
     if (which == LYMPH_RHS_STAT) c->have_rhs_stat = true; else c->have_rhs_dyn = true;
@@ -1046,6 +1055,7 @@ int lymph_make_rhs_double_couple(lymph_ctx* c, int which, int32_t tet, const dou
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) moment[i * 3 + j] = (s[i] * n[j] + s[j] * n[i]) * M0 / vol;
     double* out = (which == LYMPH_RHS_STAT) ? c->d_rhs_stat : c->d_rhs_dyn;
+    c->rhs_version++;
     LYMPH_TRY(lymph_dev_double_couple(c, tet, P, moment, out));
     LYMPH_TRY(lymph_sync_status(c, "lymph_make_rhs_double_couple"));
     if (which == LYMPH_RHS_STAT) c->have_rhs_stat = true; else c->have_rhs_dyn = true;

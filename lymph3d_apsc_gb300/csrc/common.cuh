@@ -67,6 +67,8 @@ struct lymph_ctx {
     // sizes
     int n_node = 0, n_tet = 0, n_poly = 0, n_mat = 0;
     uint64_t mesh_hash = 0;         // FNV-1a of the mesh descriptor's arrays (checkpoints carry it)
+    uint64_t uid = 0;               // unique per context in the process (caches keyed by context)
+    int64_t rhs_version = 0;        // bumped whenever rhs_dyn or M^-1 change (caches of M^-1 F)
     int64_t n_blocks = 0, n_face_sides = 0, n_block_faces = 0;
     cudaStream_t stream = nullptr;
     // host copies needed for set-up logic

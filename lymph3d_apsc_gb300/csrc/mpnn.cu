@@ -262,6 +262,9 @@ struct lymph_mpnn {
     int64_t nv_cap = 0;
     double *d_d1 = nullptr, *d_d2 = nullptr, *d_ss = nullptr;
     double* d_u3 = nullptr;  // the predicted u^{n+K}, checked after the closing plain step
+    double* d_minvf = nullptr;        // M^-1 rhs_dyn of the context minvf_uid at its rhs_version minvf_ver
+    uint64_t minvf_uid = 0;
+    int64_t minvf_ver = -1;
     double* d_a1 = nullptr;  // dt^2 M^-1 (K d1 - gdiff F) (a feature)
     double* d_sig = nullptr;  // per-polyhedron scales [n_poly][4] of the last features
     const lymph_ctx* have_u3 = nullptr;      // context of the last prediction
@@ -684,50 +687,81 @@ __global__ void k_sum3(int nblk, const double* __restrict__ part, double* out) {
 // polyhedron's RMS of vector b plus 1e-3 x its mesh-wide RMS s_b (a floor
 // where the field is quiet).  sig[P][b] = r_b (the per-polyhedron scales of
 // the correction).
-constexpr int FEAT_THREADS = 128;  // >= 3 Np for p <= 4 (105)
+constexpr int FEAT_WARPS = 8;  // one warp per polyhedron, 8 per CTA
 
-__global__ void __launch_bounds__(FEAT_THREADS) k_features(
+// A positive double v as m 2^e with m in [1, 2) (m as a float, e an int);
+// v below the smallest normal double gives m = 0.  Integer and FP32 work only.
+__device__ __forceinline__ float split_pow2(double v, int* e) {
+    const long long bits = __double_as_longlong(v);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    if (ex == 0) { *e = 0; return 0.0f; }
+    *e = ex - 1023;
+    const float hi = __int_as_float(0x3f800000 | (int)((bits >> 29) & 0x7fffff));  // mantissa rounded down to 23 bits
+    return hi;
+}
+// 2^e as a double (e in the normal range)
+__device__ __forceinline__ double pow2d(int e) { return __longlong_as_double((long long)(e + 1023) << 52); }
+
+// sqrt(v) for a double v >= 0 to FP32 accuracy, over the whole double range,
+// without FP64 arithmetic: the exponent halved exactly, the mantissa's root in FP32
+__device__ __forceinline__ double sqrt_fp32acc(double v) {
+    int e;
+    float m = split_pow2(v, &e);
+    if (m == 0.0f) return 0.0;
+    if (e & 1) { m *= 2.0f; e -= 1; }
+    return (double)sqrtf(m) * pow2d(e / 2);
+}
+
+// The node features, a warp per polyhedron.  The GB300's FP64 pipe retires
+// one warp instruction per 64 cycles on each SM quarter however few lanes
+// are active, so the per-polyhedron scalar math (square roots, reciprocals,
+// logarithms) runs on split exponents and FP32 mantissas, lane-parallel: the
+// sums of squares are FP64, the scales carry FP32 rounding over the full
+// double range (the states of a quiet start are far below FP32's).
+__global__ void __launch_bounds__(32 * FEAT_WARPS) k_features(
     int n_poly, int nd, int F, const double* __restrict__ u1, const double* __restrict__ d1,
-    const double* __restrict__ d2, const double* __restrict__ a1, const double* __restrict__ ss, int64_t n_all,
-    const int32_t* __restrict__ pptr, const int32_t* __restrict__ ptets, const int32_t* __restrict__ tmat,
-    const double* __restrict__ mat, float* x, double* sig) {
-    __shared__ double red[4][FEAT_THREADS];
-    __shared__ double r[4];
-    const int P = blockIdx.x, tid = threadIdx.x;
+    const double* __restrict__ d2, const double* __restrict__ a1, const double* __restrict__ ss, double inv_nd,
+    double inv_nall, const int32_t* __restrict__ pptr, const int32_t* __restrict__ ptets,
+    const int32_t* __restrict__ tmat, const double* __restrict__ mat, float* x, double* sig) {
+    const int P = blockIdx.x * FEAT_WARPS + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (P >= n_poly) return;
     const int64_t q = (int64_t)P * nd;
     const double* vec[4] = {u1, d1, d2, a1};
+    double mine = 0.0;  // lane b (< 4): vector b's sum of squares
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
         double v = 0.0;
-        for (int c = tid; c < nd; c += FEAT_THREADS) {
+        for (int c = lane; c < nd; c += 32) {
             const double w = vec[b][q + c];
             v += w * w;
         }
-        red[b][tid] = v;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == b) mine = v;
     }
-    __syncthreads();
-    for (int w = FEAT_THREADS / 2; w > 0; w >>= 1) {
-        if (tid < w)
-            for (int b = 0; b < 4; ++b) red[b][tid] += red[b][tid + w];
-        __syncthreads();
-    }
-    if (tid < 4) {
-        const double glob = sqrt(ss[tid] / (double)n_all);
-        r[tid] = sqrt(red[tid][0] / (double)nd) + 1e-3 * glob + 1e-300;
-        sig[(int64_t)P * 4 + tid] = r[tid];
-    }
-    __syncthreads();
+    const int bl = lane & 3;
+    // r_b = RMS of the polyhedron's vector b + 1e-3 x its mesh-wide RMS (+ a floor)
+    const double rl = sqrt_fp32acc(mine * inv_nd) + 1e-3 * sqrt_fp32acc(ss[bl] * inv_nall) + 1e-300;
+    int er;
+    const float mr = split_pow2(rl, &er);
+    const double invl = (double)(1.0f / mr) * pow2d(-er);       // 1 / r_b
+    const float lgl = ((float)er + log2f(mr)) * 0.30102999566f;  // log10 r_b
+    if (lane < 4) sig[(int64_t)P * 4 + lane] = rl;
     float* row = x + (int64_t)P * F;
-    for (int c = tid; c < F; c += FEAT_THREADS) {
-        double v = 0.0;
-        if (c < 4 * nd) v = vec[c / nd][q + c % nd] / r[c / nd];
-        else if (c == 4 * nd) v = log10(r[1] / r[0]);
-        else if (c == 4 * nd + 1) v = log10(r[2] / r[1]);
-        else if (c == 4 * nd + 2) v = log10(r[3] / r[2]);
-        else if (c < 4 * nd + 6) v = mat[tmat[ptets[pptr[P]]] * 3 + (c - 4 * nd - 2) % 3];
-        row[c] = (float)v;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const double inv = __shfl_sync(0xffffffffu, invl, b);
+        for (int c = lane; c < nd; c += 32) row[b * nd + c] = (float)(vec[b][q + c] * inv);
     }
+    const float lg_next = __shfl_down_sync(0xffffffffu, lgl, 1);
+    const int c = 4 * nd + lane;
+    if (c < F) {
+        float v = 0.0f;
+        if (lane < 3) v = lg_next - lgl;  // log10(r_{b+1} / r_b)
+        else if (lane < 6) v = (float)mat[tmat[ptets[pptr[P]]] * 3 + (lane - 2) % 3];
+        row[c] = v;
+    }
+    for (int cc = c + 32; cc < F; cc += 32) row[cc] = 0.0f;
 }
 
 // y[q] = sum_c Minv_P[m, c] rhs[P, i, c] for q = (P, i, m): M^-1 applied to
@@ -784,26 +818,36 @@ __global__ void k_predict(int64_t n, int nd, int K, const double* __restrict__ u
                           const double* __restrict__ d2, const double* __restrict__ a1,
                           const double* __restrict__ sig, const float* __restrict__ y, int use_net,
                           double* out_a, double* out_b, double* out_c) {
+    // the extrapolation in FP64 with its coefficients formed once per thread;
+    // the network's correction (FP32 coefficients y, FP32 scale) in FP32
     const double Kd = (double)K;
+    double ck[3], ck2[3], ck3[3];
+    float cp3[3], cp4[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const double k = Kd - 3.0 + j;
+        const double c3 = k * (k + 1.0) * (k + 2.0);
+        ck[j] = k;
+        ck2[j] = 0.5 * k * (k + 1.0);
+        ck3[j] = c3 / 6.0;
+        cp3[j] = (float)(c3 / (Kd * Kd * Kd));
+        cp4[j] = (float)(c3 / (Kd * Kd * Kd) * (k + 3.0) / Kd);
+    }
+    const float k4 = (float)(Kd * Kd * Kd * Kd / 24.0);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t P = i / nd, c = i % nd;
-        double y3 = 0.0, y4 = 0.0, sc = 0.0;
+        const int64_t P = i / nd, c = i - P * nd;
+        float y3 = 0.0f, y4 = 0.0f;
         if (use_net) {
-            y3 = (double)y[P * 2 * nd + c];
-            y4 = (double)y[P * 2 * nd + nd + c];
-            const double r3 = sig[P * 4 + 2], r4 = sig[P * 4 + 3];
-            sc = (r4 * r4 / r3) * Kd * Kd * Kd * Kd / 24.0;
+            const float r3 = (float)sig[P * 4 + 2], r4 = (float)sig[P * 4 + 3];
+            const float sc = (r4 * r4 / r3) * k4;
+            y3 = sc * y[P * 2 * nd + c];
+            y4 = sc * y[P * 2 * nd + nd + c];
         }
+        const double vu = u1[i], vd1 = d1[i], vd2 = d2[i], va = a1[i];
         double* outs[3] = {out_a, out_b, out_c};
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const double k = Kd - 3.0 + j;
-            const double c3 = k * (k + 1.0) * (k + 2.0);
-            const double p3 = c3 / (Kd * Kd * Kd);
-            const double p4 = p3 * (k + 3.0) / Kd;
-            outs[j][i] = u1[i] + k * d1[i] + 0.5 * k * (k + 1.0) * d2[i] - (c3 / 6.0) * a1[i] +
-                         sc * (y3 * p3 + y4 * p4);
-        }
+        for (int j = 0; j < 3; ++j)
+            outs[j][i] = vu + ck[j] * vd1 + ck2[j] * vd2 - ck3[j] * va + (double)(y3 * cp3[j] + y4 * cp4[j]);
     }
 }
 
@@ -880,6 +924,7 @@ int lymph_mpnn_destroy(lymph_mpnn* n) {
     for (void* p : {(void*)n->d_p, (void*)n->d_g, (void*)n->d_m, (void*)n->d_v, (void*)n->d_pb, (void*)n->d_partial,
                     (void*)n->d_wt, (void*)n->d_status,
                     (void*)n->d_d1, (void*)n->d_d2, (void*)n->d_ss, (void*)n->d_u3, (void*)n->d_a1, (void*)n->d_sig,
+                    (void*)n->d_minvf,
                     (void*)n->d_x, (void*)n->d_z0, (void*)n->d_y, (void*)n->d_t, (void*)n->d_dy, (void*)n->d_gf,
                     (void*)n->d_yg, (void*)n->d_dyg,
                     (void*)n->d_dh, (void*)n->d_dz, (void*)n->d_dtmp, (void*)n->d_dm, (void*)n->d_wp, (void*)n->d_wi,
@@ -1060,14 +1105,16 @@ int surrogate_front(lymph_ctx* c, lymph_mpnn* n, bool with_features, double gdif
     }
     const int64_t nv = (int64_t)c->n_poly * nd;
     if (nv > n->nv_cap) {  // scratch grows once per (network, largest mesh) and is kept
-        for (double** p : {&n->d_d1, &n->d_d2, &n->d_ss, &n->d_u3, &n->d_a1, &n->d_sig})
+        for (double** p : {&n->d_d1, &n->d_d2, &n->d_ss, &n->d_u3, &n->d_a1, &n->d_sig, &n->d_minvf})
             if (*p) { cudaFree(*p); *p = nullptr; }
         n->nv_cap = 0;
+        n->minvf_uid = 0;
         if (cudaMalloc(&n->d_sig, sizeof(double) * 4 * (size_t)c->n_poly) != cudaSuccess ||
             cudaMalloc(&n->d_d1, sizeof(double) * nv) != cudaSuccess ||
             cudaMalloc(&n->d_d2, sizeof(double) * nv) != cudaSuccess ||
             cudaMalloc(&n->d_u3, sizeof(double) * nv) != cudaSuccess ||
             cudaMalloc(&n->d_a1, sizeof(double) * nv) != cudaSuccess ||
+            cudaMalloc(&n->d_minvf, sizeof(double) * nv) != cudaSuccess ||
             cudaMalloc(&n->d_ss, sizeof(double) * (6 * SS_BLOCKS + 6)) != cudaSuccess) {
             lymph_set_error(std::string(who) + ": out of memory");
             return LYMPH_ERR_OOM;
@@ -1089,14 +1136,23 @@ int surrogate_front(lymph_ctx* c, lymph_mpnn* n, bool with_features, double gdif
     const float* k32 = c->surrogate_apply_fp32 ? lymph_dev_blocks_f32(c) : nullptr;
     if (k32) LYMPH_TRY(lymph_dev_apply_fp32(c, k32, n->d_d1, n->d_a1));
     else LYMPH_TRY(lymph_dev_apply(c, n->d_d1, n->d_a1));
-    k_minv_rhs<<<1024, 256, 0, st>>>(c->n_poly, c->Np, c->d_Minv, c->d_rhs_dyn, n->d_u3);  // u3: free until k_predict
-    k_accel_combine<<<1024, 256, 0, st>>>(nv, c->dt * c->dt, gdiff, n->d_u3, n->d_a1);
+    // M^-1 F changes only with the source's right-hand side or the mass
+    // matrices: computed once per (context, right-hand side) and kept
+    if (n->minvf_uid != c->uid || n->minvf_ver != c->rhs_version) {
+        k_minv_rhs<<<1024, 256, 0, st>>>(c->n_poly, c->Np, c->d_Minv, c->d_rhs_dyn, n->d_minvf);
+        c->launches++;
+        n->minvf_uid = c->uid;
+        n->minvf_ver = c->rhs_version;
+    }
+    k_accel_combine<<<1024, 256, 0, st>>>(nv, c->dt * c->dt, gdiff, n->d_minvf, n->d_a1);
     k_one_sumsq<<<SS_BLOCKS, 256, 0, st>>>(nv, n->d_a1, part);
     k_sum3<<<1, 96, 0, st>>>(SS_BLOCKS, part, ss + 3);  // ss[3] (ss[4], ss[5] get zeros)
-    c->launches += 4;
+    c->launches += 3;
     if (with_features) {
-        k_features<<<c->n_poly, FEAT_THREADS, 0, st>>>(c->n_poly, nd, n->F, lymph_slot_ptr(c, LYMPH_SLOT_UN),
-                                                      n->d_d1, n->d_d2, n->d_a1, ss, nv, c->d_poly_ptr,
+        const unsigned blocks = (unsigned)((c->n_poly + FEAT_WARPS - 1) / FEAT_WARPS);
+        k_features<<<blocks, 32 * FEAT_WARPS, 0, st>>>(c->n_poly, nd, n->F, lymph_slot_ptr(c, LYMPH_SLOT_UN),
+                                                      n->d_d1, n->d_d2, n->d_a1, ss, 1.0 / nd, 1.0 / (double)nv,
+                                                      c->d_poly_ptr,
                                                       c->d_poly_tets, c->d_tet_mat, c->d_mat, n->d_x, n->d_sig);
         c->launches++;
     }

@@ -297,7 +297,9 @@ def test_device_features_match_host(require_gpu):
     # the rest of the features from the device's a1
     xh, sch, sigh, _, _ = S.features(um, u0, u1, a1_dev, S.poly_material(m), F)
     assert max(abs(a - b) / b for a, b in zip(sc, sch)) <= 1e-10
-    assert np.abs(sig / sigh - 1.0).max() <= 1e-10
+    # the per-polyhedron scales: sums of squares in FP64, the square roots in
+    # FP32 (the device keeps scalar per-polyhedron math off the FP64 pipe)
+    assert np.abs(sig / sigh - 1.0).max() <= 1e-6
     # float32 rows
     assert np.abs(x - xh).max() <= 1e-5 * np.abs(xh).max()
     assert rel(x[:, 3 * nd:4 * nd], xh[:, 3 * nd:4 * nd]) <= 1e-6
