@@ -86,7 +86,7 @@ CONFIGS = {
     # c2 mesh at p = 3, dt = 2e-5, a 50 Hz Ricker point source at the centre,
     # 2000 steps after 600 plain ones, K = 8
     "c4": dict(n=40, agglomeration="bfs", group=(4, 12), seed=0, p=3, material=(1.0, 1.0, 1.0), lognormal=True,
-               dt=2e-5, sample_n=None, surrogate=dict(n_traj=200, iters=20000, K=8, f0=50.0, warm=600,
+               dt=2e-5, sample_n=None, surrogate=dict(n_traj=200, iters=40000, K=8, f0=50.0, warm=600,
                                                       res_tols=(1e-6, 1e-5), sizes=(4, 5, 6, 8, 10),
                                                       stated_rel_l2=3e-4)),
 }
@@ -473,8 +473,18 @@ def run_ensemble(cfg, precision, steps, warmup, info):
     b.close()
     for s in solvers:
         s.close()
+    # the operator work of one step of every problem (block paths): 2 nnz FLOP
+    # plus the M^-1 apply and update, and the blocks' bytes
+    flops = bytes_ = 0.0
+    for mt in meta:
+        Np = (mt["p"] + 1) * (mt["p"] + 2) * (mt["p"] + 3) // 6
+        nd = 3 * Np
+        flops += 2.0 * mt["n_blocks"] * nd * nd + mt["n_poly"] * (3 * 2 * Np * Np + 6 * nd)
+        bytes_ += mt["n_blocks"] * nd * nd * (8 if precision == 0 else 4) + \
+            mt["n_poly"] * (3 * nd * 8 + 2 * Np * Np * 8 + 2 * nd * 8)
     return {"dofs": dofs, "steps": steps, "ms": ms, "seq_ms": seq_ms, "launches": launches, "clocks": clk.summary(),
-            "grid": grid, "order": order, "shape": shape, "finite": finite, "meta": meta}
+            "grid": grid, "order": order, "shape": shape, "finite": finite, "meta": meta,
+            "flops_per_step": flops, "bytes_per_step": bytes_}
 
 
 def run_surrogate(cfg, steps):
@@ -758,6 +768,14 @@ def main():
                            {"column_slices_p1_to_p4": list(BATCH_TILE_SHAPES[r["shape"]])}},
                 "sequential_value": r["dofs"] * r["steps"] / (r["seq_ms"] / 1e3),
                 "batched_speedup_vs_sequential": r["seq_ms"] / r["ms"],
+                "operator_work": None if precision == 2 else {
+                    "bound": "fp64" if precision == 0 else "hbm",
+                    "fp64_tflops_batched": r["flops_per_step"] * r["steps"] / (r["ms"] / 1e3) / 1e12,
+                    "fp64_tflops_sequential": r["flops_per_step"] * r["steps"] / (r["seq_ms"] / 1e3) / 1e12,
+                    "fp64_peak_tflops": FP64_NOMINAL_TFLOPS,
+                    "hbm_gbs_batched": r["bytes_per_step"] * r["steps"] / (r["ms"] / 1e3) / 1e9,
+                    "hbm_gbs_sequential": r["bytes_per_step"] * r["steps"] / (r["seq_ms"] / 1e3) / 1e9,
+                    "hbm_peak_gbs": measured_peaks()[0]},
                 "state_finite": r["finite"], "gpu_launches": r["launches"], "clocks": r["clocks"]}
         print(json.dumps(line), flush=True)
         return
