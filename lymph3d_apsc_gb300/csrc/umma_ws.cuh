@@ -11,10 +11,12 @@
 //               stage's "full" mbarrier with the bytes expected;
 //   warps 2..   split (WS_SPLIT_WARPS = 16 warps: the pass sets the pace of
 //               the ring, 4 warps took 0.73 ms per forward, 16 take 0.57):
-//               wait for "full", split the raw A tile in place into
-//               hi (low 13 mantissa bits cleared) and lo (the rest) — an
-//               elementwise pass, blind to the swizzle — fence the generic
-//               writes for the tensor core and arrive on "split";
+//               wait for "full", write the lo part of the raw A tile (the
+//               value minus the value with its low 13 mantissa bits cleared)
+//               into the lo tile — an elementwise pass, blind to the swizzle;
+//               the raw tile itself serves as hi, since kind::tf32 ignores
+//               those 13 bits — fence the generic writes for the tensor core
+//               and arrive on "split";
 //               afterwards the epilogue in groups of 4 warps on interleaved
 //               32-column blocks (warp w reads TMEM lanes 32 (w % 4) .. +31,
 //               transposed through shared memory into coalesced 16-byte row
@@ -178,17 +180,20 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_umma_gemm_ws(const __grid_con
         for (int kt = 0; kt < T; ++kt) {
             const int st = kt % WS_STAGES;
             if (!mbar_wait_ab(smem_u32(&full[st]), (uint32_t)((kt / WS_STAGES) & 1), abort)) break;
-            float4* hi = (float4*)(smem + st * WS_STAGE);
+            const float4* hi = (const float4*)(smem + st * WS_STAGE);
             float4* lo = (float4*)(smem + st * WS_STAGE + WS_TILE_A);
+            // kind::tf32 reads an FP32 operand's upper 19 bits and ignores the
+            // low 13 mantissa bits (checked on the device: the raw tile and
+            // the tile with those bits cleared give the same bits), so the
+            // raw tile is the hi part as it stands; only lo is written
 #pragma unroll 4
             for (int i = u; i < BM * BK / 4; i += WS_SPLIT) {
                 const float4 v = hi[i];
-                float4 h, l;
-                h.x = __uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u); l.x = v.x - h.x;
-                h.y = __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u); l.y = v.y - h.y;
-                h.z = __uint_as_float(__float_as_uint(v.z) & 0xFFFFE000u); l.z = v.z - h.z;
-                h.w = __uint_as_float(__float_as_uint(v.w) & 0xFFFFE000u); l.w = v.w - h.w;
-                hi[i] = h;
+                float4 l;
+                l.x = v.x - __uint_as_float(__float_as_uint(v.x) & 0xFFFFE000u);
+                l.y = v.y - __uint_as_float(__float_as_uint(v.y) & 0xFFFFE000u);
+                l.z = v.z - __uint_as_float(__float_as_uint(v.z) & 0xFFFFE000u);
+                l.w = v.w - __uint_as_float(__float_as_uint(v.w) & 0xFFFFE000u);
                 lo[i] = l;
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
