@@ -323,7 +323,8 @@ int lymph_mpnn_forward(lymph_mpnn* net, const float* x, float* y);
 int lymph_mpnn_loss_grad(lymph_mpnn* net, const float* x, const float* target, double* loss);
 int lymph_mpnn_adam(lymph_mpnn* net, float lr, float beta1, float beta2, float eps);
 int lymph_mpnn_launch_count(const lymph_mpnn* net, int64_t* count);
-/* Average device time of `reps` forwards on the features already on the
+/* Average device time of `reps` inference forwards (no pre-activation
+ * stores, as lymph_mpnn_forward runs it) on the features already on the
  * device (after a lymph_mpnn_forward), CUDA events on the network's stream. */
 int lymph_mpnn_time_forward(lymph_mpnn* net, int32_t reps, double* ms);
 /* 1 when the forward GEMMs run on the tensor cores (tcgen05, TF32 hi/lo split

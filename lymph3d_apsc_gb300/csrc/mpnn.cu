@@ -490,8 +490,11 @@ int ensure_capacity(lymph_mpnn* n, int N) {
     return LYMPH_OK;
 }
 
-// forward on the current graph; x in d_x, g in d_gf, output in d_y
-void forward(lymph_mpnn* n) {
+// forward on the current graph; x in d_x, g in d_gf, output in d_y.
+// keep_z: also store the pre-activations z0 / zm / zu the backward pass
+// reads; inference (forward, predict) leaves them out on the tensor-core
+// path, one N x H store per GEMM fewer.
+void forward(lymph_mpnn* n, bool keep_z = true) {
     const int N = n->n_nodes, H = n->H, F = n->F, G = n->G, O = n->O;
     const bool tc = umma_ok(n, H, {F, H, G}) && umma_ok(n, O, {H});
     if (tc) {
@@ -499,16 +502,17 @@ void forward(lymph_mpnn* n) {
         // a = W m, h1 = h + relu([h a g] Wu + bu); y = h Wo + bo
         refresh_wt(n);
         umma::Seg s0[1] = {{n->d_x, F, F}};
-        umma_gemm(n, (int)pidx(n, "W0", 0), N, s0, 1, P_(n, "b0"), n->d_h[0], H, n->d_z0, nullptr, umma::EPI_RELU);
+        umma_gemm(n, (int)pidx(n, "W0", 0), N, s0, 1, P_(n, "b0"), n->d_h[0], H, keep_z ? n->d_z0 : nullptr,
+                  nullptr, umma::EPI_RELU);
         for (int l = 0; l < n->L; ++l) {
             float* h = n->d_h[l];
             umma::Seg sm[1] = {{h, H, H}};
-            umma_gemm(n, (int)pidx(n, "Wm", l), N, sm, 1, P_(n, "bm", l), n->d_m_[l], H, n->d_zm[l], nullptr,
-                      umma::EPI_RELU);
+            umma_gemm(n, (int)pidx(n, "Wm", l), N, sm, 1, P_(n, "bm", l), n->d_m_[l], H,
+                      keep_z ? n->d_zm[l] : nullptr, nullptr, umma::EPI_RELU);
             aggregate(n, false, H, n->d_m_[l], n->d_a[l]);
             umma::Seg su[3] = {{h, H, H}, {n->d_a[l], H, H}, {n->d_gf, G, G}};
-            umma_gemm(n, (int)pidx(n, "Wu", l), N, su, 3, P_(n, "bu", l), n->d_h[l + 1], H, n->d_zu[l], h,
-                      umma::EPI_RES_RELU);
+            umma_gemm(n, (int)pidx(n, "Wu", l), N, su, 3, P_(n, "bu", l), n->d_h[l + 1], H,
+                      keep_z ? n->d_zu[l] : nullptr, h, umma::EPI_RES_RELU);
         }
         umma::Seg so[1] = {{n->d_h[n->L], H, H}};
         umma_gemm(n, (int)pidx(n, "Wo", 0), N, so, 1, P_(n, "bo"), n->d_y, O, nullptr, nullptr, umma::EPI_STORE);
@@ -975,7 +979,7 @@ int lymph_mpnn_set_graph(lymph_mpnn* n, int32_t n_nodes, const int32_t* w_ptr, c
 int lymph_mpnn_forward(lymph_mpnn* n, const float* x, float* y) {
     if (!n || !x || !y || n->n_nodes <= 0) return LYMPH_ERR_INVALID;
     LYMPH_CUDA_TRY(cudaMemcpyAsync(n->d_x, x, sizeof(float) * (size_t)n->n_nodes * n->F, cudaMemcpyHostToDevice, n->stream));
-    forward(n);
+    forward(n, false);
     LYMPH_CUDA_TRY(cudaGetLastError());
     LYMPH_CUDA_TRY(cudaMemcpyAsync(y, eff_out(n), sizeof(float) * (size_t)n->n_nodes * eff_width(n),
                                    cudaMemcpyDeviceToHost, n->stream));
@@ -1031,7 +1035,8 @@ int lymph_mpnn_set_gate(lymph_mpnn* n, int32_t nd, int32_t B) {
     return LYMPH_OK;
 }
 
-// Device time of the forward on the features already on the device (from
+// Device time of the inference forward (as lymph_mpnn_forward and the
+// surrogate's predict run it) on the features already on the device (from
 // the last lymph_mpnn_forward / _loss_grad): `reps` forwards between two CUDA
 // events on the network's stream; *ms = the average.
 int lymph_mpnn_time_forward(lymph_mpnn* n, int32_t reps, double* ms) {
@@ -1039,9 +1044,9 @@ int lymph_mpnn_time_forward(lymph_mpnn* n, int32_t reps, double* ms) {
     cudaEvent_t e0, e1;
     LYMPH_CUDA_TRY(cudaEventCreate(&e0));
     LYMPH_CUDA_TRY(cudaEventCreate(&e1));
-    forward(n);  // weight copies refreshed outside the timed region
+    forward(n, false);  // weight copies refreshed outside the timed region
     cudaEventRecord(e0, n->stream);
-    for (int r = 0; r < reps; ++r) forward(n);
+    for (int r = 0; r < reps; ++r) forward(n, false);
     cudaEventRecord(e1, n->stream);
     cudaError_t e = cudaEventSynchronize(e1);
     float t = 0.0f;
@@ -1223,7 +1228,7 @@ int lymph_surrogate_predict(lymph_ctx* c, lymph_mpnn* n, int32_t K, int32_t use_
         cudaStream_t own = n->stream;
         n->stream = st;
         const int64_t before = n->launches;
-        forward(n);
+        forward(n, false);
         c->launches += n->launches - before;
         n->stream = own;
     }
