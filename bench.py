@@ -314,14 +314,17 @@ def prepare(cfg, precision):
     m = make_mesh(cfg)
     t1 = time.perf_counter()
     g = MatrixFree(m, cfg["p"], cfg["dt"], precision=precision)
-    g.MAKE_MATRICES_FREE()
+    ta = time.perf_counter()
+    g.MAKE_MATRICES_FREE()   # returns once the device is done (it reads back the status word)
+    g.make_matrices_s = time.perf_counter() - ta
     g.MAKE_RHS_FREE(_lib.RHS_STAT, _lib.F_NULL, _lib.GD_NULL, _lib.GN_NULL)
     g.MAKE_RHS_FREE(_lib.RHS_DYN, _lib.F_TIME, _lib.GD, _lib.GN)
     g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_DISPLACEMENT, _lib.SLOT_U0)
     g.COMPUTE_MODAL_COEFFICIENTS_FREE(_lib.FUN_IC_VELOCITY, _lib.SLOT_V0)
     g.FIRST_TIME_STEP_MATRIX_FREE(0.0)
     t2 = time.perf_counter()
-    log(f"[bench] mesh {m.n_tet} tets / {m.n_poly} polyhedra in {t1 - t0:.1f}s; device set-up {t2 - t1:.1f}s; "
+    log(f"[bench] mesh {m.n_tet} tets / {m.n_poly} polyhedra in {t1 - t0:.1f}s; device set-up {t2 - t1:.1f}s "
+        f"(MAKE_MATRICES_FREE {g.make_matrices_s:.2f}s); "
         f"{g.n_blocks} blocks, {g.device_bytes() / 1e9:.2f} GB on device")
     return m, g
 
@@ -391,7 +394,8 @@ def run_gpu(cfg, precision, steps, warmup, rank_info, want_e2e=True):
     t, n2, ms2, mk = g.run_steps(t, 1e30, steps, kernel_timing=True)
     out = {"dofs": dofs, "steps": n, "ms": ms, "kernel_ms_avg": mk / n2, "launches": launches,
            "clocks": clk.summary(), "n_blocks": g.n_blocks, "n_poly": g.n_poly, "n_tet": m.n_tet, "Np": g.Np,
-           "bytes": step_bytes(g, precision), "flops": step_flops(g), "t": t}
+           "bytes": step_bytes(g, precision), "flops": step_flops(g), "t": t,
+           "make_matrices_s": g.make_matrices_s}
     if precision == 2:
         out["mf_flops"] = mf_flops(g)
     # errors after ERROR_STEPS steps in all (the configurations' 1000-step
@@ -809,6 +813,7 @@ def main():
         "data": "synthetic (generated cube mesh, manufactured solution; no public dataset)",
         "config": workload_config(cfg, r["n_tet"], r["n_poly"], r["Np"], r["n_blocks"], args.precision, info["world"]),
         "err_L2": r["err_L2"], "err_DG": r["err_DG"], "error_after_steps": r["error_steps"],
+        "make_matrices_s": r["make_matrices_s"],
         "roofline": roof,
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
@@ -840,7 +845,7 @@ def main():
                          "err_DG_ratio_vs_fp64": rm["err_DG"] / r["err_DG"],
                          "error_after_steps": rm["error_steps"], "kernel_ms": rm["kernel_ms_avg"],
                          "achieved_gbs": rm["bytes"] / (rm["kernel_ms_avg"] / 1e3) / 1e9,
-                         "bytes_per_launch": rm["bytes"]}
+                         "bytes_per_launch": rm["bytes"], "make_matrices_s": rm["make_matrices_s"]}
             if "mf_flops" in rm:
                 line[key]["fp32_tflops"] = rm["mf_flops"] / (rm["kernel_ms_avg"] / 1e3) / 1e12
                 line[key]["flops_per_launch"] = rm["mf_flops"]

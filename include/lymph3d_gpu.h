@@ -401,6 +401,12 @@ int lymph_compute_error_dg_free(lymph_ctx* ctx, int slot_uh, int slot_uex, doubl
  * mixed precision (the FP32 values are widened). */
 int lymph_get_pattern(lymph_ctx* ctx, int32_t* row_ptr, int32_t* col);
 int lymph_get_blocks(lymph_ctx* ctx, int which, double* vals);
+/* The self blocks the step kernels apply, vals[n_poly][3Np][3Np] row-major:
+ * the FP64 blocks, or the stored FP32 values widened (LYMPH_MIXED_MF: the
+ * tensor-core assembly of MAKE_STIFFNESS_VOLUME + MAKE_STIFFNESS_FACE's
+ * self terms, src/assemble_element.f90:24-77, 404-661).  A read-back for
+ * parity checks; no counterpart in the reference. */
+int lymph_get_self_blocks(lymph_ctx* ctx, double* vals);
 /* Mass data per polyhedron, [n_poly][Np][Np] row-major: which = 0 M_loc (rho
  * weighted), 1 M_modal_loc, 2 R_M_loc (upper Cholesky factor), 3 R_M_modal_loc,
  * 4 the inverse of M_loc the step kernel applies. */

@@ -97,6 +97,7 @@ _SIGS = {
     "lymph_compute_error_dg_free": (c_int, [c_void_p, c_int, c_int, P_F64]),
     "lymph_get_pattern": (c_int, [c_void_p, P_I32, P_I32]),
     "lymph_get_blocks": (c_int, [c_void_p, c_int, P_F64]),
+    "lymph_get_self_blocks": (c_int, [c_void_p, P_F64]),
     "lymph_get_mass": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_get_rhs": (c_int, [c_void_p, c_int, P_F64]),
     "lymph_get_poly_geometry": (c_int, [c_void_p, P_F64, P_F64]),

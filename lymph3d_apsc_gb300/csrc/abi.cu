@@ -26,6 +26,8 @@ int lymph_dev_assemble_list(lymph_ctx* c, int which, void* out, int out_fp32, bo
 int lymph_mf_setup(lymph_ctx* c, const RefTables& R);
 int lymph_dev_cholesky(lymph_ctx* c);
 int lymph_dev_damping(lymph_ctx* c, bool assemble);
+int lymph_dev_mass(lymph_ctx* c, const int64_t* self_list);
+int lymph_dev_self_tc(lymph_ctx* c, float* out);
 int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scale, double* out);
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
@@ -473,8 +475,9 @@ int lymph_sizes(const lymph_ctx* c, int32_t* Np, int32_t* n_poly, int64_t* n_blo
     return LYMPH_OK;
 }
 
-// Matrix-free neighbour terms: the FP32 self blocks (assembled alone, into
-// consecutive slots) and the per-triangle / per-polyhedron FP32 tables.
+// Matrix-free neighbour terms: the FP32 self blocks (on the tensor cores,
+// one per polyhedron in consecutive slots), the FP64 mass matrices and the
+// per-triangle / per-polyhedron FP32 tables.
 static int make_mf_matrices(lymph_ctx* c) {
     const int np = c->n_poly, nd = c->nd;
     const size_t nK = (size_t)np * nd * nd;
@@ -495,7 +498,8 @@ static int make_mf_matrices(lymph_ctx* c) {
     LYMPH_CUDA_TRY(cudaMalloc(&d_list, sizeof(int64_t) * (size_t)np));
     int rc = cudaMemcpy(d_list, self.data(), sizeof(int64_t) * (size_t)np, cudaMemcpyHostToDevice) == cudaSuccess
                  ? LYMPH_OK : LYMPH_ERR_CUDA;
-    if (rc == LYMPH_OK) rc = lymph_dev_assemble_list(c, LYMPH_BLOCKS_K, c->d_K, 1, true, d_list, np, (int64_t)nd * nd);
+    if (rc == LYMPH_OK) rc = lymph_dev_mass(c, d_list);
+    if (rc == LYMPH_OK) rc = lymph_dev_self_tc(c, (float*)c->d_K);
     if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
     cudaFree(d_list);
     LYMPH_TRY(rc);
@@ -971,6 +975,31 @@ int lymph_get_blocks(lymph_ctx* c, int which, double* vals) {
         for (int r = 0; r < nd; ++r)
             for (int cc = 0; cc < nd; ++cc) vals[((size_t)b * nd + r) * nd + cc] = tmp[((size_t)b * nd + cc) * nd + r];
     return lymph_sync_status(c, "lymph_get_blocks");
+}
+
+int lymph_get_self_blocks(lymph_ctx* c, double* vals) {
+    if (!c || !vals) return LYMPH_ERR_INVALID;
+    if (!c->have_matrices) { lymph_set_error("lymph_get_self_blocks: call lymph_make_matrices first"); return LYMPH_ERR_ORDER; }
+    const int nd = c->nd;
+    const size_t nb = (size_t)nd * nd;
+    std::vector<double> tmp(nb);
+    std::vector<float> tf(nb);
+    for (int P = 0; P < c->n_poly; ++P) {
+        // MIXED_MF stores the self blocks alone, one per polyhedron; the
+        // block-CSR modes store each row's self block first
+        const size_t slot = c->precision == LYMPH_MIXED_MF ? (size_t)P : (size_t)c->h_row_ptr[P];
+        if (c->precision == LYMPH_FP64) {
+            LYMPH_CUDA_TRY(cudaMemcpy(tmp.data(), (const double*)c->d_K + slot * nb, nb * sizeof(double),
+                                      cudaMemcpyDeviceToHost));
+        } else {
+            LYMPH_CUDA_TRY(cudaMemcpy(tf.data(), (const float*)c->d_K + slot * nb, nb * sizeof(float),
+                                      cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < nb; ++i) tmp[i] = tf[i];
+        }
+        for (int r = 0; r < nd; ++r)
+            for (int cc = 0; cc < nd; ++cc) vals[((size_t)P * nd + r) * nd + cc] = tmp[(size_t)cc * nd + r];
+    }
+    return lymph_sync_status(c, "lymph_get_self_blocks");
 }
 
 int lymph_get_mass(lymph_ctx* c, int which, double* vals) {

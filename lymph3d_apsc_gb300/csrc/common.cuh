@@ -252,5 +252,46 @@ __device__ __forceinline__ void sum_fixed_order_1024(int64_t n, const double* __
     if (threadIdx.x == 0) *out = red[0];
 }
 
+// ---------------------------------------------------------------------------
+// FP32 basis tabulation shared by the mixed kernels (mf.cu, selftc.cu)
+// ---------------------------------------------------------------------------
+// The reference's basis order (basis_list, basis_function.f90:12-44): degree
+// triples (x, y, z) for q1 = p..0, q2 = p-q1..0, q3 = p-q1-q2..0.
+template <int PD> struct Blist {
+    int d[(PD + 1) * (PD + 2) * (PD + 3) / 6][3];
+    constexpr Blist() : d() {
+        int ii = 0;
+        for (int q1 = PD; q1 >= 0; --q1)
+            for (int q2 = PD - q1; q2 >= 0; --q2)
+                for (int q3 = PD - q1 - q2; q3 >= 0; --q3) {
+                    d[ii][0] = q1;
+                    d[ii][1] = q2;
+                    d[ii][2] = q3;
+                    ++ii;
+                }
+    }
+};
+
+// Legendre polynomials L_0..L_PD on [-1, 1] and their derivatives at x,
+// as (L, L') pairs (Bonnet's recurrence; the reference evaluates the same
+// polynomials in closed form, basis_function.f90:268-437).
+template <int PD>
+__device__ __forceinline__ void legendre_f32(float x, float2* out) {
+    float Lv[PD + 1], Ld[PD + 1];
+    Lv[0] = 1.0f;
+    Ld[0] = 0.0f;
+    if (PD >= 1) {
+        Lv[1] = x;
+        Ld[1] = 1.0f;
+    }
+#pragma unroll
+    for (int n = 1; n < PD; ++n) {
+        Lv[n + 1] = ((2 * n + 1) * x * Lv[n] - n * Lv[n - 1]) * (1.0f / (n + 1));
+        Ld[n + 1] = Ld[n - 1] + (2 * n + 1) * Lv[n];
+    }
+#pragma unroll
+    for (int n = 0; n <= PD; ++n) out[n] = make_float2(Lv[n], Ld[n]);
+}
+
 // launch helpers (defined in abi.cu)
 int lymph_sync_status(lymph_ctx* c, const char* where);

@@ -140,44 +140,6 @@ template <int PD> struct MfShape {
     static_assert(ND <= MF_THREADS, "one thread per row of the self block");
 };
 
-// The reference's basis order (basis_list, basis_function.f90:12-44): degree
-// triples (x, y, z) for q1 = p..0, q2 = p-q1..0, q3 = p-q1-q2..0.
-template <int PD> struct Blist {
-    int d[Deg<PD>::NP][3];
-    constexpr Blist() : d() {
-        int ii = 0;
-        for (int q1 = PD; q1 >= 0; --q1)
-            for (int q2 = PD - q1; q2 >= 0; --q2)
-                for (int q3 = PD - q1 - q2; q3 >= 0; --q3) {
-                    d[ii][0] = q1;
-                    d[ii][1] = q2;
-                    d[ii][2] = q3;
-                    ++ii;
-                }
-    }
-};
-
-// Legendre polynomials L_0..L_PD on [-1, 1] and their derivatives at x,
-// as (L, L') pairs (Bonnet's recurrence; the reference evaluates the same
-// polynomials in closed form, basis_function.f90:268-437).
-template <int PD>
-__device__ __forceinline__ void legendre(float x, float2* out) {
-    float Lv[PD + 1], Ld[PD + 1];
-    Lv[0] = 1.0f;
-    Ld[0] = 0.0f;
-    if (PD >= 1) {
-        Lv[1] = x;
-        Ld[1] = 1.0f;
-    }
-#pragma unroll
-    for (int n = 1; n < PD; ++n) {
-        Lv[n + 1] = ((2 * n + 1) * x * Lv[n] - n * Lv[n - 1]) * (1.0f / (n + 1));
-        Ld[n + 1] = Ld[n - 1] + (2 * n + 1) * Lv[n];
-    }
-#pragma unroll
-    for (int n = 0; n <= PD; ++n) out[n] = make_float2(Lv[n], Ld[n]);
-}
-
 // Position of basis function (a, b, c) in the reference's order.
 template <int PD> struct Bidx {
     int i[PD + 1][PD + 1][PD + 1];
@@ -432,9 +394,9 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
             }
             const MfPoly& pq = s_polyQ[b][t];
             float2 X[L], Y[L], Z[L];
-            legendre<PD>(xq[0] * pq.ih[0], X);
-            legendre<PD>(xq[1] * pq.ih[1], Y);
-            legendre<PD>(xq[2] * pq.ih[2], Z);
+            legendre_f32<PD>(xq[0] * pq.ih[0], X);
+            legendre_f32<PD>(xq[1] * pq.ih[1], Y);
+            legendre_f32<PD>(xq[2] * pq.ih[2], Z);
             // Q's map: phi = sc L L L, d_k phi = sc ih_k (...)
             const float sq = pq.sc, gx = sq * pq.ih[0], gy = sq * pq.ih[1], gz = sq * pq.ih[2];
             float v[3], D[3][3];
@@ -476,9 +438,9 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
             // stores of a quarter-warp on distinct banks)
             constexpr int LW = (3 * L + 1) / 2;
             float2 LP[2 * LW];
-            legendre<PD>(xp[0] * pP.ih[0], LP);
-            legendre<PD>(xp[1] * pP.ih[1], LP + L);
-            legendre<PD>(xp[2] * pP.ih[2], LP + 2 * L);
+            legendre_f32<PD>(xp[0] * pP.ih[0], LP);
+            legendre_f32<PD>(xp[1] * pP.ih[1], LP + L);
+            legendre_f32<PD>(xp[2] * pP.ih[2], LP + 2 * L);
             if (2 * LW > 3 * L) LP[2 * LW - 1] = make_float2(0.0f, 0.0f);
             float4* lw = reinterpret_cast<float4*>(s_w.loop.leg[tid]);
 #pragma unroll

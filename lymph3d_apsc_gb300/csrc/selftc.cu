@@ -1,0 +1,439 @@
+// selftc.cu -- the FP32 self blocks of the mixed operator (LYMPH_MIXED_MF)
+// assembled on the 5th-generation tensor cores (tcgen05, kind::tf32).
+//
+// The self block K_PP of MAKE_MATRICES_FREE (src/matrix_free.f90:27-464) is
+// the volume stiffness of P's sub-tetrahedra (MAKE_STIFFNESS_VOLUME,
+// src/assemble_element.f90:24-77) plus the self part of the face terms on
+// P's Dirichlet faces and on the faces it shares with other polyhedra
+// (MAKE_STIFFNESS_FACE, :404-661).  Every one of its terms is a sum over
+// quadrature points of a product of two basis tabulations, so with rows
+// r = (i, a) and columns c = (j, b) (component, basis function) the block is
+// two matrix products over a common K dimension of quadrature slots plus a
+// re-indexing:
+//     K_PP[(i,a),(j,b)] = O_D[(i,a),(j,b)] + O_S[(j,a),(i,b)]
+//                         + delta_ij sum_k O_S[(k,a),(k,b)],
+//     O_D = A B_D^T,  O_S = A B_S^T,
+// where, per slot, the A row (i, a) and the B rows (j, b) are
+//   volume point (w = weight |J|):   A = d_i phi_a,
+//       B_D = w lambda d_j phi_b,  B_S = w mu d_j phi_b
+//   face point, "d" slot (W = weight * area, cI = 1 on Dirichlet faces,
+//   1/2 on shared ones, n P's outward normal):  A = d_i phi_a,
+//       B_D = theta cI W lambda n_j phi_b,  B_S = theta cI W mu n_j phi_b
+//   face point, "n phi" slot:  A = n_i phi_a,
+//       B_D = -cI W lambda d_j phi_b,  B_S = sigma W / 2 n_j phi_b - cI W mu d_j phi_b.
+// O_D gives lambda G_ij of the volume term and the lambda parts of the
+// consistency and symmetry integrals; the block transpose of O_S gives
+// mu G_ji, their mu parts and the penalty's n_i n_j part; the trace of O_S
+// gives the delta_ij mu tr G term, the delta_ij mu n.H terms and the
+// penalty's identity part (sum_k n_k^2 = 1).  Each face point enters twice
+// (a "d" slot and an "n phi" slot); face integrals use the symmetric
+// triangle rule exact to degree 2p of the matrix-free kernel (mf.cu), whose
+// integrals equal the reference's collapsed rule's in exact arithmetic,
+// volume integrals the reference's collapsed Gauss rule.
+//
+// One CTA of 512 threads per polyhedron.  The K slots come in chunks of 32
+// (the tetrahedra's volume points, then the faces); per chunk warp 0 maps
+// each slot to its physical point, weights and Legendre values, all 16
+// warps write the operands into shared memory, each value split into its
+// nearest TF32 value and the TF32-rounded remainder (together within 2^-23
+// of the value), in the 128-byte-swizzled K-major layout the MMA reads, and
+// thread 0 issues the four products A_hi B_hi + A_hi B_lo + A_lo B_hi +
+// A_lo B_lo (FP32-accurate, not TF32 rounded) into an FP32 accumulator in
+// tensor memory.  Two operand stages
+// let the tabulation of one chunk overlap the MMAs of the last.  The tensor
+// cores add each MMA's products to the accumulator with truncation (round
+// toward zero: an emulation with that rounding reproduces the measured
+// errors, one with round-to-nearest gives 10x less), so the error grows
+// with the number of MMAs an accumulator takes.  Each chunk's 16 MMAs
+// therefore go into a fresh accumulator, drained into FP32 registers (round
+// to nearest) two chunks later while the next chunk accumulates into the
+// other of two accumulators: 3.5e-7 per row at p = 4 in that emulation,
+// against 1.2-1.6e-6 with one drain every 4 chunks.  The epilogue
+// stages O_D and O_S in shared memory, applies the re-indexing and writes
+// the block column-major, coalesced.  Every mbarrier wait is bounded; on
+// expiry the kernel sets ST_TIMEOUT, waits (bounded) for its MMAs in flight,
+// frees its tensor memory and returns.
+
+#include <cstddef>
+
+#include "common.cuh"
+#include "tc_prims.cuh"
+
+extern "C" int lymph_mf_face_rule(int32_t p, int32_t* n, double* xyw);
+
+namespace {
+
+using namespace umma;
+
+constexpr int ST_THREADS = 512;   // 16 warps: 4 per tensor-memory lane quadrant
+constexpr int ST_BK = 32;         // K slots per chunk (4 MMAs of K = 8)
+constexpr int ST_SEG = 1;         // chunks per accumulation segment (drained into registers after each)
+constexpr int ST_FACE_NQ[5] = {0, 3, 6, 12, 16};   // nodes of the symmetric triangle rule (mf.cu)
+
+template <int PD> struct TcShape {
+    static constexpr int NP = (PD + 1) * (PD + 2) * (PD + 3) / 6;
+    static constexpr int ND = 3 * NP;
+    static constexpr int NQ3 = (PD + 1) * (PD + 1) * (PD + 1);
+    static constexpr int NF = ST_FACE_NQ[PD];
+    static constexpr int FPC = (ST_BK / (2 * NF)) > 0 ? ST_BK / (2 * NF) : 1;   // faces per chunk
+    static constexpr int CPT = (NQ3 + ST_BK - 1) / ST_BK;                       // chunks per tetrahedron
+    static constexpr int NH = (ND + 15) / 16 * 16;   // columns of O_D (and of O_S)
+    static constexpr int NT = 2 * NH;                // the MMA's N: O_D | O_S
+    static constexpr int NCOL = NT / 4;              // accumulator columns drained per thread
+    static constexpr int TCOLS = 2 * NT <= 64 ? 64 : (2 * NT <= 128 ? 128 : (2 * NT <= 256 ? 256 : 512));
+    static constexpr int LS = (3 * (PD + 1)) | 1;    // (L, L') pairs per slot, odd: no bank conflicts
+    static constexpr size_t A_TILE = 128 * 128;      // 128 rows x 32 TF32 slots
+    static constexpr size_t B_TILE = (size_t)NT * 128;
+    static constexpr size_t STAGE = 2 * A_TILE + 2 * B_TILE;
+    static constexpr size_t LEG_OFF = 2 * STAGE;
+    static constexpr size_t COEF_OFF = LEG_OFF + (size_t)ST_BK * LS * 8;
+    static constexpr size_t BAR_OFF = COEF_OFF + (size_t)ST_BK * 3 * 16;
+    static constexpr size_t SMEM = BAR_OFF + 64 + 1024;   // + room to align the base to 1 KB
+    static_assert(NT <= 256 && NT % 16 == 0, "MMA N");
+    static_assert(2 * NT <= TCOLS, "two accumulators");
+    static_assert(NCOL % 8 == 0, "drain in x16/x8 loads");
+    static_assert(2 * (size_t)ND * ND * 4 <= 2 * STAGE, "epilogue staging fits the operand stages");
+    static_assert(COEF_OFF % 16 == 0 && BAR_OFF % 8 == 0, "alignment");
+};
+
+// the reference's basis order as degree triples, per degree
+__constant__ Blist<1> c_bl1 = Blist<1>{};
+__constant__ Blist<2> c_bl2 = Blist<2>{};
+__constant__ Blist<3> c_bl3 = Blist<3>{};
+__constant__ Blist<4> c_bl4 = Blist<4>{};
+template <int PD> __device__ __forceinline__ int3 blist_row(int a);
+template <> __device__ __forceinline__ int3 blist_row<1>(int a) { return make_int3(c_bl1.d[a][0], c_bl1.d[a][1], c_bl1.d[a][2]); }
+template <> __device__ __forceinline__ int3 blist_row<2>(int a) { return make_int3(c_bl2.d[a][0], c_bl2.d[a][1], c_bl2.d[a][2]); }
+template <> __device__ __forceinline__ int3 blist_row<3>(int a) { return make_int3(c_bl3.d[a][0], c_bl3.d[a][1], c_bl3.d[a][2]); }
+template <> __device__ __forceinline__ int3 blist_row<4>(int a) { return make_int3(c_bl4.d[a][0], c_bl4.d[a][1], c_bl4.d[a][2]); }
+
+struct SelfTcArgs {
+    const int32_t* poly_ptr;
+    const int32_t* poly_tets;
+    const int32_t* tet_poly;
+    const int32_t* tet_mat;
+    const int32_t* neigh;
+    const double* mat;
+    const double* fk;
+    const double* jdet;
+    const double* nrm;
+    const double* area;
+    const double* bbox;
+    const double* hk;
+    const RefTables* ref;
+    const int32_t* row_ptr;
+    const int64_t* bf_ptr;
+    const int32_t* bf;
+    double alpha, theta;
+    float* out;            // [n_poly][ND * ND], column-major blocks
+    int* status;
+    double frule[3 * 16];  // (xi, eta, w) of the symmetric triangle rule
+};
+
+// v rounded to the nearest TF32 value (10 explicit mantissa bits; ties away
+// from zero), exact in TF32
+__device__ __forceinline__ float tf32_rn(float v) { return __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u); }
+
+// value v into row `row`, slot k of a 128-byte-swizzled K-major tile pair:
+// hi = v rounded to TF32, lo = the remainder v - hi (exact in FP32, at most
+// 2^-11 |v|) rounded to TF32, so v = hi + lo to within 2^-23 |v| and the
+// MMA, which reads only the TF32 bits, sees both exactly
+__device__ __forceinline__ void put_split(char* hi, char* lo, int row, int k, float v) {
+    const int off = row * 128 + ((((k >> 2) ^ (row & 7)) << 4) | ((k & 3) << 2));
+    const float h = tf32_rn(v);
+    *(float*)(hi + off) = h;
+    *(float*)(lo + off) = tf32_rn(v - h);
+}
+
+// Adds this thread's NCOL accumulator columns (tensor-memory address taddr:
+// its warp's lane quadrant, its column group) to run, 16 columns per load
+// (fewer registers in flight than 32-column loads beside run).
+template <int NCOL> __device__ __forceinline__ void drain(uint32_t taddr, float (&run)[NCOL]) {
+    constexpr int N16 = NCOL / 16, N8 = (NCOL % 16) / 8;
+#pragma unroll
+    for (int q = 0; q < N16; ++q) {
+        uint32_t r[16];
+        tmem_ld16(taddr + 16 * q, r);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) run[16 * q + i] += __uint_as_float(r[i]);
+    }
+    if (N8) {
+        uint32_t r[8];
+        tmem_ld8(taddr + 16 * N16, r);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) run[16 * N16 + i] += __uint_as_float(r[i]);
+    }
+}
+
+template <int PD>
+__global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant__ SelfTcArgs A) {
+    using S = TcShape<PD>;
+    constexpr int NP = S::NP, ND = S::ND, L = PD + 1;
+    extern __shared__ __align__(1024) char smem_raw[];
+    // the swizzle pattern is a function of the address: align the stages to 1 KB
+    char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    float2* leg = (float2*)(smem + S::LEG_OFF);    // [32][LS]: (L, L') of x, y, z per slot
+    float4* coef = (float4*)(smem + S::COEF_OFF);  // [32][3]: slot coefficients and normal
+    uint64_t* bars = (uint64_t*)(smem + S::BAR_OFF);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2);
+    __shared__ int s_ok;
+    __shared__ float s_box[4];   // ih_x, ih_y, ih_z, sc of P's Legendre map
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int P = blockIdx.x;
+    const uint32_t sbase = smem_u32(smem);
+    // after one CTA's wait ran out the launch has failed: the others return
+    // at once instead of waiting out their own limits
+    if (*(volatile int*)A.status & ST_TIMEOUT) return;
+
+    // zero both operand stages: padding rows are never written again
+    for (int i = t; i < (int)(2 * S::STAGE / 16); i += ST_THREADS) ((float4*)smem)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const double* bb = A.bbox + (int64_t)P * 6;
+    if (t == 0) {
+        double hprod = 1.0;
+        for (int d = 0; d < 3; ++d) {
+            const double h = (bb[2 * d + 1] - bb[2 * d]) / 2.0;
+            s_box[d] = (float)(1.0 / h);
+            hprod *= h;
+        }
+        s_box[3] = (float)(1.0 / sqrt(hprod));
+        mbar_init(smem_u32(&bars[0]), 1);
+        mbar_init(smem_u32(&bars[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)S::TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the zeroed stages, for the MMAs
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    const int t0 = A.poly_ptr[P], ntet = A.poly_ptr[P + 1] - t0;
+    const int64_t kself = A.row_ptr[P];   // the self block leads its row
+    const int64_t f0 = A.bf_ptr[kself];
+    const int nface = (int)(A.bf_ptr[kself + 1] - f0);
+    const int nvc = ntet * S::CPT;
+    const int nch = nvc + (nface + S::FPC - 1) / S::FPC;
+    const float sc = s_box[3], sx = sc * s_box[0], sy = sc * s_box[1], sz = sc * s_box[2];
+    const int grp = warp >> 2;                                   // column group of the drain
+    const uint32_t tq = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(grp * S::NCOL);
+    const uint32_t idesc = idesc_tf32(128, S::NT);
+
+    float run[S::NCOL];
+#pragma unroll
+    for (int j = 0; j < S::NCOL; ++j) run[j] = 0.0f;
+    bool ok = true;
+    int issued = 0;
+    for (int c = 0; c < nch; ++c) {
+        const int st = c & 1, seg = c / ST_SEG;
+        // the MMAs of chunk c - 2 read this stage: thread 0 waits for them
+        if (c >= 2 && t == 0) s_ok = mbar_wait(smem_u32(&bars[st]), (uint32_t)(((c - 2) >> 1) & 1)) ? 1 : 0;
+        // ---- warp 0: slot `lane` of chunk c -> point, weights, Legendre values ----
+        if (warp == 0) {
+            const int k = lane;
+            double xg[3] = {0.0, 0.0, 0.0};
+            float bd = 0.f, bn = 0.f, dd = 0.f, dn = 0.f, sd = 0.f, sn = 0.f, nv[3] = {0.f, 0.f, 0.f};
+            bool valid = false;
+            if (c < nvc) {
+                const int q = (c % S::CPT) * ST_BK + k;
+                if (q < S::NQ3) {
+                    const int tt = A.poly_tets[t0 + c / S::CPT];
+                    const double* F = A.fk + (int64_t)tt * 12;
+                    const double* rp = A.ref->nodtet3 + q * 4;
+                    for (int d = 0; d < 3; ++d)
+                        xg[d] = F[d * 4 + 0] * rp[0] + F[d * 4 + 1] * rp[1] + F[d * 4 + 2] * rp[2] + F[d * 4 + 3] * rp[3];
+                    const double w = A.ref->weitet3[q] * fabs(A.jdet[tt]);
+                    const int mid = A.tet_mat[tt];
+                    bd = 1.f;
+                    dd = (float)(w * A.mat[mid * 3 + 1]);
+                    sd = (float)(w * A.mat[mid * 3 + 2]);
+                    valid = true;
+                }
+            } else {
+                const int fi = (c - nvc) * S::FPC + k / (2 * S::NF), r = k % (2 * S::NF);
+                if (k < S::FPC * 2 * S::NF && fi < nface) {
+                    const int code = A.bf[f0 + fi];
+                    const int tt = code >> 2, f = code & 3;
+                    const int E2 = A.neigh[code];
+                    const bool dir = (E2 == LYMPH_BC_DIRI);
+                    const double hmin = dir ? A.hk[P] : fmin(A.hk[P], A.hk[A.tet_poly[E2]]);
+                    const int mid = A.tet_mat[tt];
+                    const double lam = A.mat[mid * 3 + 1], mu = A.mat[mid * 3 + 2];
+                    const double sigma = A.alpha * (double)(PD * PD) / hmin * (lam + 2.0 * mu);
+                    const double cI = dir ? 1.0 : 0.5;
+                    const int q = r % S::NF;
+                    const double xi = A.frule[3 * q], eta = A.frule[3 * q + 1];
+                    const double W = A.frule[3 * q + 2] * A.area[(int64_t)tt * 4 + f];
+                    // the face map of basis_boundary (basis_function.f90:560-577): x = Fk node_maps(:,:,f) (xi, eta, 1, 1)
+                    const double* F = A.fk + (int64_t)tt * 12;
+                    const double* nm = A.ref->node_maps + f * 16;
+                    for (int d = 0; d < 3; ++d) {
+                        double cm[4];
+                        for (int l = 0; l < 4; ++l) {
+                            double s = 0.0;
+                            for (int m = 0; m < 4; ++m) s += F[d * 4 + m] * nm[m * 4 + l];
+                            cm[l] = s;
+                        }
+                        xg[d] = cm[2] + cm[3] + xi * cm[0] + eta * cm[1];
+                        nv[d] = (float)A.nrm[(int64_t)tt * 12 + f * 3 + d];
+                    }
+                    if (r < S::NF) {   // "d" slot
+                        bd = 1.f;
+                        dn = (float)(A.theta * cI * W * lam);
+                        sn = (float)(A.theta * cI * W * mu);
+                    } else {           // "n phi" slot
+                        bn = 1.f;
+                        dd = (float)(-cI * W * lam);
+                        sd = (float)(-cI * W * mu);
+                        sn = (float)(0.5 * sigma * W);
+                    }
+                    valid = true;
+                }
+            }
+            float2* lg = leg + k * S::LS;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double cen = (bb[2 * d] + bb[2 * d + 1]) / 2.0, h = (bb[2 * d + 1] - bb[2 * d]) / 2.0;
+                legendre_f32<PD>(valid ? (float)((xg[d] - cen) / h) : 0.0f, lg + d * L);
+            }
+            coef[k * 3 + 0] = make_float4(bd, bn, dd, dn);
+            coef[k * 3 + 1] = make_float4(sd, sn, nv[0], nv[1]);
+            coef[k * 3 + 2] = make_float4(nv[2], 0.f, 0.f, 0.f);
+        }
+        __syncthreads();
+        if (c >= 2 && !s_ok) {
+            ok = false;
+            break;
+        }
+        // a chunk that starts segment seg >= 2 reuses the accumulator of
+        // segment seg - 2, whose MMAs (chunks up to c - 2) are complete
+        if (c % ST_SEG == 0 && seg >= 2) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            drain<S::NCOL>(tq + (uint32_t)((seg & 1) * S::NT), run);
+        }
+        // ---- all warps: the operands of chunk c, basis function a = warp + 16 i, slot = lane ----
+        {
+            char* ahi = smem + st * S::STAGE;
+            char* alo = ahi + S::A_TILE;
+            char* bhi = alo + S::A_TILE;
+            char* blo = bhi + S::B_TILE;
+            const int k = lane;
+            const float4 c0 = coef[k * 3 + 0], c1 = coef[k * 3 + 1];
+            const float n3[3] = {c1.z, c1.w, coef[k * 3 + 2].x};
+            const float2* lg = leg + k * S::LS;
+            for (int a = warp; a < NP; a += ST_THREADS / 32) {
+                const int3 tr = blist_row<PD>(a);
+                const float2 X = lg[tr.x], Y = lg[L + tr.y], Z = lg[2 * L + tr.z];
+                const float yz = Y.x * Z.x;
+                const float phi = sc * X.x * yz;
+                const float g[3] = {sx * X.y * yz, sy * X.x * Y.y * Z.x, sz * X.x * Y.x * Z.y};
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float np_ = n3[i] * phi;
+                    const int row = i * NP + a;
+                    put_split(ahi, alo, row, k, fmaf(c0.x, g[i], c0.y * np_));
+                    put_split(bhi, blo, row, k, fmaf(c0.z, g[i], c0.w * np_));
+                    put_split(bhi, blo, S::NH + row, k, fmaf(c1.x, g[i], c1.y * np_));
+                }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic-proxy writes -> the MMAs
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (t == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ahi = sbase + (uint32_t)(st * S::STAGE), alo = ahi + (uint32_t)S::A_TILE;
+            const uint32_t bhi = alo + (uint32_t)S::A_TILE, blo = bhi + (uint32_t)S::B_TILE;
+            const uint32_t d = tmem + (uint32_t)((seg & 1) * S::NT);
+#pragma unroll
+            for (int j = 0; j < ST_BK / 8; ++j) {   // k-step j: bytes 32 j .. 32 j + 31 of every row
+                const uint64_t dah = sdesc_sw128(ahi + 32 * j), dal = sdesc_sw128(alo + 32 * j);
+                const uint64_t dbh = sdesc_sw128(bhi + 32 * j), dbl = sdesc_sw128(blo + 32 * j);
+                mma_tf32(d, dah, dbh, idesc, (c % ST_SEG == 0 && j == 0) ? 0u : 1u);
+                mma_tf32(d, dah, dbl, idesc, 1u);
+                mma_tf32(d, dal, dbh, idesc, 1u);
+                mma_tf32(d, dal, dbl, idesc, 1u);
+            }
+            mma_commit(smem_u32(&bars[st]));
+        }
+        issued = c + 1;
+    }
+    // the last commit covers every MMA issued before it
+    if (t == 0) {
+        bool done = true;
+        if (issued > 0) done = mbar_wait(smem_u32(&bars[(issued - 1) & 1]), (uint32_t)(((issued - 1) >> 1) & 1));
+        if (!done || !ok) atomicOr(A.status, ST_TIMEOUT);
+        s_ok = (done && ok) ? 1 : 0;
+    }
+    __syncthreads();
+    ok = s_ok != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int nseg = (nch + ST_SEG - 1) / ST_SEG;   // segments 0 .. nseg - 3 are drained
+        if (nseg >= 2) drain<S::NCOL>(tq + (uint32_t)(((nseg - 2) & 1) * S::NT), run);
+        drain<S::NCOL>(tq + (uint32_t)(((nseg - 1) & 1) * S::NT), run);
+        // ---- epilogue: O_D column-major and O_S row-major in the free stages ----
+        float* Dm = (float*)smem;
+        float* Sm = Dm + ND * ND;
+        const int row = (warp & 3) * 32 + lane;
+        if (row < ND) {
+#pragma unroll
+            for (int j = 0; j < S::NCOL; ++j) {
+                const int col = grp * S::NCOL + j;
+                if (col < ND) Dm[col * ND + row] = run[j];
+                else if (col >= S::NH && col < S::NH + ND) Sm[row * ND + (col - S::NH)] = run[j];
+            }
+        }
+        __syncthreads();
+        float* out = A.out + (int64_t)P * ND * ND;
+        for (int e = t; e < ND * ND; e += ST_THREADS) {
+            const int col = e / ND, r = e - col * ND;
+            const int i = r / NP, a = r - i * NP, j = col / NP, b = col - j * NP;
+            float v = Dm[e] + Sm[(j * NP + a) * ND + i * NP + b];
+            if (i == j) v += (Sm[a * ND + b] + Sm[(NP + a) * ND + NP + b]) + Sm[(2 * NP + a) * ND + 2 * NP + b];
+            out[e] = v;
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)S::TCOLS));
+}
+
+template <int PD> int launch_self_tc(lymph_ctx* c, float* out) {
+    using S = TcShape<PD>;
+    SelfTcArgs A;
+    A.poly_ptr = c->d_poly_ptr; A.poly_tets = c->d_poly_tets; A.tet_poly = c->d_tet_poly; A.tet_mat = c->d_tet_mat;
+    A.neigh = c->d_neigh; A.mat = c->d_mat; A.fk = c->d_fk; A.jdet = c->d_jdet; A.nrm = c->d_normal; A.area = c->d_area;
+    A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.row_ptr = c->d_row_ptr; A.bf_ptr = c->d_bf_ptr;
+    A.bf = c->d_bf; A.alpha = c->alpha; A.theta = c->theta; A.out = out; A.status = c->d_status;
+    int32_t nq = 0;
+    if (lymph_mf_face_rule(PD, &nq, nullptr) != LYMPH_OK || nq != S::NF) {
+        lymph_set_error("self-block assembly: no triangle rule for this degree");
+        return LYMPH_ERR_INVALID;
+    }
+    lymph_mf_face_rule(PD, &nq, A.frule);
+    LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_self_tc<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM));
+    if (c->n_poly > 0) {
+        k_self_tc<PD><<<c->n_poly, ST_THREADS, S::SMEM, c->stream>>>(A);
+        c->launches++;
+        LYMPH_CUDA_TRY(cudaGetLastError());
+    }
+    return LYMPH_OK;
+}
+
+}  // namespace
+
+// The FP32 self block of every polyhedron into out[n_poly][nd * nd]
+// (column-major blocks), on the tensor cores.
+int lymph_dev_self_tc(lymph_ctx* c, float* out) {
+    switch (c->p) {
+        case 1: return launch_self_tc<1>(c, out);
+        case 2: return launch_self_tc<2>(c, out);
+        case 3: return launch_self_tc<3>(c, out);
+        case 4: return launch_self_tc<4>(c, out);
+        default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
+    }
+}

@@ -21,6 +21,9 @@
 namespace {
 
 constexpr int ASM_THREADS = 256;
+// AsmArgs::which for the mass matrices alone (the self blocks of the
+// mixed operators come from the tensor-core assembly in selftc.cu)
+constexpr int ASM_MASS_ONLY = 2;
 
 template <int P> struct Deg {
     static constexpr int NP = (P + 1) * (P + 2) * (P + 3) / 6;
@@ -172,7 +175,9 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
     const bool self = (Qc == P);
     const double pdeg2 = (double)(PD * PD);
 
-    for (int i = tid; i < ND * ND; i += ASM_THREADS) acc[i] = 0.0;
+    const bool mass_only = (A.which == ASM_MASS_ONLY);
+    if (!mass_only)
+        for (int i = tid; i < ND * ND; i += ASM_THREADS) acc[i] = 0.0;
 
     if (self) {
         // ---- volume terms and mass matrices over the sub-tetrahedra ----
@@ -218,6 +223,11 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
                     const int pr = tid + u * ASM_THREADS;
                     if (pr < D::NPAIR) {
                         const int m = pr / NP, n = pr % NP;
+                        if (mass_only) {
+                            for (int qq = 0; qq < nq; ++qq)
+                                Mt[u] += (tw[qq] * tphi[qq * NP + m]) * tphi[qq * NP + n];
+                            continue;
+                        }
                         for (int qq = 0; qq < nq; ++qq) {
                             const double w = tw[qq];
                             const double a0 = w * tdphi[(qq * 3 + 0) * NP + m];
@@ -241,14 +251,16 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
                 if (pr < D::NPAIR) {
                     const int m = pr / NP, n = pr % NP;
                     const double tr = G[u][0] + G[u][4] + G[u][8];
+                    if (!mass_only) {
 #pragma unroll
-                    for (int i = 0; i < 3; ++i)
+                        for (int i = 0; i < 3; ++i)
 #pragma unroll
-                        for (int j = 0; j < 3; ++j) {
-                            double v = lam * G[u][i * 3 + j] + mu * G[u][j * 3 + i];
-                            if (i == j) v += mu * tr;
-                            acc[(i * NP + m) * ND + j * NP + n] += v;
-                        }
+                            for (int j = 0; j < 3; ++j) {
+                                double v = lam * G[u][i * 3 + j] + mu * G[u][j * 3 + i];
+                                if (i == j) v += mu * tr;
+                                acc[(i * NP + m) * ND + j * NP + n] += v;
+                            }
+                    }
                     msum[u] += Mt[u];
                     mrho[u] += Mt[u] * rho;
                 }
@@ -265,6 +277,8 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
             }
         }
     }
+
+    if (mass_only) return;
 
     // ---- face terms ----
     {
@@ -874,6 +888,14 @@ int lymph_dev_assemble_list(lymph_ctx* c, int which, void* out, int out_fp32, bo
         case 4: return launch_assemble<4>(c, which, out, out_fp32, write_mass, list, n_list, out_stride);
         default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
     }
+}
+
+// The rho-weighted and the plain mass matrix of every polyhedron (the
+// self-block CTAs of k_assemble with the stiffness and face terms skipped:
+// the same sums in the same order, so M and Mm have the bits a full assembly
+// gives them).
+int lymph_dev_mass(lymph_ctx* c, const int64_t* self_list) {
+    return lymph_dev_assemble_list(c, ASM_MASS_ONLY, nullptr, 0, true, self_list, c->n_poly, 0);
 }
 
 int lymph_dev_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {

@@ -173,6 +173,12 @@ class MatrixFree:
         check(self.lib.lymph_get_blocks(self.ctx, which, ptr(out, c_double)), "get_blocks")
         return out
 
+    def self_blocks(self) -> np.ndarray:
+        """The self blocks the step applies, [n_poly][3Np][3Np] row-major."""
+        out = np.empty((self.n_poly, self.nd, self.nd), np.float64)
+        check(self.lib.lymph_get_self_blocks(self.ctx, ptr(out, c_double)), "get_self_blocks")
+        return out
+
     def mass(self, which: int) -> np.ndarray:
         out = np.empty((self.n_poly, self.Np, self.Np), np.float64)
         check(self.lib.lymph_get_mass(self.ctx, which, ptr(out, c_double)), "get_mass")

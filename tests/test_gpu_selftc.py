@@ -1,0 +1,69 @@
+"""The tensor-core self blocks of LYMPH_MIXED_MF (csrc/selftc.cu) against the
+FP64 assembly.
+
+The matrix-free mixed path stores only each polyhedron's self block, in FP32,
+assembled by k_self_tc<p> on the tcgen05 tensor cores: kind::tf32 MMAs of
+operands split into their nearest TF32 value and the TF32-rounded remainder
+(four products, FP32-accurate), FP32 accumulation in tensor memory drained
+to registers after every 32 quadrature slots (the tensor cores' accumulation
+truncates).  Bars (written in each assertion):
+  * the self block of every polyhedron against the FP64 path's self block
+    (k_assemble, the reference's sums in FP64) with random coefficients:
+    max_P ||(K_tc - K_64) u_P|| / ||K_64 u_P|| <= TOL_SELF (1e-6); the
+    FP32 rounding of the FP64 block alone, printed beside it, is ~5e-8, and
+    the algebra of the decomposition is checked in FP64 on the CPU
+    (tests/test_selfblock_formula.py, 1e-12);
+  * the mass matrices of the matrix-free context (the k_assemble CTAs with
+    the stiffness skipped) equal the FP64 context's bit for bit;
+  * the operator apply of the whole path stays within TOL_APPLY_FP32 of the
+    oracle (tests/test_gpu_mf.py, every mesh kind and degree).
+"""
+import numpy as np
+import pytest
+
+from lymph3d_apsc_gb300 import MatrixFree, _lib
+from test_gpu_parity import KINDS, _mesh
+
+pytestmark = pytest.mark.gpu
+
+TOL_SELF = 1e-6
+
+
+def _self_and_mass(m, p, precision, theta=-1.0):
+    with MatrixFree(m, p, 1e-3, precision=precision, theta=theta) as g:
+        g.MAKE_MATRICES_FREE()
+        return g.self_blocks(), g.mass(0), g.mass(1)
+
+
+def _apply_rel(Ka, Kb, seed):
+    u = np.random.default_rng(seed).standard_normal((Ka.shape[0], Ka.shape[1]))
+    ya = np.einsum("prc,pc->pr", Ka, u)
+    yb = np.einsum("prc,pc->pr", Kb, u)
+    return float(np.max(np.linalg.norm(ya - yb, axis=1) / np.linalg.norm(yb, axis=1)))
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_tensor_core_self_blocks_match_fp64_assembly(require_gpu, kind, p):
+    m = _mesh(kind)
+    K64, M64, Mm64 = _self_and_mass(m, p, _lib.FP64)
+    Ktc, Mtc, Mmtc = _self_and_mass(m, p, _lib.MIXED_MF)
+    e = _apply_rel(Ktc, K64, 7 + p)
+    e_round = _apply_rel(K64.astype(np.float32).astype(np.float64), K64, 7 + p)
+    print(f"{kind} p={p}: tensor-core self blocks {e:.2e} (FP32 rounding of the FP64 blocks {e_round:.2e})")
+    assert e <= TOL_SELF, e
+    assert np.array_equal(Mtc, M64) and np.array_equal(Mmtc, Mm64)
+
+
+@pytest.mark.parametrize("theta", [0.0, 1.0])
+def test_tensor_core_self_blocks_other_theta(require_gpu, theta):
+    """theta = 0 (IIPG) and 1 (NIPG): the symmetry terms enter O_D and O_S
+    with other weights, and the blocks are no longer symmetric."""
+    m = _mesh("bfs_lognormal")
+    K64, _, _ = _self_and_mass(m, 3, _lib.FP64, theta)
+    Ktc, _, _ = _self_and_mass(m, 3, _lib.MIXED_MF, theta)
+    e = _apply_rel(Ktc, K64, 3)
+    print(f"theta={theta}: {e:.2e}")
+    assert e <= TOL_SELF, e
+    if theta != -1.0:
+        assert not np.allclose(K64, np.transpose(K64, (0, 2, 1)), rtol=1e-3)
