@@ -71,9 +71,13 @@ extern "C" {
 /* ---- precision of the operator apply ----------------------------------- */
 #define LYMPH_FP64   0   /* every operation in FP64 (the plain path) */
 #define LYMPH_MIXED  1   /* operator blocks and their mat-vec in FP32, FP32
-                            accumulation; geometry, assembly, mass inverse,
-                            time update and error norms in FP64 */
-#define LYMPH_MIXED_MF 2  /* FP32 self blocks; the neighbour terms evaluated
+                            accumulation; self blocks assembled on the tensor
+                            cores (kind::tf32, FP32-accurate split products),
+                            neighbour blocks by the FP64 assembly rounded;
+                            geometry, mass matrices, mass inverse, time update
+                            and error norms in FP64 */
+#define LYMPH_MIXED_MF 2  /* FP32 self blocks (assembled on the tensor cores,
+                            as for LYMPH_MIXED); the neighbour terms evaluated
                             matrix-free in FP32 at every step from the face
                             quadrature (Q's field and gradient at P's
                             quadrature points, tested against P's basis), so no
@@ -176,7 +180,8 @@ int lymph_sizes(const lymph_ctx* ctx, int32_t* Np, int32_t* n_poly, int64_t* n_b
 
 /* MAKE_MATRICES_FREE (src/matrix_free.f90:27-464) followed by the Cholesky
  * factorisation of the mass matrices (src/Lymph3D.f90:264-271): assembles
- * K_loc, M_loc, M_modal_loc and their factors on the device. */
+ * K_loc, M_loc, M_modal_loc and their factors on the device (the FP32 self
+ * blocks of the mixed precisions on the tensor cores). */
 int lymph_make_matrices(lymph_ctx* ctx);
 
 /* MAKE_RHS_FREE (src/matrix_free.f90:467-843): which = LYMPH_RHS_STAT or
@@ -402,8 +407,8 @@ int lymph_compute_error_dg_free(lymph_ctx* ctx, int slot_uh, int slot_uex, doubl
 int lymph_get_pattern(lymph_ctx* ctx, int32_t* row_ptr, int32_t* col);
 int lymph_get_blocks(lymph_ctx* ctx, int which, double* vals);
 /* The self blocks the step kernels apply, vals[n_poly][3Np][3Np] row-major:
- * the FP64 blocks, or the stored FP32 values widened (LYMPH_MIXED_MF: the
- * tensor-core assembly of MAKE_STIFFNESS_VOLUME + MAKE_STIFFNESS_FACE's
+ * the FP64 blocks, or the stored FP32 values widened (the mixed precisions:
+ * the tensor-core assembly of MAKE_STIFFNESS_VOLUME + MAKE_STIFFNESS_FACE's
  * self terms, src/assemble_element.f90:24-77, 404-661).  A read-back for
  * parity checks; no counterpart in the reference. */
 int lymph_get_self_blocks(lymph_ctx* ctx, double* vals);

@@ -27,7 +27,8 @@ int lymph_mf_setup(lymph_ctx* c, const RefTables& R);
 int lymph_dev_cholesky(lymph_ctx* c);
 int lymph_dev_damping(lymph_ctx* c, bool assemble);
 int lymph_dev_mass(lymph_ctx* c, const int64_t* self_list);
-int lymph_dev_self_tc(lymph_ctx* c, float* out);
+int lymph_dev_self_tc(lymph_ctx* c, float* out, bool block_csr);
+int lymph_dev_assemble_at(lymph_ctx* c, int which, void* out, int out_fp32, const int64_t* list, int64_t n_list);
 int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scale, double* out);
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
@@ -499,13 +500,36 @@ static int make_mf_matrices(lymph_ctx* c) {
     int rc = cudaMemcpy(d_list, self.data(), sizeof(int64_t) * (size_t)np, cudaMemcpyHostToDevice) == cudaSuccess
                  ? LYMPH_OK : LYMPH_ERR_CUDA;
     if (rc == LYMPH_OK) rc = lymph_dev_mass(c, d_list);
-    if (rc == LYMPH_OK) rc = lymph_dev_self_tc(c, (float*)c->d_K);
+    if (rc == LYMPH_OK) rc = lymph_dev_self_tc(c, (float*)c->d_K, false);
     if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
     cudaFree(d_list);
     LYMPH_TRY(rc);
     RefTables R;
     if (!build_ref_tables(c->p, R)) { lymph_set_error("lymph_make_matrices: no quadrature for this degree"); return LYMPH_ERR_INVALID; }
     return lymph_mf_setup(c, R);
+}
+
+// FP32 blocks (LYMPH_MIXED): the self blocks on the tensor cores, the
+// neighbour blocks (face terms only) by the FP64 assembly rounded to FP32,
+// the mass matrices in FP64.
+static int make_mixed_blocks(lymph_ctx* c) {
+    const int np = c->n_poly;
+    std::vector<int64_t> lists;
+    lists.reserve((size_t)c->n_blocks);
+    for (int P = 0; P < np; ++P) lists.push_back(c->h_row_ptr[P]);
+    for (int P = 0; P < np; ++P)
+        for (int64_t k = (int64_t)c->h_row_ptr[P] + 1; k < c->h_row_ptr[P + 1]; ++k) lists.push_back(k);
+    const int64_t n_nb = (int64_t)lists.size() - np;
+    int64_t* d_lists = nullptr;
+    LYMPH_CUDA_TRY(cudaMalloc(&d_lists, sizeof(int64_t) * lists.size()));
+    int rc = cudaMemcpy(d_lists, lists.data(), sizeof(int64_t) * lists.size(), cudaMemcpyHostToDevice) == cudaSuccess
+                 ? LYMPH_OK : LYMPH_ERR_CUDA;
+    if (rc == LYMPH_OK) rc = lymph_dev_mass(c, d_lists);
+    if (rc == LYMPH_OK && n_nb > 0) rc = lymph_dev_assemble_at(c, LYMPH_BLOCKS_K, c->d_K, 1, d_lists + np, n_nb);
+    if (rc == LYMPH_OK) rc = lymph_dev_self_tc(c, (float*)c->d_K, true);
+    if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
+    cudaFree(d_lists);
+    return rc;
 }
 
 int lymph_make_matrices(lymph_ctx* c) {
@@ -552,7 +576,8 @@ int lymph_make_matrices(lymph_ctx* c) {
     }
     c->k32_valid = false;  // an FP32 copy made from earlier blocks is stale
     c->rhs_version++;      // and so is any cached M^-1 F
-    LYMPH_TRY(lymph_dev_assemble(c, LYMPH_BLOCKS_K, c->d_K, c->precision == LYMPH_MIXED, true));
+    if (c->precision == LYMPH_MIXED) LYMPH_TRY(make_mixed_blocks(c));
+    else LYMPH_TRY(lymph_dev_assemble(c, LYMPH_BLOCKS_K, c->d_K, 0, true));
     LYMPH_TRY(lymph_dev_cholesky(c));
     LYMPH_TRY(lymph_dev_damping(c, true));
     LYMPH_TRY(lymph_sync_status(c, "lymph_make_matrices"));

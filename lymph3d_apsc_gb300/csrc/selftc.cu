@@ -1,5 +1,6 @@
-// selftc.cu -- the FP32 self blocks of the mixed operator (LYMPH_MIXED_MF)
-// assembled on the 5th-generation tensor cores (tcgen05, kind::tf32).
+// selftc.cu -- the FP32 self blocks of the mixed operators (LYMPH_MIXED_MF,
+// LYMPH_MIXED) assembled on the 5th-generation tensor cores (tcgen05,
+// kind::tf32).
 //
 // The self block K_PP of MAKE_MATRICES_FREE (src/matrix_free.f90:27-464) is
 // the volume stiffness of P's sub-tetrahedra (MAKE_STIFFNESS_VOLUME,
@@ -125,7 +126,8 @@ struct SelfTcArgs {
     const int64_t* bf_ptr;
     const int32_t* bf;
     double alpha, theta;
-    float* out;            // [n_poly][ND * ND], column-major blocks
+    float* out;            // column-major ND x ND blocks: P's at slot P, or at slot row_ptr[P]
+    int slot_row_ptr;      // 1: the block-CSR operator of LYMPH_MIXED (self block first in each row)
     int* status;
     double frule[3 * 16];  // (xi, eta, w) of the symmetric triangle rule
 };
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
             }
         }
         __syncthreads();
-        float* out = A.out + (int64_t)P * ND * ND;
+        float* out = A.out + (A.slot_row_ptr ? kself : (int64_t)P) * ND * ND;
         for (int e = t; e < ND * ND; e += ST_THREADS) {
             const int col = e / ND, r = e - col * ND;
             const int i = r / NP, a = r - i * NP, j = col / NP, b = col - j * NP;
@@ -402,13 +404,13 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)S::TCOLS));
 }
 
-template <int PD> int launch_self_tc(lymph_ctx* c, float* out) {
+template <int PD> int launch_self_tc(lymph_ctx* c, float* out, bool block_csr) {
     using S = TcShape<PD>;
     SelfTcArgs A;
     A.poly_ptr = c->d_poly_ptr; A.poly_tets = c->d_poly_tets; A.tet_poly = c->d_tet_poly; A.tet_mat = c->d_tet_mat;
     A.neigh = c->d_neigh; A.mat = c->d_mat; A.fk = c->d_fk; A.jdet = c->d_jdet; A.nrm = c->d_normal; A.area = c->d_area;
     A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.row_ptr = c->d_row_ptr; A.bf_ptr = c->d_bf_ptr;
-    A.bf = c->d_bf; A.alpha = c->alpha; A.theta = c->theta; A.out = out; A.status = c->d_status;
+    A.bf = c->d_bf; A.alpha = c->alpha; A.theta = c->theta; A.out = out; A.slot_row_ptr = block_csr ? 1 : 0; A.status = c->d_status;
     int32_t nq = 0;
     if (lymph_mf_face_rule(PD, &nq, nullptr) != LYMPH_OK || nq != S::NF) {
         lymph_set_error("self-block assembly: no triangle rule for this degree");
@@ -426,14 +428,15 @@ template <int PD> int launch_self_tc(lymph_ctx* c, float* out) {
 
 }  // namespace
 
-// The FP32 self block of every polyhedron into out[n_poly][nd * nd]
-// (column-major blocks), on the tensor cores.
-int lymph_dev_self_tc(lymph_ctx* c, float* out) {
+// The FP32 self block of every polyhedron on the tensor cores, column-major,
+// into out[n_poly][nd * nd] or (block_csr) into the self-block slots
+// row_ptr[P] of a block-CSR operator.
+int lymph_dev_self_tc(lymph_ctx* c, float* out, bool block_csr) {
     switch (c->p) {
-        case 1: return launch_self_tc<1>(c, out);
-        case 2: return launch_self_tc<2>(c, out);
-        case 3: return launch_self_tc<3>(c, out);
-        case 4: return launch_self_tc<4>(c, out);
+        case 1: return launch_self_tc<1>(c, out, block_csr);
+        case 2: return launch_self_tc<2>(c, out, block_csr);
+        case 3: return launch_self_tc<3>(c, out, block_csr);
+        case 4: return launch_self_tc<4>(c, out, block_csr);
         default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
     }
 }

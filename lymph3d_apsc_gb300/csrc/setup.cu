@@ -152,6 +152,7 @@ struct AsmArgs {
     void* out;        // [n][out_stride] blocks, each [ND][ND] column-major
     const int64_t* list;  // blocks to assemble (null: all, in order); output slot = position in the list
     int64_t out_stride;   // elements from one output block to the next (>= ND*ND)
+    int out_at_block;     // block list[i] goes to output slot list[i] (else slot i)
     double* M;        // [n_poly][NP][NP] rho-weighted mass (self blocks only; may be null)
     double* Mm;       // unweighted (modal) mass
     int64_t block0;   // first block of this launch
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
         double* tphi = tab;                 // [QC][NP]
         double* tdphi = tphi + QC * NP;     // [QC][3][NP]
         double* tw = tdphi + QC * 3 * NP;   // [QC]
+        double* ttl = tw + QC;              // [QC][3][p+1] (value, derivative) pairs
         double msum[PPT], mrho[PPT];
 #pragma unroll
         for (int u = 0; u < PPT; ++u) { msum[u] = 0.0; mrho[u] = 0.0; }
@@ -203,17 +205,74 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
             }
             for (int q0 = 0; q0 < NQ3; q0 += QC) {
                 __syncthreads();
-                for (int it = tid; it < QC * NP; it += ASM_THREADS) {
-                    int qq = it / NP, f = it % NP, q = q0 + qq;
+                if (mass_only) {
+                    // phi alone, from one table of the 1-D factors per point
+                    // (3 (p+1) legendre_1d calls instead of 3 Np), multiplied
+                    // in basis_eval's order, and w phi_m once per (q, m): the
+                    // same values and sums as the full assembly, bit for bit
+                    constexpr int L1 = PD + 1;
+                    double* tleg = tdphi;               // [QC][3][L1]
+                    double* twphi = tdphi + QC * 3 * L1; // [QC][NP]
+                    for (int it = tid; it < QC * 3 * L1; it += ASM_THREADS) {
+                        const int qq = it / (3 * L1), r = it % (3 * L1), d = r / L1, deg = r % L1, q = q0 + qq;
+                        if (q < NQ3) {
+                            double pt[3], v, dv;
+                            tet_point(fk, A.ref, q, pt);
+                            legendre_1d(pt[d], deg, bb[2 * d], bb[2 * d + 1], &v, &dv);
+                            tleg[it] = v;
+                            if (r == 0) tw[qq] = A.ref->weitet3[q] * aj;
+                        }
+                    }
+                    __syncthreads();
+                    for (int it = tid; it < QC * NP; it += ASM_THREADS) {
+                        const int qq = it / NP, f = it % NP, q = q0 + qq;
+                        if (q < NQ3) {
+                            const int* bl = &A.ref->blist[f * 3];
+                            const double* tq = tleg + qq * 3 * L1;
+                            const double ph = tq[bl[0]] * tq[L1 + bl[1]] * tq[2 * L1 + bl[2]];
+                            tphi[qq * NP + f] = ph;
+                            twphi[qq * NP + f] = tw[qq] * ph;
+                        }
+                    }
+                    __syncthreads();
+                    const int nq = (NQ3 - q0) < QC ? (NQ3 - q0) : QC;
+#pragma unroll
+                    for (int u = 0; u < PPT; ++u) {
+                        const int pr = tid + u * ASM_THREADS;
+                        if (pr < D::NPAIR) {
+                            const int m = pr / NP, n = pr % NP;
+                            for (int qq = 0; qq < nq; ++qq) Mt[u] += twphi[qq * NP + m] * tphi[qq * NP + n];
+                        }
+                    }
+                    continue;
+                }
+                // basis_eval's 1-D factors (value, derivative) per point,
+                // coordinate and degree, then their products in its order:
+                // the same bits at 3 (p+1) legendre_1d calls per point
+                // instead of 3 Np
+                constexpr int L1 = PD + 1;
+                for (int it = tid; it < QC * 3 * L1; it += ASM_THREADS) {
+                    const int qq = it / (3 * L1), r = it % (3 * L1), d = r / L1, deg = r % L1, q = q0 + qq;
                     if (q < NQ3) {
-                        double pt[3], ph, dp[3];
+                        double pt[3];
                         tet_point(fk, A.ref, q, pt);
-                        basis_eval(pt, bb, &A.ref->blist[f * 3], &ph, dp);
-                        tphi[qq * NP + f] = ph;
-                        tdphi[(qq * 3 + 0) * NP + f] = dp[0];
-                        tdphi[(qq * 3 + 1) * NP + f] = dp[1];
-                        tdphi[(qq * 3 + 2) * NP + f] = dp[2];
-                        if (f == 0) tw[qq] = A.ref->weitet3[q] * aj;
+                        legendre_1d(pt[d], deg, bb[2 * d], bb[2 * d + 1], &ttl[2 * it], &ttl[2 * it + 1]);
+                        if (r == 0) tw[qq] = A.ref->weitet3[q] * aj;
+                    }
+                }
+                __syncthreads();
+                for (int it = tid; it < QC * NP; it += ASM_THREADS) {
+                    const int qq = it / NP, f = it % NP, q = q0 + qq;
+                    if (q < NQ3) {
+                        const int* bl = &A.ref->blist[f * 3];
+                        const double* tq = ttl + 2 * qq * 3 * L1;
+                        const double vx = tq[2 * bl[0]], dx = tq[2 * bl[0] + 1];
+                        const double vy = tq[2 * (L1 + bl[1])], dy = tq[2 * (L1 + bl[1]) + 1];
+                        const double vz = tq[2 * (2 * L1 + bl[2])], dz = tq[2 * (2 * L1 + bl[2]) + 1];
+                        tphi[qq * NP + f] = vx * vy * vz;
+                        tdphi[(qq * 3 + 0) * NP + f] = dx * vy * vz;
+                        tdphi[(qq * 3 + 1) * NP + f] = vx * dy * vz;
+                        tdphi[(qq * 3 + 2) * NP + f] = vx * vy * dz;
                     }
                 }
                 __syncthreads();
@@ -223,11 +282,6 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
                     const int pr = tid + u * ASM_THREADS;
                     if (pr < D::NPAIR) {
                         const int m = pr / NP, n = pr % NP;
-                        if (mass_only) {
-                            for (int qq = 0; qq < nq; ++qq)
-                                Mt[u] += (tw[qq] * tphi[qq * NP + m]) * tphi[qq * NP + n];
-                            continue;
-                        }
                         for (int qq = 0; qq < nq; ++qq) {
                             const double w = tw[qq];
                             const double a0 = w * tdphi[(qq * 3 + 0) * NP + m];
@@ -285,6 +339,7 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
         double* fpt = tab;                        // [NQ2][3]
         double* fphi = fpt + NQ2 * 3;             // [2][NQ2][NP]
         double* fdphi = fphi + 2 * NQ2 * NP;      // [2][NQ2][3][NP]
+        double* ftl = fdphi + 2 * NQ2 * 3 * NP;   // [2][NQ2][3][p+1] (value, derivative) pairs
         const double* bbp = &A.bbox[P * 6];
         for (int64_t e = A.bf_ptr[k]; e < A.bf_ptr[k + 1]; ++e) {
             const int code = A.bf[e];
@@ -305,15 +360,25 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
             __syncthreads();
             for (int q = tid; q < NQ2; q += ASM_THREADS) face_point(fk, A.ref, f, q, &fpt[q * 3]);
             __syncthreads();
+            constexpr int L1 = PD + 1;
+            for (int it = tid; it < nside * NQ2 * 3 * L1; it += ASM_THREADS) {
+                const int s = it / (NQ2 * 3 * L1), rem = it % (NQ2 * 3 * L1), q = rem / (3 * L1);
+                const int d = (rem % (3 * L1)) / L1, deg = rem % L1;
+                const double* bb = (s == 0) ? bbp : &A.bbox[Qn * 6];
+                legendre_1d(fpt[q * 3 + d], deg, bb[2 * d], bb[2 * d + 1], &ftl[2 * it], &ftl[2 * it + 1]);
+            }
+            __syncthreads();
             for (int it = tid; it < nside * NQ2 * NP; it += ASM_THREADS) {
                 const int s = it / (NQ2 * NP), rem = it % (NQ2 * NP), q = rem / NP, fb = rem % NP;
-                const double* bb = (s == 0) ? bbp : &A.bbox[Qn * 6];
-                double ph, dp[3];
-                basis_eval(&fpt[q * 3], bb, &A.ref->blist[fb * 3], &ph, dp);
-                fphi[(s * NQ2 + q) * NP + fb] = ph;
-                fdphi[((s * NQ2 + q) * 3 + 0) * NP + fb] = dp[0];
-                fdphi[((s * NQ2 + q) * 3 + 1) * NP + fb] = dp[1];
-                fdphi[((s * NQ2 + q) * 3 + 2) * NP + fb] = dp[2];
+                const int* bl = &A.ref->blist[fb * 3];
+                const double* tq = ftl + 2 * (s * NQ2 + q) * 3 * L1;
+                const double vx = tq[2 * bl[0]], dx = tq[2 * bl[0] + 1];
+                const double vy = tq[2 * (L1 + bl[1])], dy = tq[2 * (L1 + bl[1]) + 1];
+                const double vz = tq[2 * (2 * L1 + bl[2])], dz = tq[2 * (2 * L1 + bl[2]) + 1];
+                fphi[(s * NQ2 + q) * NP + fb] = vx * vy * vz;
+                fdphi[((s * NQ2 + q) * 3 + 0) * NP + fb] = dx * vy * vz;
+                fdphi[((s * NQ2 + q) * 3 + 1) * NP + fb] = vx * dy * vz;
+                fdphi[((s * NQ2 + q) * 3 + 2) * NP + fb] = vx * vy * dz;
             }
             __syncthreads();
             const double nv[3] = {n0, n1, n2};
@@ -379,7 +444,7 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
     }
     __syncthreads();
     // write the block column-major (entry (r,c) at c*ND + r)
-    const int64_t base = slot * A.out_stride;
+    const int64_t base = (A.out_at_block ? k : slot) * A.out_stride;
     if (A.out_fp32) {
         float* o = (float*)A.out;
         for (int i = tid; i < ND * ND; i += ASM_THREADS) {
@@ -398,8 +463,8 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
 template <int PD> size_t asm_smem() {
     using D = Deg<PD>;
     constexpr int QC = D::NQ3 < 32 ? D::NQ3 : 32;
-    size_t vol = (size_t)QC * D::NP * 4 + QC;
-    size_t face = (size_t)D::NQ2 * 3 + 2 * (size_t)D::NQ2 * D::NP * 4;
+    size_t vol = (size_t)QC * D::NP * 4 + QC + (size_t)QC * 3 * (PD + 1) * 2;
+    size_t face = (size_t)D::NQ2 * 3 + 2 * (size_t)D::NQ2 * D::NP * 4 + 2 * (size_t)D::NQ2 * 3 * (PD + 1) * 2;
     return sizeof(double) * ((size_t)D::ND * D::ND + (vol > face ? vol : face));
 }
 
@@ -581,6 +646,13 @@ __global__ void __launch_bounds__(VEC_THREADS) k_vector(VecArgs A) {
     double* s_dat = s_dphi + NQ2 * 3 * NP;// [NQ3][3]
     double* s_w = s_dat + NQ3 * 3;        // [NQ3]
     double* s_pt = s_w + NQ3;             // [NQ2][3]
+    // 1-D factors of basis_eval (legendre_1d of each coordinate and degree):
+    // volume [NQ3][3][L1] values, faces [NQ2][3][L1] (value, derivative)
+    // pairs; the basis values are their products in basis_eval's order, so
+    // they are the same bits at 3 (p+1) instead of 3 Np legendre_1d calls
+    constexpr int L1 = PD + 1;
+    static_assert(NQ3 >= 2 * NQ2, "the face table fits the volume table's space");
+    double* s_tab = s_pt + NQ2 * 3;
     const int tid = threadIdx.x, P = blockIdx.x;
     const double* bb = &A.bbox[P * 6];
     for (int i = tid; i < ND; i += VEC_THREADS) s_acc[i] = 0.0;
@@ -591,18 +663,26 @@ __global__ void __launch_bounds__(VEC_THREADS) k_vector(VecArgs A) {
         const double rho = A.mat[mid * 3 + 0], lam = A.mat[mid * 3 + 1], mu = A.mat[mid * 3 + 2];
         const double aj = fabs(A.jdet[t]);
         __syncthreads();
-        for (int it = tid; it < NQ3 * NP; it += VEC_THREADS) {
-            const int q = it / NP, f = it % NP;
-            double pt[3], dp[3];
+        for (int it = tid; it < NQ3 * 3 * L1; it += VEC_THREADS) {
+            const int q = it / (3 * L1), rr = it % (3 * L1), d = rr / L1, deg = rr % L1;
+            double pt[3], v, dv;
             tet_point(fk, A.ref, q, pt);
-            basis_eval(pt, bb, &A.ref->blist[f * 3], &s_phi[q * NP + f], dp);
-            if (f == 0) {
+            legendre_1d(pt[d], deg, bb[2 * d], bb[2 * d + 1], &v, &dv);
+            s_tab[it] = v;
+            if (rr == 0) {
                 double r[3];
                 if (A.mode == 0) dev_forcing(A.fid, lam, mu, pt, rho, r);
                 else dev_analytic(A.fid, pt, r);
                 s_dat[q * 3 + 0] = r[0]; s_dat[q * 3 + 1] = r[1]; s_dat[q * 3 + 2] = r[2];
                 s_w[q] = aj * A.ref->weitet3[q];
             }
+        }
+        __syncthreads();
+        for (int it = tid; it < NQ3 * NP; it += VEC_THREADS) {
+            const int q = it / NP, f = it % NP;
+            const int* bl = &A.ref->blist[f * 3];
+            const double* tq = s_tab + q * 3 * L1;
+            s_phi[q * NP + f] = tq[bl[0]] * tq[L1 + bl[1]] * tq[2 * L1 + bl[2]];
         }
         __syncthreads();
         for (int r = tid; r < ND; r += VEC_THREADS) {
@@ -643,13 +723,22 @@ __global__ void __launch_bounds__(VEC_THREADS) k_vector(VecArgs A) {
                 s_dat[q * 3 + 0] = g[0]; s_dat[q * 3 + 1] = g[1]; s_dat[q * 3 + 2] = g[2];
             }
             __syncthreads();
+            for (int it = tid; it < NQ2 * 3 * L1; it += VEC_THREADS) {
+                const int q = it / (3 * L1), rr = it % (3 * L1), d = rr / L1, deg = rr % L1;
+                legendre_1d(s_pt[q * 3 + d], deg, bb[2 * d], bb[2 * d + 1], &s_tab[2 * it], &s_tab[2 * it + 1]);
+            }
+            __syncthreads();
             for (int it = tid; it < NQ2 * NP; it += VEC_THREADS) {
                 const int q = it / NP, fb = it % NP;
-                double dp[3];
-                basis_eval(&s_pt[q * 3], bb, &A.ref->blist[fb * 3], &s_phi[q * NP + fb], dp);
-                s_dphi[(q * 3 + 0) * NP + fb] = dp[0];
-                s_dphi[(q * 3 + 1) * NP + fb] = dp[1];
-                s_dphi[(q * 3 + 2) * NP + fb] = dp[2];
+                const int* bl = &A.ref->blist[fb * 3];
+                const double* tq = s_tab + 2 * q * 3 * L1;
+                const double vx = tq[2 * bl[0]], dx = tq[2 * bl[0] + 1];
+                const double vy = tq[2 * (L1 + bl[1])], dy = tq[2 * (L1 + bl[1]) + 1];
+                const double vz = tq[2 * (2 * L1 + bl[2])], dz = tq[2 * (2 * L1 + bl[2]) + 1];
+                s_phi[q * NP + fb] = vx * vy * vz;
+                s_dphi[(q * 3 + 0) * NP + fb] = dx * vy * vz;
+                s_dphi[(q * 3 + 1) * NP + fb] = vx * dy * vz;
+                s_dphi[(q * 3 + 2) * NP + fb] = vx * vy * dz;
             }
             __syncthreads();
             const double sigma = A.alpha * (double)(PD * PD) / A.hk[P] * (lam + 2 * mu);
@@ -817,7 +906,7 @@ __global__ void k_double_couple(int Np, int nq3, int t, int P, const double* __r
 
 template <int PD>
 int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass, const int64_t* list,
-                    int64_t n_list, int64_t out_stride) {
+                    int64_t n_list, int64_t out_stride, bool out_at_block = false) {
     size_t smem = asm_smem<PD>();
     LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_assemble<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     AsmArgs A;
@@ -827,7 +916,7 @@ int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write
     A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.alpha = c->alpha; A.theta = c->theta;
     A.which = which; A.out_fp32 = out_fp32; A.out = out;
     A.M = write_mass ? c->d_M : nullptr; A.Mm = write_mass ? c->d_Mm : nullptr;
-    A.list = list; A.out_stride = out_stride;
+    A.list = list; A.out_stride = out_stride; A.out_at_block = out_at_block ? 1 : 0;
     const int64_t n = list ? n_list : c->n_blocks;
     const int64_t chunk = 1 << 20;
     for (int64_t b0 = 0; b0 < n; b0 += chunk) {
@@ -848,7 +937,9 @@ int launch_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scal
     A.area = c->d_area; A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.alpha = c->alpha; A.theta = c->theta;
     A.mode = mode; A.fid = fid; A.did = did; A.nid = nid; A.R = c->d_Rm; A.RT = c->d_RmT; A.scale = scale; A.out = out;
     using D = Deg<PD>;
-    size_t smem = sizeof(double) * ((size_t)D::ND + D::NQ3 * D::NP + D::NQ2 * 3 * D::NP + D::NQ3 * 3 + D::NQ3 + D::NQ2 * 3);
+    // + the 1-D factor table (NQ3 * 3 (p+1) >= NQ2 * 3 (p+1) * 2 doubles)
+    size_t smem = sizeof(double) * ((size_t)D::ND + D::NQ3 * D::NP + D::NQ2 * 3 * D::NP + D::NQ3 * 3 + D::NQ3 + D::NQ2 * 3 +
+                                    (size_t)D::NQ3 * 3 * (PD + 1));
     LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_vector<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_vector<PD><<<c->n_poly, VEC_THREADS, smem, c->stream>>>(A);
     c->launches++;
@@ -896,6 +987,18 @@ int lymph_dev_assemble_list(lymph_ctx* c, int which, void* out, int out_fp32, bo
 // gives them).
 int lymph_dev_mass(lymph_ctx* c, const int64_t* self_list) {
     return lymph_dev_assemble_list(c, ASM_MASS_ONLY, nullptr, 0, true, self_list, c->n_poly, 0);
+}
+
+// Blocks list[0..n_list) each into its own slot of the block-CSR array out.
+int lymph_dev_assemble_at(lymph_ctx* c, int which, void* out, int out_fp32, const int64_t* list, int64_t n_list) {
+    const int64_t st = (int64_t)c->nd * c->nd;
+    switch (c->p) {
+        case 1: return launch_assemble<1>(c, which, out, out_fp32, false, list, n_list, st, true);
+        case 2: return launch_assemble<2>(c, which, out, out_fp32, false, list, n_list, st, true);
+        case 3: return launch_assemble<3>(c, which, out, out_fp32, false, list, n_list, st, true);
+        case 4: return launch_assemble<4>(c, which, out, out_fp32, false, list, n_list, st, true);
+        default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
+    }
 }
 
 int lymph_dev_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {

@@ -1,8 +1,10 @@
-"""The tensor-core self blocks of LYMPH_MIXED_MF (csrc/selftc.cu) against the
-FP64 assembly.
+"""The tensor-core self blocks of the mixed operators (csrc/selftc.cu) against
+the FP64 assembly.
 
-The matrix-free mixed path stores only each polyhedron's self block, in FP32,
-assembled by k_self_tc<p> on the tcgen05 tensor cores: kind::tf32 MMAs of
+The matrix-free mixed path (LYMPH_MIXED_MF) stores only each polyhedron's
+self block, in FP32, and the FP32-block path (LYMPH_MIXED) stores it first in
+each block row; both are assembled by k_self_tc<p> on the tcgen05 tensor
+cores: kind::tf32 MMAs of
 operands split into their nearest TF32 value and the TF32-rounded remainder
 (four products, FP32-accurate), FP32 accumulation in tensor memory drained
 to registers after every 32 quadrature slots (the tensor cores' accumulation
@@ -13,8 +15,10 @@ truncates).  Bars (written in each assertion):
     FP32 rounding of the FP64 block alone, printed beside it, is ~5e-8, and
     the algebra of the decomposition is checked in FP64 on the CPU
     (tests/test_selfblock_formula.py, 1e-12);
-  * the mass matrices of the matrix-free context (the k_assemble CTAs with
-    the stiffness skipped) equal the FP64 context's bit for bit;
+  * the mass matrices of the mixed contexts (the k_assemble CTAs with the
+    stiffness skipped) equal the FP64 context's bit for bit, and so do
+    LYMPH_MIXED's neighbour blocks once the FP64 ones are rounded to FP32
+    (the FP64 assembly, rounded);
   * the operator apply of the whole path stays within TOL_APPLY_FP32 of the
     oracle (tests/test_gpu_mf.py, every mesh kind and degree).
 """
@@ -29,10 +33,11 @@ pytestmark = pytest.mark.gpu
 TOL_SELF = 1e-6
 
 
-def _self_and_mass(m, p, precision, theta=-1.0):
+def _self_and_mass(m, p, precision, theta=-1.0, blocks=False):
     with MatrixFree(m, p, 1e-3, precision=precision, theta=theta) as g:
         g.MAKE_MATRICES_FREE()
-        return g.self_blocks(), g.mass(0), g.mass(1)
+        out = (g.self_blocks(), g.mass(0), g.mass(1))
+        return out + ((g.blocks(), g.pattern()[0]) if blocks else ())
 
 
 def _apply_rel(Ka, Kb, seed):
@@ -46,13 +51,18 @@ def _apply_rel(Ka, Kb, seed):
 @pytest.mark.parametrize("p", [1, 2, 3, 4])
 def test_tensor_core_self_blocks_match_fp64_assembly(require_gpu, kind, p):
     m = _mesh(kind)
-    K64, M64, Mm64 = _self_and_mass(m, p, _lib.FP64)
-    Ktc, Mtc, Mmtc = _self_and_mass(m, p, _lib.MIXED_MF)
-    e = _apply_rel(Ktc, K64, 7 + p)
+    K64, M64, Mm64, B64, rp = _self_and_mass(m, p, _lib.FP64, blocks=True)
     e_round = _apply_rel(K64.astype(np.float32).astype(np.float64), K64, 7 + p)
-    print(f"{kind} p={p}: tensor-core self blocks {e:.2e} (FP32 rounding of the FP64 blocks {e_round:.2e})")
-    assert e <= TOL_SELF, e
-    assert np.array_equal(Mtc, M64) and np.array_equal(Mmtc, Mm64)
+    for name, prec in (("mixed_mf", _lib.MIXED_MF), ("fp32_blocks", _lib.MIXED)):
+        got = _self_and_mass(m, p, prec, blocks=(prec == _lib.MIXED))
+        Ktc, Mtc, Mmtc = got[:3]
+        e = _apply_rel(Ktc, K64, 7 + p)
+        print(f"{kind} p={p} {name}: tensor-core self blocks {e:.2e} (FP32 rounding of the FP64 blocks {e_round:.2e})")
+        assert e <= TOL_SELF, (name, e)
+        assert np.array_equal(Mtc, M64) and np.array_equal(Mmtc, Mm64), name
+        if prec == _lib.MIXED:
+            nb = np.setdiff1d(np.arange(B64.shape[0]), rp[:-1])   # every block but the self blocks
+            assert np.array_equal(got[3][nb], B64[nb].astype(np.float32).astype(np.float64))
 
 
 @pytest.mark.parametrize("theta", [0.0, 1.0])
