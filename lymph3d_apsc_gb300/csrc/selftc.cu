@@ -33,15 +33,17 @@
 // volume integrals the reference's collapsed Gauss rule.
 //
 // One CTA of 512 threads per polyhedron.  The K slots come in chunks of 32
-// (the tetrahedra's volume points, then the faces); per chunk warp 0 maps
-// each slot to its physical point, weights and Legendre values, all 16
-// warps write the operands into shared memory, each value split into its
-// nearest TF32 value and the TF32-rounded remainder (together within 2^-23
-// of the value), in the 128-byte-swizzled K-major layout the MMA reads, and
-// thread 0 issues the four products A_hi B_hi + A_hi B_lo + A_lo B_hi +
-// A_lo B_lo (FP32-accurate, not TF32 rounded) into an FP32 accumulator in
-// tensor memory.  Two operand stages
-// let the tabulation of one chunk overlap the MMAs of the last.  The tensor
+// (the tetrahedra's volume points, then the faces).  P's tetrahedra (map,
+// |J|, material) and faces (quadrature map, normal, area, weight factors)
+// are staged in shared memory at CTA start; while warp 0 maps each slot of
+// the next chunk to its physical point, weights and Legendre values, warps
+// 1-15 write the current chunk's operands into shared memory, each value
+// split into its nearest TF32 value and the TF32-rounded remainder (together
+// within 2^-23 of the value), in the 128-byte-swizzled K-major layout the MMA
+// reads, and lane 0 of warp 1 issues the four products A_hi B_hi + A_hi B_lo
+// + A_lo B_hi + A_lo B_lo (FP32-accurate, not TF32 rounded) into an FP32
+// accumulator in tensor memory.  Two operand stages let the tabulation of
+// one chunk overlap the MMAs of the last.  The tensor
 // cores add each MMA's products to the accumulator with truncation (round
 // toward zero: an emulation with that rounding reproduces the measured
 // errors, one with round-to-nearest gives 10x less), so the error grows
@@ -68,7 +70,9 @@ using namespace umma;
 
 constexpr int ST_THREADS = 512;   // 16 warps: 4 per tensor-memory lane quadrant
 constexpr int ST_BK = 32;         // K slots per chunk (4 MMAs of K = 8)
-constexpr int ST_SEG = 1;         // chunks per accumulation segment (drained into registers after each)
+constexpr int ST_TMAX = 32;       // tetrahedra of a polyhedron kept in shared memory (the rest read from the arrays)
+constexpr int ST_FMAX = 64;       // faces of a polyhedron kept in shared memory
+constexpr int ST_FW = 18;         // floats per face entry (face_entry)
 constexpr int ST_FACE_NQ[5] = {0, 3, 6, 12, 16};   // nodes of the symmetric triangle rule (mf.cu)
 
 template <int PD> struct TcShape {
@@ -86,15 +90,20 @@ template <int PD> struct TcShape {
     static constexpr size_t A_TILE = 128 * 128;      // 128 rows x 32 TF32 slots
     static constexpr size_t B_TILE = (size_t)NT * 128;
     static constexpr size_t STAGE = 2 * A_TILE + 2 * B_TILE;
-    static constexpr size_t LEG_OFF = 2 * STAGE;
-    static constexpr size_t COEF_OFF = LEG_OFF + (size_t)ST_BK * LS * 8;
-    static constexpr size_t BAR_OFF = COEF_OFF + (size_t)ST_BK * 3 * 16;
+    static constexpr size_t LEG_OFF = 2 * STAGE;                             // two slot buffers
+    static constexpr size_t COEF_OFF = LEG_OFF + 2 * (size_t)ST_BK * LS * 8;
+    static constexpr size_t TET_OFF = COEF_OFF + 2 * (size_t)ST_BK * 3 * 16;
+    static constexpr size_t FACE_OFF = TET_OFF + (size_t)ST_TMAX * 16 * 4;
+    static constexpr size_t REF_OFF = FACE_OFF + (size_t)ST_FMAX * ST_FW * 4;   // the volume rule in FP32
+    static constexpr size_t BAR_OFF = REF_OFF + (size_t)NQ3 * 4 * 4;
     static constexpr size_t SMEM = BAR_OFF + 64 + 1024;   // + room to align the base to 1 KB
     static_assert(NT <= 256 && NT % 16 == 0, "MMA N");
     static_assert(2 * NT <= TCOLS, "two accumulators");
     static_assert(NCOL % 8 == 0, "drain in x16/x8 loads");
     static_assert(2 * (size_t)ND * ND * 4 <= 2 * STAGE, "epilogue staging fits the operand stages");
-    static_assert(COEF_OFF % 16 == 0 && BAR_OFF % 8 == 0, "alignment");
+    static_assert(COEF_OFF % 16 == 0 && TET_OFF % 16 == 0 && FACE_OFF % 8 == 0 && REF_OFF % 16 == 0 && BAR_OFF % 8 == 0,
+                  "alignment");
+    static_assert(SMEM <= 232448, "shared memory per CTA");
 };
 
 // the reference's basis order as degree triples, per degree
@@ -129,12 +138,82 @@ struct SelfTcArgs {
     float* out;            // column-major ND x ND blocks: P's at slot P, or at slot row_ptr[P]
     int slot_row_ptr;      // 1: the block-CSR operator of LYMPH_MIXED (self block first in each row)
     int* status;
-    double frule[3 * 16];  // (xi, eta, w) of the symmetric triangle rule
+    float frule[3 * 16];   // (xi, eta, w) of the symmetric triangle rule
 };
 
 // v rounded to the nearest TF32 value (10 explicit mantissa bits; ties away
 // from zero), exact in TF32
 __device__ __forceinline__ float tf32_rn(float v) { return __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u); }
+
+// P's box: centre and inverse half-widths, in FP64.
+struct Box {
+    double c[3], ih[3];
+};
+__device__ __forceinline__ Box box_of(const double* bb) {
+    Box b;
+    for (int d = 0; d < 3; ++d) {
+        b.c[d] = (bb[2 * d] + bb[2 * d + 1]) / 2.0;
+        b.ih[d] = 2.0 / (bb[2 * d + 1] - bb[2 * d]);
+    }
+    return b;
+}
+
+// Tetrahedron tt in P's box coordinates (FP64 arithmetic, FP32 result):
+// xhat = M (xi, eta, zeta) + v for the reference point (xi, eta, zeta) of
+// jacobians' affine map (Poly_ref_mappings.f90:18-75), M = diag(ih) Fk[:, 0:3],
+// v = diag(ih) (Fk[:, 3] - c); then |J|, lambda, mu.  out[16].
+__device__ __noinline__ void tet_entry(const SelfTcArgs& A, const Box& bx, int tt, float* out) {
+    const double* F = A.fk + (int64_t)tt * 12;
+    for (int d = 0; d < 3; ++d) {
+        for (int l = 0; l < 3; ++l) out[d * 3 + l] = (float)(F[d * 4 + l] * bx.ih[d]);
+        out[9 + d] = (float)((F[d * 4 + 3] - bx.c[d]) * bx.ih[d]);
+    }
+    const int mid = A.tet_mat[tt];
+    out[12] = (float)fabs(A.jdet[tt]);
+    out[13] = (float)A.mat[mid * 3 + 1];
+    out[14] = (float)A.mat[mid * 3 + 2];
+    out[15] = 0.f;
+}
+
+// Entry e of P's self-block face list in P's box coordinates (FP64
+// arithmetic, FP32 result): the quadrature map xhat = o + xi e1 + eta e2 of
+// basis_boundary (basis_function.f90:560-577: x = Fk node_maps(:,:,f)
+// (xi, eta, 1, 1)), P's outward normal, the area and the factors of the slot
+// weights W = w_q area: theta cI lambda, theta cI mu, -cI lambda, -cI mu,
+// sigma / 2 (cI = 1 on a Dirichlet face, 1/2 on a shared one; lambda, mu of
+// P's tetrahedron).  out[ST_FW].
+template <int PD>
+__device__ __noinline__ void face_entry(const SelfTcArgs& A, int P, const Box& bx, int64_t e, float* out) {
+    const int code = A.bf[e];
+    const int tt = code >> 2, f = code & 3;
+    const int E2 = A.neigh[code];
+    const bool dir = (E2 == LYMPH_BC_DIRI);
+    const double hmin = dir ? A.hk[P] : fmin(A.hk[P], A.hk[A.tet_poly[E2]]);
+    const int mid = A.tet_mat[tt];
+    const double lam = A.mat[mid * 3 + 1], mu = A.mat[mid * 3 + 2];
+    const double sigma = A.alpha * (double)(PD * PD) / hmin * (lam + 2.0 * mu);
+    const double cI = dir ? 1.0 : 0.5;
+    const double* F = A.fk + (int64_t)tt * 12;
+    const double* nm = A.ref->node_maps + f * 16;
+    for (int d = 0; d < 3; ++d) {
+        double cm[4];
+        for (int l = 0; l < 4; ++l) {
+            double s = 0.0;
+            for (int m = 0; m < 4; ++m) s += F[d * 4 + m] * nm[m * 4 + l];
+            cm[l] = s;
+        }
+        out[d] = (float)((cm[2] + cm[3] - bx.c[d]) * bx.ih[d]);
+        out[3 + d] = (float)(cm[0] * bx.ih[d]);
+        out[6 + d] = (float)(cm[1] * bx.ih[d]);
+        out[9 + d] = (float)A.nrm[(int64_t)tt * 12 + f * 3 + d];
+    }
+    out[12] = (float)A.area[(int64_t)tt * 4 + f];
+    out[13] = (float)(A.theta * cI * lam);
+    out[14] = (float)(A.theta * cI * mu);
+    out[15] = (float)(-cI * lam);
+    out[16] = (float)(-cI * mu);
+    out[17] = (float)(0.5 * sigma);
+}
 
 // value v into row `row`, slot k of a 128-byte-swizzled K-major tile pair:
 // hi = v rounded to TF32, lo = the remainder v - hi (exact in FP32, at most
@@ -174,8 +253,11 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     extern __shared__ __align__(1024) char smem_raw[];
     // the swizzle pattern is a function of the address: align the stages to 1 KB
     char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    float2* leg = (float2*)(smem + S::LEG_OFF);    // [32][LS]: (L, L') of x, y, z per slot
-    float4* coef = (float4*)(smem + S::COEF_OFF);  // [32][3]: slot coefficients and normal
+    float2* leg = (float2*)(smem + S::LEG_OFF);      // [2][32][LS]: (L, L') of x, y, z per slot
+    float4* coef = (float4*)(smem + S::COEF_OFF);    // [2][32][3]: slot coefficients and normal
+    float* s_tet = (float*)(smem + S::TET_OFF);      // [ST_TMAX][16]: P's tetrahedra (tet_entry)
+    float* s_face = (float*)(smem + S::FACE_OFF);    // [ST_FMAX][ST_FW]: P's faces (face_entry)
+    float4* s_ref = (float4*)(smem + S::REF_OFF);    // [NQ3]: the volume rule's (xi, eta, zeta, w)
     uint64_t* bars = (uint64_t*)(smem + S::BAR_OFF);
     uint32_t* tmem_slot = (uint32_t*)(bars + 2);
     __shared__ int s_ok;
@@ -183,13 +265,31 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int P = blockIdx.x;
     const uint32_t sbase = smem_u32(smem);
+    constexpr int ISSUER = 32;   // lane 0 of warp 1 waits on the barriers and issues the MMAs
     // after one CTA's wait ran out the launch has failed: the others return
     // at once instead of waiting out their own limits
     if (*(volatile int*)A.status & ST_TIMEOUT) return;
 
+    const int t0 = A.poly_ptr[P], ntet = A.poly_ptr[P + 1] - t0;
+    const int64_t kself = A.row_ptr[P];   // the self block leads its row
+    const int64_t f0 = A.bf_ptr[kself];
+    const int nface = (int)(A.bf_ptr[kself + 1] - f0);
+    const int nvc = ntet * S::CPT;
+    const int nch = nvc + (nface + S::FPC - 1) / S::FPC;
+    const double* bb = A.bbox + (int64_t)P * 6;
+    const Box bx = box_of(bb);
+
     // zero both operand stages: padding rows are never written again
     for (int i = t; i < (int)(2 * S::STAGE / 16); i += ST_THREADS) ((float4*)smem)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const double* bb = A.bbox + (int64_t)P * 6;
+    // P's tetrahedra and faces in its box coordinates, and the volume rule,
+    // in shared memory and FP32, so the per-chunk slot set-up reads no global
+    // memory and does no FP64 arithmetic (beyond ST_TMAX / ST_FMAX it forms
+    // the entries from the arrays)
+    if (t < ntet && t < ST_TMAX) tet_entry(A, bx, A.poly_tets[t0 + t], s_tet + t * 16);
+    if (t >= 64 && t - 64 < nface && t - 64 < ST_FMAX) face_entry<PD>(A, P, bx, f0 + (t - 64), s_face + (t - 64) * ST_FW);
+    for (int q = t; q < S::NQ3; q += ST_THREADS)
+        s_ref[q] = make_float4((float)A.ref->nodtet3[q * 4], (float)A.ref->nodtet3[q * 4 + 1],
+                               (float)A.ref->nodtet3[q * 4 + 2], (float)A.ref->weitet3[q]);
     if (t == 0) {
         double hprod = 1.0;
         for (int d = 0; d < 3; ++d) {
@@ -212,121 +312,113 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-
-    const int t0 = A.poly_ptr[P], ntet = A.poly_ptr[P + 1] - t0;
-    const int64_t kself = A.row_ptr[P];   // the self block leads its row
-    const int64_t f0 = A.bf_ptr[kself];
-    const int nface = (int)(A.bf_ptr[kself + 1] - f0);
-    const int nvc = ntet * S::CPT;
-    const int nch = nvc + (nface + S::FPC - 1) / S::FPC;
     const float sc = s_box[3], sx = sc * s_box[0], sy = sc * s_box[1], sz = sc * s_box[2];
     const int grp = warp >> 2;                                   // column group of the drain
     const uint32_t tq = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(grp * S::NCOL);
     const uint32_t idesc = idesc_tf32(128, S::NT);
+
+    // warp 0: slot `lane` of chunk c -> point (box coordinates), weights,
+    // Legendre values, into buffer b; FP32 from the tables
+    auto slot_setup = [&](int c, int b) {
+        const int k = lane;
+        float xh[3] = {0.f, 0.f, 0.f};
+        float bd = 0.f, bn = 0.f, dd = 0.f, dn = 0.f, sd = 0.f, sn = 0.f, nv[3] = {0.f, 0.f, 0.f};
+        if (c < nvc) {
+            const int q = (c % S::CPT) * ST_BK + k, j = c / S::CPT;
+            if (q < S::NQ3) {
+                float e[16];
+                if (j < ST_TMAX) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) e[i] = s_tet[j * 16 + i];
+                } else {   // beyond the table (out of line: few registers on the common path)
+                    float ev[16];
+                    tet_entry(A, bx, A.poly_tets[t0 + j], ev);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) e[i] = ev[i];
+                }
+                const float4 r = s_ref[q];
+                for (int d = 0; d < 3; ++d)
+                    xh[d] = fmaf(e[d * 3 + 0], r.x, fmaf(e[d * 3 + 1], r.y, fmaf(e[d * 3 + 2], r.z, e[9 + d])));
+                const float w = r.w * e[12];
+                bd = 1.f;
+                dd = w * e[13];
+                sd = w * e[14];
+            }
+        } else {
+            const int fi = (c - nvc) * S::FPC + k / (2 * S::NF), r = k % (2 * S::NF);
+            if (k < S::FPC * 2 * S::NF && fi < nface) {
+                float e[ST_FW];
+                if (fi < ST_FMAX) {
+#pragma unroll
+                    for (int i = 0; i < ST_FW; ++i) e[i] = s_face[fi * ST_FW + i];
+                } else {
+                    float ev[ST_FW];
+                    face_entry<PD>(A, P, bx, f0 + fi, ev);
+#pragma unroll
+                    for (int i = 0; i < ST_FW; ++i) e[i] = ev[i];
+                }
+                const int q = r % S::NF;
+                const float xi = A.frule[3 * q], eta = A.frule[3 * q + 1], W = A.frule[3 * q + 2] * e[12];
+                for (int d = 0; d < 3; ++d) {
+                    xh[d] = fmaf(eta, e[6 + d], fmaf(xi, e[3 + d], e[d]));
+                    nv[d] = e[9 + d];
+                }
+                if (r < S::NF) {   // "d" slot
+                    bd = 1.f;
+                    dn = e[13] * W;
+                    sn = e[14] * W;
+                } else {           // "n phi" slot
+                    bn = 1.f;
+                    dd = e[15] * W;
+                    sd = e[16] * W;
+                    sn = e[17] * W;
+                }
+            }
+        }
+        float2* lg = leg + (b * ST_BK + k) * S::LS;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) legendre_f32<PD>(xh[d], lg + d * L);
+        float4* cf = coef + (b * ST_BK + k) * 3;
+        cf[0] = make_float4(bd, bn, dd, dn);
+        cf[1] = make_float4(sd, sn, nv[0], nv[1]);
+        cf[2] = make_float4(nv[2], 0.f, 0.f, 0.f);
+    };
 
     float run[S::NCOL];
 #pragma unroll
     for (int j = 0; j < S::NCOL; ++j) run[j] = 0.0f;
     bool ok = true;
     int issued = 0;
+    if (warp == 0 && nch > 0) slot_setup(0, 0);
     for (int c = 0; c < nch; ++c) {
-        const int st = c & 1, seg = c / ST_SEG;
-        // the MMAs of chunk c - 2 read this stage: thread 0 waits for them
-        if (c >= 2 && t == 0) s_ok = mbar_wait(smem_u32(&bars[st]), (uint32_t)(((c - 2) >> 1) & 1)) ? 1 : 0;
-        // ---- warp 0: slot `lane` of chunk c -> point, weights, Legendre values ----
-        if (warp == 0) {
-            const int k = lane;
-            double xg[3] = {0.0, 0.0, 0.0};
-            float bd = 0.f, bn = 0.f, dd = 0.f, dn = 0.f, sd = 0.f, sn = 0.f, nv[3] = {0.f, 0.f, 0.f};
-            bool valid = false;
-            if (c < nvc) {
-                const int q = (c % S::CPT) * ST_BK + k;
-                if (q < S::NQ3) {
-                    const int tt = A.poly_tets[t0 + c / S::CPT];
-                    const double* F = A.fk + (int64_t)tt * 12;
-                    const double* rp = A.ref->nodtet3 + q * 4;
-                    for (int d = 0; d < 3; ++d)
-                        xg[d] = F[d * 4 + 0] * rp[0] + F[d * 4 + 1] * rp[1] + F[d * 4 + 2] * rp[2] + F[d * 4 + 3] * rp[3];
-                    const double w = A.ref->weitet3[q] * fabs(A.jdet[tt]);
-                    const int mid = A.tet_mat[tt];
-                    bd = 1.f;
-                    dd = (float)(w * A.mat[mid * 3 + 1]);
-                    sd = (float)(w * A.mat[mid * 3 + 2]);
-                    valid = true;
-                }
-            } else {
-                const int fi = (c - nvc) * S::FPC + k / (2 * S::NF), r = k % (2 * S::NF);
-                if (k < S::FPC * 2 * S::NF && fi < nface) {
-                    const int code = A.bf[f0 + fi];
-                    const int tt = code >> 2, f = code & 3;
-                    const int E2 = A.neigh[code];
-                    const bool dir = (E2 == LYMPH_BC_DIRI);
-                    const double hmin = dir ? A.hk[P] : fmin(A.hk[P], A.hk[A.tet_poly[E2]]);
-                    const int mid = A.tet_mat[tt];
-                    const double lam = A.mat[mid * 3 + 1], mu = A.mat[mid * 3 + 2];
-                    const double sigma = A.alpha * (double)(PD * PD) / hmin * (lam + 2.0 * mu);
-                    const double cI = dir ? 1.0 : 0.5;
-                    const int q = r % S::NF;
-                    const double xi = A.frule[3 * q], eta = A.frule[3 * q + 1];
-                    const double W = A.frule[3 * q + 2] * A.area[(int64_t)tt * 4 + f];
-                    // the face map of basis_boundary (basis_function.f90:560-577): x = Fk node_maps(:,:,f) (xi, eta, 1, 1)
-                    const double* F = A.fk + (int64_t)tt * 12;
-                    const double* nm = A.ref->node_maps + f * 16;
-                    for (int d = 0; d < 3; ++d) {
-                        double cm[4];
-                        for (int l = 0; l < 4; ++l) {
-                            double s = 0.0;
-                            for (int m = 0; m < 4; ++m) s += F[d * 4 + m] * nm[m * 4 + l];
-                            cm[l] = s;
-                        }
-                        xg[d] = cm[2] + cm[3] + xi * cm[0] + eta * cm[1];
-                        nv[d] = (float)A.nrm[(int64_t)tt * 12 + f * 3 + d];
-                    }
-                    if (r < S::NF) {   // "d" slot
-                        bd = 1.f;
-                        dn = (float)(A.theta * cI * W * lam);
-                        sn = (float)(A.theta * cI * W * mu);
-                    } else {           // "n phi" slot
-                        bn = 1.f;
-                        dd = (float)(-cI * W * lam);
-                        sd = (float)(-cI * W * mu);
-                        sn = (float)(0.5 * sigma * W);
-                    }
-                    valid = true;
-                }
-            }
-            float2* lg = leg + k * S::LS;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const double cen = (bb[2 * d] + bb[2 * d + 1]) / 2.0, h = (bb[2 * d + 1] - bb[2 * d]) / 2.0;
-                legendre_f32<PD>(valid ? (float)((xg[d] - cen) / h) : 0.0f, lg + d * L);
-            }
-            coef[k * 3 + 0] = make_float4(bd, bn, dd, dn);
-            coef[k * 3 + 1] = make_float4(sd, sn, nv[0], nv[1]);
-            coef[k * 3 + 2] = make_float4(nv[2], 0.f, 0.f, 0.f);
-        }
+        const int st = c & 1;
+        // the MMAs of chunk c - 2 read this stage and wrote the accumulator
+        // chunk c takes: the issuing thread waits for them
+        if (c >= 2 && t == ISSUER) s_ok = mbar_wait(smem_u32(&bars[st]), (uint32_t)(((c - 2) >> 1) & 1)) ? 1 : 0;
         __syncthreads();
         if (c >= 2 && !s_ok) {
             ok = false;
             break;
         }
-        // a chunk that starts segment seg >= 2 reuses the accumulator of
-        // segment seg - 2, whose MMAs (chunks up to c - 2) are complete
-        if (c % ST_SEG == 0 && seg >= 2) {
+        if (c >= 2) {   // chunk c - 2's products, complete, into the running sums
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            drain<S::NCOL>(tq + (uint32_t)((seg & 1) * S::NT), run);
+            drain<S::NCOL>(tq + (uint32_t)(st * S::NT), run);
         }
-        // ---- all warps: the operands of chunk c, basis function a = warp + 16 i, slot = lane ----
-        {
+        if (warp == 0) {
+            // the next chunk's slots while warps 1-15 write this chunk's operands
+            if (c + 1 < nch) slot_setup(c + 1, (c + 1) & 1);
+        } else {
+            // ---- the operands of chunk c: basis function a = warp - 1 + 15 i, slot = lane ----
             char* ahi = smem + st * S::STAGE;
             char* alo = ahi + S::A_TILE;
             char* bhi = alo + S::A_TILE;
             char* blo = bhi + S::B_TILE;
             const int k = lane;
-            const float4 c0 = coef[k * 3 + 0], c1 = coef[k * 3 + 1];
-            const float n3[3] = {c1.z, c1.w, coef[k * 3 + 2].x};
-            const float2* lg = leg + k * S::LS;
-            for (int a = warp; a < NP; a += ST_THREADS / 32) {
+            const float4* cf = coef + (st * ST_BK + k) * 3;
+            const float4 c0 = cf[0], c1 = cf[1];
+            const float n3[3] = {c1.z, c1.w, cf[2].x};
+            const float2* lg = leg + (st * ST_BK + k) * S::LS;
+            for (int a = warp - 1; a < NP; a += ST_THREADS / 32 - 1) {
                 const int3 tr = blist_row<PD>(a);
                 const float2 X = lg[tr.x], Y = lg[L + tr.y], Z = lg[2 * L + tr.z];
                 const float yz = Y.x * Z.x;
@@ -341,20 +433,20 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
                     put_split(bhi, blo, S::NH + row, k, fmaf(c1.x, g[i], c1.y * np_));
                 }
             }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic-proxy writes -> the MMAs
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic-proxy writes -> the MMAs
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        if (t == 0) {
+        if (t == ISSUER) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t ahi = sbase + (uint32_t)(st * S::STAGE), alo = ahi + (uint32_t)S::A_TILE;
             const uint32_t bhi = alo + (uint32_t)S::A_TILE, blo = bhi + (uint32_t)S::B_TILE;
-            const uint32_t d = tmem + (uint32_t)((seg & 1) * S::NT);
+            const uint32_t d = tmem + (uint32_t)(st * S::NT);
 #pragma unroll
             for (int j = 0; j < ST_BK / 8; ++j) {   // k-step j: bytes 32 j .. 32 j + 31 of every row
                 const uint64_t dah = sdesc_sw128(ahi + 32 * j), dal = sdesc_sw128(alo + 32 * j);
                 const uint64_t dbh = sdesc_sw128(bhi + 32 * j), dbl = sdesc_sw128(blo + 32 * j);
-                mma_tf32(d, dah, dbh, idesc, (c % ST_SEG == 0 && j == 0) ? 0u : 1u);
+                mma_tf32(d, dah, dbh, idesc, j == 0 ? 0u : 1u);
                 mma_tf32(d, dah, dbl, idesc, 1u);
                 mma_tf32(d, dal, dbh, idesc, 1u);
                 mma_tf32(d, dal, dbl, idesc, 1u);
@@ -364,7 +456,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
         issued = c + 1;
     }
     // the last commit covers every MMA issued before it
-    if (t == 0) {
+    if (t == ISSUER) {
         bool done = true;
         if (issued > 0) done = mbar_wait(smem_u32(&bars[(issued - 1) & 1]), (uint32_t)(((issued - 1) >> 1) & 1));
         if (!done || !ok) atomicOr(A.status, ST_TIMEOUT);
@@ -374,9 +466,9 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     ok = s_ok != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok) {
-        const int nseg = (nch + ST_SEG - 1) / ST_SEG;   // segments 0 .. nseg - 3 are drained
-        if (nseg >= 2) drain<S::NCOL>(tq + (uint32_t)(((nseg - 2) & 1) * S::NT), run);
-        drain<S::NCOL>(tq + (uint32_t)(((nseg - 1) & 1) * S::NT), run);
+        // chunks 0 .. nch - 3 are drained; the last two are in the accumulators
+        if (nch >= 2) drain<S::NCOL>(tq + (uint32_t)(((nch - 2) & 1) * S::NT), run);
+        if (nch >= 1) drain<S::NCOL>(tq + (uint32_t)(((nch - 1) & 1) * S::NT), run);
         // ---- epilogue: O_D column-major and O_S row-major in the free stages ----
         float* Dm = (float*)smem;
         float* Sm = Dm + ND * ND;
@@ -416,7 +508,9 @@ template <int PD> int launch_self_tc(lymph_ctx* c, float* out, bool block_csr) {
         lymph_set_error("self-block assembly: no triangle rule for this degree");
         return LYMPH_ERR_INVALID;
     }
-    lymph_mf_face_rule(PD, &nq, A.frule);
+    double xyw[3 * 16];
+    lymph_mf_face_rule(PD, &nq, xyw);
+    for (int i = 0; i < 3 * nq; ++i) A.frule[i] = (float)xyw[i];
     LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_self_tc<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM));
     if (c->n_poly > 0) {
         k_self_tc<PD><<<c->n_poly, ST_THREADS, S::SMEM, c->stream>>>(A);

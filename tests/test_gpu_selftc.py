@@ -65,6 +65,22 @@ def test_tensor_core_self_blocks_match_fp64_assembly(require_gpu, kind, p):
             assert np.array_equal(got[3][nb], B64[nb].astype(np.float32).astype(np.float64))
 
 
+def test_tensor_core_self_block_of_a_large_polyhedron(require_gpu):
+    """One polyhedron of all 162 tetrahedra of a 3^3 x 6 cube, 108 Dirichlet
+    faces: more tetrahedra and faces than k_self_tc keeps in shared memory
+    (32 and 64), so the slots beyond them read the mesh arrays directly."""
+    from lymph3d_apsc_gb300 import mesh as M
+    m = M.cube(3, bc="dirichlet", agglomeration="hex", material=(1.0, 2.0, 1.0))
+    m.tet_poly = np.zeros_like(m.tet_poly)
+    for p in (2, 4):
+        K64, M64, _ = _self_and_mass(m, p, _lib.FP64)
+        Ktc, Mtc, _ = _self_and_mass(m, p, _lib.MIXED_MF)
+        e = _apply_rel(Ktc, K64, 11)
+        print(f"one polyhedron of {m.n_tet} tetrahedra, p={p}: {e:.2e}")
+        assert e <= TOL_SELF, e
+        assert np.array_equal(Mtc, M64)
+
+
 @pytest.mark.parametrize("theta", [0.0, 1.0])
 def test_tensor_core_self_blocks_other_theta(require_gpu, theta):
     """theta = 0 (IIPG) and 1 (NIPG): the symmetry terms enter O_D and O_S
