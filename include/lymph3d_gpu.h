@@ -71,9 +71,8 @@ extern "C" {
 /* ---- precision of the operator apply ----------------------------------- */
 #define LYMPH_FP64   0   /* every operation in FP64 (the plain path) */
 #define LYMPH_MIXED  1   /* operator blocks and their mat-vec in FP32, FP32
-                            accumulation; self blocks assembled on the tensor
-                            cores (kind::tf32, FP32-accurate split products),
-                            neighbour blocks by the FP64 assembly rounded;
+                            accumulation; every block assembled on the tensor
+                            cores (kind::tf32, FP32-accurate split products);
                             geometry, mass matrices, mass inverse, time update
                             and error norms in FP64 */
 #define LYMPH_MIXED_MF 2  /* FP32 self blocks (assembled on the tensor cores,

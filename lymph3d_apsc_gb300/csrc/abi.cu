@@ -28,7 +28,7 @@ int lymph_dev_cholesky(lymph_ctx* c);
 int lymph_dev_damping(lymph_ctx* c, bool assemble);
 int lymph_dev_mass(lymph_ctx* c, const int64_t* self_list);
 int lymph_dev_self_tc(lymph_ctx* c, float* out, bool block_csr);
-int lymph_dev_assemble_at(lymph_ctx* c, int which, void* out, int out_fp32, const int64_t* list, int64_t n_list);
+int lymph_dev_nb_tc(lymph_ctx* c, float* out, const int64_t* list, int64_t n_list);
 int lymph_dev_vector(lymph_ctx* c, int mode, int fid, int did, int nid, double scale, double* out);
 int lymph_dev_step(lymph_ctx* c, bool bump);
 int lymph_dev_first_step(lymph_ctx* c);
@@ -509,9 +509,8 @@ static int make_mf_matrices(lymph_ctx* c) {
     return lymph_mf_setup(c, R);
 }
 
-// FP32 blocks (LYMPH_MIXED): the self blocks on the tensor cores, the
-// neighbour blocks (face terms only) by the FP64 assembly rounded to FP32,
-// the mass matrices in FP64.
+// FP32 blocks (LYMPH_MIXED): the self and the neighbour blocks on the
+// tensor cores, the mass matrices in FP64.
 static int make_mixed_blocks(lymph_ctx* c) {
     const int np = c->n_poly;
     std::vector<int64_t> lists;
@@ -525,7 +524,7 @@ static int make_mixed_blocks(lymph_ctx* c) {
     int rc = cudaMemcpy(d_lists, lists.data(), sizeof(int64_t) * lists.size(), cudaMemcpyHostToDevice) == cudaSuccess
                  ? LYMPH_OK : LYMPH_ERR_CUDA;
     if (rc == LYMPH_OK) rc = lymph_dev_mass(c, d_lists);
-    if (rc == LYMPH_OK && n_nb > 0) rc = lymph_dev_assemble_at(c, LYMPH_BLOCKS_K, c->d_K, 1, d_lists + np, n_nb);
+    if (rc == LYMPH_OK && n_nb > 0) rc = lymph_dev_nb_tc(c, (float*)c->d_K, d_lists + np, n_nb);
     if (rc == LYMPH_OK) rc = lymph_dev_self_tc(c, (float*)c->d_K, true);
     if (rc == LYMPH_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = LYMPH_ERR_CUDA;
     cudaFree(d_lists);

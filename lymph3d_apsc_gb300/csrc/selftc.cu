@@ -1,6 +1,7 @@
-// selftc.cu -- the FP32 self blocks of the mixed operators (LYMPH_MIXED_MF,
-// LYMPH_MIXED) assembled on the 5th-generation tensor cores (tcgen05,
-// kind::tf32).
+// selftc.cu -- the FP32 operator blocks of the mixed precisions assembled on
+// the 5th-generation tensor cores (tcgen05, kind::tf32): the self blocks of
+// LYMPH_MIXED_MF and LYMPH_MIXED (k_self_tc) and LYMPH_MIXED's neighbour
+// blocks (k_nb_tc).
 //
 // The self block K_PP of MAKE_MATRICES_FREE (src/matrix_free.f90:27-464) is
 // the volume stiffness of P's sub-tetrahedra (MAKE_STIFFNESS_VOLUME,
@@ -31,6 +32,19 @@
 // triangle rule exact to degree 2p of the matrix-free kernel (mf.cu), whose
 // integrals equal the reference's collapsed rule's in exact arithmetic,
 // volume integrals the reference's collapsed Gauss rule.
+//
+// A neighbour block K_PQ (P's test functions, Q's trial functions) has face
+// terms only, -theta/2 I - S - IT/2 over the triangles P shares with Q,
+// with P's normal and P's material; A comes from P's basis, B from Q's, and
+// the same combination applies with five slots per face point:
+//   "d":     A = d_i phi^P_a,  B_D = -theta/2 W lambda n_j phi^Q_b,  B_S = -theta/2 W mu n_j phi^Q_b
+//   "n phi": A = n_i phi^P_a,  B_D = -mu W/2 d_j phi^Q_b,
+//            B_S = -sigma W/2 n_j phi^Q_b - lambda W/2 d_j phi^Q_b
+//   "phi_k", k = 0, 1, 2:  A = delta_ik phi^P_a,  B_D = delta_jk (lambda - mu)/2 W d_n phi^Q_b,  B_S = 0.
+// The symmetry term's IT_E2 index order (assemble_element.f90:610-616) puts
+// its lambda part into the block transpose of O_S, whose trace then carries
+// lambda where that term's delta_ij part has mu; the "phi_k" slots add the
+// difference on the diagonal component blocks.
 //
 // One CTA of 512 threads per polyhedron.  The K slots come in chunks of 32
 // (the tetrahedra's volume points, then the faces).  P's tetrahedra (map,
@@ -72,10 +86,11 @@ constexpr int ST_THREADS = 512;   // 16 warps: 4 per tensor-memory lane quadrant
 constexpr int ST_BK = 32;         // K slots per chunk (4 MMAs of K = 8)
 constexpr int ST_TMAX = 32;       // tetrahedra of a polyhedron kept in shared memory (the rest read from the arrays)
 constexpr int ST_FMAX = 64;       // faces of a polyhedron kept in shared memory
-constexpr int ST_FW = 18;         // floats per face entry (face_entry)
+constexpr int ST_FW = 18;         // floats per face entry of a self block (face_entry)
+constexpr int ST_FWN = 28;        // floats per face entry of a neighbour block (face_entry_nb)
 constexpr int ST_FACE_NQ[5] = {0, 3, 6, 12, 16};   // nodes of the symmetric triangle rule (mf.cu)
 
-template <int PD> struct TcShape {
+template <int PD, bool NB = false> struct TcShape {
     static constexpr int NP = (PD + 1) * (PD + 2) * (PD + 3) / 6;
     static constexpr int ND = 3 * NP;
     static constexpr int NQ3 = (PD + 1) * (PD + 1) * (PD + 1);
@@ -86,7 +101,10 @@ template <int PD> struct TcShape {
     static constexpr int NT = 2 * NH;                // the MMA's N: O_D | O_S
     static constexpr int NCOL = NT / 4;              // accumulator columns drained per thread
     static constexpr int TCOLS = 2 * NT <= 64 ? 64 : (2 * NT <= 128 ? 128 : (2 * NT <= 256 ? 256 : 512));
-    static constexpr int LS = (3 * (PD + 1)) | 1;    // (L, L') pairs per slot, odd: no bank conflicts
+    // (L, L') pairs per slot (P's box; for a neighbour block also Q's), odd: no bank conflicts
+    static constexpr int LS = ((NB ? 6 : 3) * (PD + 1)) | 1;
+    static constexpr int FW = NB ? ST_FWN : ST_FW;
+    static constexpr int SPF = 5 * NF;               // slots per face of a neighbour block
     static constexpr size_t A_TILE = 128 * 128;      // 128 rows x 32 TF32 slots
     static constexpr size_t B_TILE = (size_t)NT * 128;
     static constexpr size_t STAGE = 2 * A_TILE + 2 * B_TILE;
@@ -94,7 +112,7 @@ template <int PD> struct TcShape {
     static constexpr size_t COEF_OFF = LEG_OFF + 2 * (size_t)ST_BK * LS * 8;
     static constexpr size_t TET_OFF = COEF_OFF + 2 * (size_t)ST_BK * 3 * 16;
     static constexpr size_t FACE_OFF = TET_OFF + (size_t)ST_TMAX * 16 * 4;
-    static constexpr size_t REF_OFF = FACE_OFF + (size_t)ST_FMAX * ST_FW * 4;   // the volume rule in FP32
+    static constexpr size_t REF_OFF = FACE_OFF + (size_t)ST_FMAX * FW * 4;   // the volume rule in FP32
     static constexpr size_t BAR_OFF = REF_OFF + (size_t)NQ3 * 4 * 4;
     static constexpr size_t SMEM = BAR_OFF + 64 + 1024;   // + room to align the base to 1 KB
     static_assert(NT <= 256 && NT % 16 == 0, "MMA N");
@@ -132,10 +150,13 @@ struct SelfTcArgs {
     const double* hk;
     const RefTables* ref;
     const int32_t* row_ptr;
+    const int32_t* blk_row;
+    const int32_t* col;
     const int64_t* bf_ptr;
     const int32_t* bf;
+    const int64_t* list;   // neighbour blocks: the blocks of this launch (one CTA each)
     double alpha, theta;
-    float* out;            // column-major ND x ND blocks: P's at slot P, or at slot row_ptr[P]
+    float* out;            // column-major ND x ND blocks: P's self block at slot P or row_ptr[P]; a neighbour block at its own slot
     int slot_row_ptr;      // 1: the block-CSR operator of LYMPH_MIXED (self block first in each row)
     int* status;
     float frule[3 * 16];   // (xi, eta, w) of the symmetric triangle rule
@@ -215,6 +236,47 @@ __device__ __noinline__ void face_entry(const SelfTcArgs& A, int P, const Box& b
     out[17] = (float)(0.5 * sigma);
 }
 
+// Entry e of the face list of neighbour block (P, Q) (MAKE_STIFFNESS_FACE's
+// E2 terms, assemble_element.f90:404-661, as MAKE_MATRICES_FREE inserts them,
+// matrix_free.f90:412-433): the quadrature map in P's and in Q's box
+// coordinates, P's outward normal, the area and the factors of the slot
+// weights W = w_q area: -theta/2 lambda, -theta/2 mu, -mu/2, -lambda/2,
+// -sigma/2 and (lambda - mu)/2 (lambda, mu of P's tetrahedron, the
+// reference's choice for both sides).  out[ST_FWN].
+template <int PD>
+__device__ __noinline__ void face_entry_nb(const SelfTcArgs& A, int P, int Q, const Box& bp, const Box& bq, int64_t e,
+                                           float* out) {
+    const int code = A.bf[e];
+    const int tt = code >> 2, f = code & 3;
+    const int mid = A.tet_mat[tt];
+    const double lam = A.mat[mid * 3 + 1], mu = A.mat[mid * 3 + 2];
+    const double sigma = A.alpha * (double)(PD * PD) / fmin(A.hk[P], A.hk[Q]) * (lam + 2.0 * mu);
+    const double* F = A.fk + (int64_t)tt * 12;
+    const double* nm = A.ref->node_maps + f * 16;
+    for (int d = 0; d < 3; ++d) {
+        double cm[4];
+        for (int l = 0; l < 4; ++l) {
+            double s = 0.0;
+            for (int m = 0; m < 4; ++m) s += F[d * 4 + m] * nm[m * 4 + l];
+            cm[l] = s;
+        }
+        out[d] = (float)((cm[2] + cm[3] - bp.c[d]) * bp.ih[d]);
+        out[3 + d] = (float)(cm[0] * bp.ih[d]);
+        out[6 + d] = (float)(cm[1] * bp.ih[d]);
+        out[9 + d] = (float)((cm[2] + cm[3] - bq.c[d]) * bq.ih[d]);
+        out[12 + d] = (float)(cm[0] * bq.ih[d]);
+        out[15 + d] = (float)(cm[1] * bq.ih[d]);
+        out[18 + d] = (float)A.nrm[(int64_t)tt * 12 + f * 3 + d];
+    }
+    out[21] = (float)A.area[(int64_t)tt * 4 + f];
+    out[22] = (float)(-0.5 * A.theta * lam);
+    out[23] = (float)(-0.5 * A.theta * mu);
+    out[24] = (float)(-0.5 * mu);
+    out[25] = (float)(-0.5 * lam);
+    out[26] = (float)(-0.5 * sigma);
+    out[27] = (float)(0.5 * (lam - mu));
+}
+
 // value v into row `row`, slot k of a 128-byte-swizzled K-major tile pair:
 // hi = v rounded to TF32, lo = the remainder v - hi (exact in FP32, at most
 // 2^-11 |v|) rounded to TF32, so v = hi + lo to within 2^-23 |v| and the
@@ -246,9 +308,11 @@ template <int NCOL> __device__ __forceinline__ void drain(uint32_t taddr, float 
     }
 }
 
-template <int PD>
-__global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant__ SelfTcArgs A) {
-    using S = TcShape<PD>;
+// One block of the operator per CTA: the self block of polyhedron
+// blockIdx.x (NB = false) or neighbour block list[blockIdx.x] (NB = true).
+template <int PD, bool NB>
+__device__ __forceinline__ void block_tc(const SelfTcArgs& A) {
+    using S = TcShape<PD, NB>;
     constexpr int NP = S::NP, ND = S::ND, L = PD + 1;
     extern __shared__ __align__(1024) char smem_raw[];
     // the swizzle pattern is a function of the address: align the stages to 1 KB
@@ -261,23 +325,35 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     uint64_t* bars = (uint64_t*)(smem + S::BAR_OFF);
     uint32_t* tmem_slot = (uint32_t*)(bars + 2);
     __shared__ int s_ok;
-    __shared__ float s_box[4];   // ih_x, ih_y, ih_z, sc of P's Legendre map
+    __shared__ float s_box[8];   // ih_x, ih_y, ih_z, sc of P's Legendre map, then Q's
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int P = blockIdx.x;
     const uint32_t sbase = smem_u32(smem);
     constexpr int ISSUER = 32;   // lane 0 of warp 1 waits on the barriers and issues the MMAs
     // after one CTA's wait ran out the launch has failed: the others return
     // at once instead of waiting out their own limits
     if (*(volatile int*)A.status & ST_TIMEOUT) return;
 
-    const int t0 = A.poly_ptr[P], ntet = A.poly_ptr[P + 1] - t0;
-    const int64_t kself = A.row_ptr[P];   // the self block leads its row
-    const int64_t f0 = A.bf_ptr[kself];
-    const int nface = (int)(A.bf_ptr[kself + 1] - f0);
+    int P, Q, t0, ntet;
+    int64_t kblk;   // the block's slot in the block-CSR pattern
+    if constexpr (NB) {
+        kblk = A.list[blockIdx.x];
+        P = A.blk_row[kblk];
+        Q = A.col[kblk];
+        t0 = 0;
+        ntet = 0;   // face terms only
+    } else {
+        P = Q = blockIdx.x;
+        kblk = A.row_ptr[P];   // the self block leads its row
+        t0 = A.poly_ptr[P];
+        ntet = A.poly_ptr[P + 1] - t0;
+    }
+    const int64_t f0 = A.bf_ptr[kblk];
+    const int nface = (int)(A.bf_ptr[kblk + 1] - f0);
     const int nvc = ntet * S::CPT;
-    const int nch = nvc + (nface + S::FPC - 1) / S::FPC;
+    const int nch = NB ? (nface * S::SPF + ST_BK - 1) / ST_BK : nvc + (nface + S::FPC - 1) / S::FPC;
     const double* bb = A.bbox + (int64_t)P * 6;
     const Box bx = box_of(bb);
+    const Box bxq = NB ? box_of(A.bbox + (int64_t)Q * 6) : bx;
 
     // zero both operand stages: padding rows are never written again
     for (int i = t; i < (int)(2 * S::STAGE / 16); i += ST_THREADS) ((float4*)smem)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -285,19 +361,27 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     // in shared memory and FP32, so the per-chunk slot set-up reads no global
     // memory and does no FP64 arithmetic (beyond ST_TMAX / ST_FMAX it forms
     // the entries from the arrays)
-    if (t < ntet && t < ST_TMAX) tet_entry(A, bx, A.poly_tets[t0 + t], s_tet + t * 16);
-    if (t >= 64 && t - 64 < nface && t - 64 < ST_FMAX) face_entry<PD>(A, P, bx, f0 + (t - 64), s_face + (t - 64) * ST_FW);
-    for (int q = t; q < S::NQ3; q += ST_THREADS)
-        s_ref[q] = make_float4((float)A.ref->nodtet3[q * 4], (float)A.ref->nodtet3[q * 4 + 1],
-                               (float)A.ref->nodtet3[q * 4 + 2], (float)A.ref->weitet3[q]);
+    if (t >= 64 && t - 64 < nface && t - 64 < ST_FMAX) {
+        if constexpr (NB) face_entry_nb<PD>(A, P, Q, bx, bxq, f0 + (t - 64), s_face + (t - 64) * S::FW);
+        else face_entry<PD>(A, P, bx, f0 + (t - 64), s_face + (t - 64) * S::FW);
+    }
+    if constexpr (!NB) {
+        if (t < ntet && t < ST_TMAX) tet_entry(A, bx, A.poly_tets[t0 + t], s_tet + t * 16);
+        for (int q = t; q < S::NQ3; q += ST_THREADS)
+            s_ref[q] = make_float4((float)A.ref->nodtet3[q * 4], (float)A.ref->nodtet3[q * 4 + 1],
+                                   (float)A.ref->nodtet3[q * 4 + 2], (float)A.ref->weitet3[q]);
+    }
     if (t == 0) {
-        double hprod = 1.0;
-        for (int d = 0; d < 3; ++d) {
-            const double h = (bb[2 * d + 1] - bb[2 * d]) / 2.0;
-            s_box[d] = (float)(1.0 / h);
-            hprod *= h;
+        for (int side = 0; side < (NB ? 2 : 1); ++side) {
+            const double* bs = A.bbox + (int64_t)(side ? Q : P) * 6;
+            double hprod = 1.0;
+            for (int d = 0; d < 3; ++d) {
+                const double h = (bs[2 * d + 1] - bs[2 * d]) / 2.0;
+                s_box[4 * side + d] = (float)(1.0 / h);
+                hprod *= h;
+            }
+            s_box[4 * side + 3] = (float)(1.0 / sqrt(hprod));
         }
-        s_box[3] = (float)(1.0 / sqrt(hprod));
         mbar_init(smem_u32(&bars[0]), 1);
         mbar_init(smem_u32(&bars[1]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -313,6 +397,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
     const float sc = s_box[3], sx = sc * s_box[0], sy = sc * s_box[1], sz = sc * s_box[2];
+    const float scq = s_box[7], sxq = scq * s_box[4], syq = scq * s_box[5], szq = scq * s_box[6];
     const int grp = warp >> 2;                                   // column group of the drain
     const uint32_t tq = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(grp * S::NCOL);
     const uint32_t idesc = idesc_tf32(128, S::NT);
@@ -321,9 +406,47 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     // Legendre values, into buffer b; FP32 from the tables
     auto slot_setup = [&](int c, int b) {
         const int k = lane;
-        float xh[3] = {0.f, 0.f, 0.f};
+        float xh[3] = {0.f, 0.f, 0.f}, xq[3] = {0.f, 0.f, 0.f};
         float bd = 0.f, bn = 0.f, dd = 0.f, dn = 0.f, sd = 0.f, sn = 0.f, nv[3] = {0.f, 0.f, 0.f};
-        if (c < nvc) {
+        float bphi = 0.f, dc = 0.f, kc = 0.f;
+        if constexpr (NB) {
+            // slot s of the block: face s / (5 NF); per point a "d", an "n phi"
+            // and three "phi_k" slots (the delta_ij part of the symmetry term)
+            const int sidx = c * ST_BK + k, fi = sidx / S::SPF, r = sidx % S::SPF;
+            if (fi < nface) {
+                float e[ST_FWN];
+                if (fi < ST_FMAX) {
+#pragma unroll
+                    for (int i = 0; i < ST_FWN; ++i) e[i] = s_face[fi * ST_FWN + i];
+                } else {
+                    float ev[ST_FWN];
+                    face_entry_nb<PD>(A, P, Q, bx, bxq, f0 + fi, ev);
+#pragma unroll
+                    for (int i = 0; i < ST_FWN; ++i) e[i] = ev[i];
+                }
+                const int kind = r / S::NF, q = r % S::NF;
+                const float xi = A.frule[3 * q], eta = A.frule[3 * q + 1], W = A.frule[3 * q + 2] * e[21];
+                for (int d = 0; d < 3; ++d) {
+                    xh[d] = fmaf(eta, e[6 + d], fmaf(xi, e[3 + d], e[d]));
+                    xq[d] = fmaf(eta, e[15 + d], fmaf(xi, e[12 + d], e[9 + d]));
+                    nv[d] = e[18 + d];
+                }
+                if (kind == 0) {          // "d"
+                    bd = 1.f;
+                    dn = e[22] * W;
+                    sn = e[23] * W;
+                } else if (kind == 1) {   // "n phi"
+                    bn = 1.f;
+                    dd = e[24] * W;
+                    sd = e[25] * W;
+                    sn = e[26] * W;
+                } else {                  // "phi_k", k = kind - 2
+                    bphi = 1.f;
+                    dc = e[27] * W;
+                    kc = (float)(kind - 2);
+                }
+            }
+        } else if (c < nvc) {
             const int q = (c % S::CPT) * ST_BK + k, j = c / S::CPT;
             if (q < S::NQ3) {
                 float e[16];
@@ -378,10 +501,14 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
         float2* lg = leg + (b * ST_BK + k) * S::LS;
 #pragma unroll
         for (int d = 0; d < 3; ++d) legendre_f32<PD>(xh[d], lg + d * L);
+        if constexpr (NB) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) legendre_f32<PD>(xq[d], lg + (3 + d) * L);
+        }
         float4* cf = coef + (b * ST_BK + k) * 3;
         cf[0] = make_float4(bd, bn, dd, dn);
         cf[1] = make_float4(sd, sn, nv[0], nv[1]);
-        cf[2] = make_float4(nv[2], 0.f, 0.f, 0.f);
+        cf[2] = make_float4(nv[2], bphi, dc, kc);
     };
 
     float run[S::NCOL];
@@ -415,8 +542,8 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
             char* blo = bhi + S::B_TILE;
             const int k = lane;
             const float4* cf = coef + (st * ST_BK + k) * 3;
-            const float4 c0 = cf[0], c1 = cf[1];
-            const float n3[3] = {c1.z, c1.w, cf[2].x};
+            const float4 c0 = cf[0], c1 = cf[1], c2 = cf[2];
+            const float n3[3] = {c1.z, c1.w, c2.x};
             const float2* lg = leg + (st * ST_BK + k) * S::LS;
             for (int a = warp - 1; a < NP; a += ST_THREADS / 32 - 1) {
                 const int3 tr = blist_row<PD>(a);
@@ -424,13 +551,33 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
                 const float yz = Y.x * Z.x;
                 const float phi = sc * X.x * yz;
                 const float g[3] = {sx * X.y * yz, sy * X.x * Y.y * Z.x, sz * X.x * Y.x * Z.y};
+                if constexpr (NB) {
+                    // A from P's basis, B from Q's; the "phi_k" slots put
+                    // phi^P_a and (lambda - mu)/2 W d_n phi^Q_b on component kc
+                    const float2 Xq = lg[3 * L + tr.x], Yq = lg[4 * L + tr.y], Zq = lg[5 * L + tr.z];
+                    const float yzq = Yq.x * Zq.x;
+                    const float phq = scq * Xq.x * yzq;
+                    const float gq[3] = {sxq * Xq.y * yzq, syq * Xq.x * Yq.y * Zq.x, szq * Xq.x * Yq.x * Zq.y};
+                    const float dnq = fmaf(n3[0], gq[0], fmaf(n3[1], gq[1], n3[2] * gq[2]));
+                    const int kc = (int)c2.w;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const float np_ = n3[i] * phi;
-                    const int row = i * NP + a;
-                    put_split(ahi, alo, row, k, fmaf(c0.x, g[i], c0.y * np_));
-                    put_split(bhi, blo, row, k, fmaf(c0.z, g[i], c0.w * np_));
-                    put_split(bhi, blo, S::NH + row, k, fmaf(c1.x, g[i], c1.y * np_));
+                    for (int i = 0; i < 3; ++i) {
+                        const int row = i * NP + a;
+                        const float av = fmaf(c0.x, g[i], c0.y * (n3[i] * phi)) + (i == kc ? c2.y * phi : 0.f);
+                        const float bdv = fmaf(c0.z, gq[i], c0.w * (n3[i] * phq)) + (i == kc ? c2.z * dnq : 0.f);
+                        put_split(ahi, alo, row, k, av);
+                        put_split(bhi, blo, row, k, bdv);
+                        put_split(bhi, blo, S::NH + row, k, fmaf(c1.x, gq[i], c1.y * (n3[i] * phq)));
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        const float np_ = n3[i] * phi;
+                        const int row = i * NP + a;
+                        put_split(ahi, alo, row, k, fmaf(c0.x, g[i], c0.y * np_));
+                        put_split(bhi, blo, row, k, fmaf(c0.z, g[i], c0.w * np_));
+                        put_split(bhi, blo, S::NH + row, k, fmaf(c1.x, g[i], c1.y * np_));
+                    }
                 }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic-proxy writes -> the MMAs
@@ -482,7 +629,7 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
             }
         }
         __syncthreads();
-        float* out = A.out + (A.slot_row_ptr ? kself : (int64_t)P) * ND * ND;
+        float* out = A.out + ((NB || A.slot_row_ptr) ? kblk : (int64_t)P) * ND * ND;
         for (int e = t; e < ND * ND; e += ST_THREADS) {
             const int col = e / ND, r = e - col * ND;
             const int i = r / NP, a = r - i * NP, j = col / NP, b = col - j * NP;
@@ -496,21 +643,62 @@ __global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)S::TCOLS));
 }
 
-template <int PD> int launch_self_tc(lymph_ctx* c, float* out, bool block_csr) {
-    using S = TcShape<PD>;
-    SelfTcArgs A;
+template <int PD>
+__global__ void __launch_bounds__(ST_THREADS, 1) k_self_tc(const __grid_constant__ SelfTcArgs A) {
+    block_tc<PD, false>(A);
+}
+
+template <int PD>
+__global__ void __launch_bounds__(ST_THREADS, 1) k_nb_tc(const __grid_constant__ SelfTcArgs A) {
+    block_tc<PD, true>(A);
+}
+
+// The kernel arguments of a context (out, the output flags and the list are
+// the caller's); false if the degree has no triangle rule.
+template <int PD> bool tc_args(lymph_ctx* c, SelfTcArgs& A) {
     A.poly_ptr = c->d_poly_ptr; A.poly_tets = c->d_poly_tets; A.tet_poly = c->d_tet_poly; A.tet_mat = c->d_tet_mat;
     A.neigh = c->d_neigh; A.mat = c->d_mat; A.fk = c->d_fk; A.jdet = c->d_jdet; A.nrm = c->d_normal; A.area = c->d_area;
-    A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.row_ptr = c->d_row_ptr; A.bf_ptr = c->d_bf_ptr;
-    A.bf = c->d_bf; A.alpha = c->alpha; A.theta = c->theta; A.out = out; A.slot_row_ptr = block_csr ? 1 : 0; A.status = c->d_status;
+    A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.row_ptr = c->d_row_ptr; A.blk_row = c->d_blk_row;
+    A.col = c->d_col; A.bf_ptr = c->d_bf_ptr; A.bf = c->d_bf; A.list = nullptr; A.alpha = c->alpha;
+    A.theta = c->theta; A.out = nullptr; A.slot_row_ptr = 0; A.status = c->d_status;
     int32_t nq = 0;
-    if (lymph_mf_face_rule(PD, &nq, nullptr) != LYMPH_OK || nq != S::NF) {
-        lymph_set_error("self-block assembly: no triangle rule for this degree");
-        return LYMPH_ERR_INVALID;
-    }
+    if (lymph_mf_face_rule(PD, &nq, nullptr) != LYMPH_OK || nq != ST_FACE_NQ[PD]) return false;
     double xyw[3 * 16];
     lymph_mf_face_rule(PD, &nq, xyw);
     for (int i = 0; i < 3 * nq; ++i) A.frule[i] = (float)xyw[i];
+    return true;
+}
+
+template <int PD> int launch_nb_tc(lymph_ctx* c, float* out, const int64_t* list, int64_t n_list) {
+    using S = TcShape<PD, true>;
+    SelfTcArgs A;
+    if (!tc_args<PD>(c, A)) {
+        lymph_set_error("neighbour-block assembly: no triangle rule for this degree");
+        return LYMPH_ERR_INVALID;
+    }
+    A.out = out;
+    A.list = list;
+    LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_nb_tc<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM));
+    const int64_t chunk = 1 << 20;
+    for (int64_t b0 = 0; b0 < n_list; b0 += chunk) {
+        A.list = list + b0;
+        const int64_t nb = n_list - b0 < chunk ? n_list - b0 : chunk;
+        k_nb_tc<PD><<<(unsigned)nb, ST_THREADS, S::SMEM, c->stream>>>(A);
+        c->launches++;
+        LYMPH_CUDA_TRY(cudaGetLastError());
+    }
+    return LYMPH_OK;
+}
+
+template <int PD> int launch_self_tc(lymph_ctx* c, float* out, bool block_csr) {
+    using S = TcShape<PD>;
+    SelfTcArgs A;
+    if (!tc_args<PD>(c, A)) {
+        lymph_set_error("self-block assembly: no triangle rule for this degree");
+        return LYMPH_ERR_INVALID;
+    }
+    A.out = out;
+    A.slot_row_ptr = block_csr ? 1 : 0;
     LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_self_tc<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM));
     if (c->n_poly > 0) {
         k_self_tc<PD><<<c->n_poly, ST_THREADS, S::SMEM, c->stream>>>(A);
@@ -525,6 +713,18 @@ template <int PD> int launch_self_tc(lymph_ctx* c, float* out, bool block_csr) {
 // The FP32 self block of every polyhedron on the tensor cores, column-major,
 // into out[n_poly][nd * nd] or (block_csr) into the self-block slots
 // row_ptr[P] of a block-CSR operator.
+// The FP32 neighbour blocks list[0..n_list) of the block-CSR operator out,
+// each into its own slot, on the tensor cores.
+int lymph_dev_nb_tc(lymph_ctx* c, float* out, const int64_t* list, int64_t n_list) {
+    switch (c->p) {
+        case 1: return launch_nb_tc<1>(c, out, list, n_list);
+        case 2: return launch_nb_tc<2>(c, out, list, n_list);
+        case 3: return launch_nb_tc<3>(c, out, list, n_list);
+        case 4: return launch_nb_tc<4>(c, out, list, n_list);
+        default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
+    }
+}
+
 int lymph_dev_self_tc(lymph_ctx* c, float* out, bool block_csr) {
     switch (c->p) {
         case 1: return launch_self_tc<1>(c, out, block_csr);

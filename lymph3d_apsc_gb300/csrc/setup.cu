@@ -152,7 +152,6 @@ struct AsmArgs {
     void* out;        // [n][out_stride] blocks, each [ND][ND] column-major
     const int64_t* list;  // blocks to assemble (null: all, in order); output slot = position in the list
     int64_t out_stride;   // elements from one output block to the next (>= ND*ND)
-    int out_at_block;     // block list[i] goes to output slot list[i] (else slot i)
     double* M;        // [n_poly][NP][NP] rho-weighted mass (self blocks only; may be null)
     double* Mm;       // unweighted (modal) mass
     int64_t block0;   // first block of this launch
@@ -444,7 +443,7 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(AsmArgs A) {
     }
     __syncthreads();
     // write the block column-major (entry (r,c) at c*ND + r)
-    const int64_t base = (A.out_at_block ? k : slot) * A.out_stride;
+    const int64_t base = slot * A.out_stride;
     if (A.out_fp32) {
         float* o = (float*)A.out;
         for (int i = tid; i < ND * ND; i += ASM_THREADS) {
@@ -906,7 +905,7 @@ __global__ void k_double_couple(int Np, int nq3, int t, int P, const double* __r
 
 template <int PD>
 int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass, const int64_t* list,
-                    int64_t n_list, int64_t out_stride, bool out_at_block = false) {
+                    int64_t n_list, int64_t out_stride) {
     size_t smem = asm_smem<PD>();
     LYMPH_CUDA_TRY(cudaFuncSetAttribute(k_assemble<PD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     AsmArgs A;
@@ -916,7 +915,7 @@ int launch_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write
     A.bbox = c->d_bbox; A.hk = c->d_hk; A.ref = c->d_ref; A.alpha = c->alpha; A.theta = c->theta;
     A.which = which; A.out_fp32 = out_fp32; A.out = out;
     A.M = write_mass ? c->d_M : nullptr; A.Mm = write_mass ? c->d_Mm : nullptr;
-    A.list = list; A.out_stride = out_stride; A.out_at_block = out_at_block ? 1 : 0;
+    A.list = list; A.out_stride = out_stride;
     const int64_t n = list ? n_list : c->n_blocks;
     const int64_t chunk = 1 << 20;
     for (int64_t b0 = 0; b0 < n; b0 += chunk) {
@@ -987,18 +986,6 @@ int lymph_dev_assemble_list(lymph_ctx* c, int which, void* out, int out_fp32, bo
 // gives them).
 int lymph_dev_mass(lymph_ctx* c, const int64_t* self_list) {
     return lymph_dev_assemble_list(c, ASM_MASS_ONLY, nullptr, 0, true, self_list, c->n_poly, 0);
-}
-
-// Blocks list[0..n_list) each into its own slot of the block-CSR array out.
-int lymph_dev_assemble_at(lymph_ctx* c, int which, void* out, int out_fp32, const int64_t* list, int64_t n_list) {
-    const int64_t st = (int64_t)c->nd * c->nd;
-    switch (c->p) {
-        case 1: return launch_assemble<1>(c, which, out, out_fp32, false, list, n_list, st, true);
-        case 2: return launch_assemble<2>(c, which, out, out_fp32, false, list, n_list, st, true);
-        case 3: return launch_assemble<3>(c, which, out, out_fp32, false, list, n_list, st, true);
-        case 4: return launch_assemble<4>(c, which, out, out_fp32, false, list, n_list, st, true);
-        default: lymph_set_error("degree not supported on the device"); return LYMPH_ERR_INVALID;
-    }
 }
 
 int lymph_dev_assemble(lymph_ctx* c, int which, void* out, int out_fp32, bool write_mass) {

@@ -15,6 +15,9 @@ oracle's assembled self blocks (MAKE_STIFFNESS_VOLUME +
 MAKE_STIFFNESS_FACE's self terms): the same integrals, so they agree to FP64
 rounding (1e-12 relative to the block's largest entry), for every theta,
 Dirichlet and Neumann faces, jittered tetrahedra and lognormal materials.
+k_nb_tc, for the neighbour blocks of LYMPH_MIXED, uses the same two products
+with five slots per face point; the second test restates that form and
+checks it against the oracle's neighbour blocks the same way.
 """
 from ctypes import POINTER, byref, c_double, c_int32
 
@@ -160,4 +163,88 @@ def test_decomposition_reproduces_the_self_blocks(p, theta, bc):
         ref = blocks[(P, P)]
         worst = max(worst, float(np.abs(K - ref).max() / np.abs(ref).max()))
     print(f"p={p} theta={theta} bc={bc}: {m.n_poly} self blocks, worst {worst:.2e}")
+    assert worst <= 1e-12, worst
+
+
+def _decomposed_neighbour_blocks(m, p, bbox, hk, alpha, theta, pairs):
+    """The neighbour blocks K_PQ by the same two products: per face point five
+    slots -- "d" (A = d_i phi^P_a), "n phi" (A = n_i phi^P_a) and three
+    "phi_k" slots (A = delta_ik phi^P_a) that carry the delta_ij part of the
+    symmetry term, whose IT_E2 index order gives the block transpose of O_S
+    lambda where that part needs mu."""
+    lib = _lib.load()
+    n = c_int32()
+    lib.lymph_mf_face_rule(p, byref(n), None)
+    xyw = np.zeros(3 * n.value)
+    lib.lymph_mf_face_rule(p, byref(n), xyw.ctypes.data_as(POINTER(c_double)))
+    xyw = xyw.reshape(-1, 3)
+    NP = (p + 1) * (p + 2) * (p + 3) // 6
+    ND = 3 * NP
+    blist = [(a, b, c) for a in range(p, -1, -1) for b in range(p - a, -1, -1) for c in range(p - a - b, -1, -1)]
+    X, tv, tp = m.coords, m.tet_vert, m.tet_poly
+    nb = m.neigh.reshape(-1, 4)
+    out = {}
+    for P, Q in pairs:
+        A, BD, BS = [], [], []
+        for t in np.where(tp == P)[0]:
+            for f in range(4):
+                e2 = nb[t, f]
+                if e2 < 0 or tp[e2] != Q:
+                    continue
+                V = X[tv[t]]
+                F = np.concatenate([np.stack([V[1] - V[0], V[2] - V[0], V[3] - V[0]], 1), V[0][:, None]], 1)
+                cm = F @ NODE_MAPS[f]
+                c1, c2, c3 = (X[tv[t, v]] for v in FACE_VERTS[f])
+                Qv, Pv = c1 - c2, c3 - c2
+                nn = np.array([Pv[1] * Qv[2] - Pv[2] * Qv[1], -Pv[0] * Qv[2] + Pv[2] * Qv[0],
+                               Pv[0] * Qv[1] - Pv[1] * Qv[0]])
+                area = np.linalg.norm(nn)
+                nv = nn / area
+                lam, mu = m.mat[m.tet_mat[t], 1], m.mat[m.tet_mat[t], 2]
+                sigma = alpha * p * p / min(hk[P], hk[Q]) * (lam + 2 * mu)
+                xs = (cm[:, 2] + cm[:, 3])[None, :] + xyw[:, :1] * cm[:, 0] + xyw[:, 1:2] * cm[:, 1]
+                W = xyw[:, 2] * area
+                phP, grP = _tabulate(xs, bbox[P], p, blist)
+                phQ, grQ = _tabulate(xs, bbox[Q], p, blist)
+                nP = nv[:, None, None] * phP[None]
+                nQ = nv[:, None, None] * phQ[None]
+                dnQ = np.einsum("k,kbq->bq", nv, grQ)            # d_n phi^Q_b
+                zero = np.zeros_like(grQ)
+                A.append(grP.reshape(ND, -1))                      # "d"
+                BD.append((nQ * (-0.5 * theta * W * lam)).reshape(ND, -1))
+                BS.append((nQ * (-0.5 * theta * W * mu)).reshape(ND, -1))
+                A.append(nP.reshape(ND, -1))                       # "n phi"
+                BD.append((grQ * (-0.5 * mu * W)).reshape(ND, -1))
+                BS.append((nQ * (-0.5 * sigma * W) + grQ * (-0.5 * lam * W)).reshape(ND, -1))
+                for k in range(3):                                 # "phi_k"
+                    a_k = np.zeros_like(grP)
+                    a_k[k] = phP
+                    b_k = np.zeros_like(grQ)
+                    b_k[k] = dnQ * (0.5 * (lam - mu) * W)
+                    A.append(a_k.reshape(ND, -1))
+                    BD.append(b_k.reshape(ND, -1))
+                    BS.append(zero.reshape(ND, -1))
+        A = np.concatenate(A, 1)
+        OD = (A @ np.concatenate(BD, 1).T).reshape(3, NP, 3, NP)
+        OS = (A @ np.concatenate(BS, 1).T).reshape(3, NP, 3, NP)
+        K = OD + np.transpose(OS, (2, 1, 0, 3))
+        tr = OS[0, :, 0, :] + OS[1, :, 1, :] + OS[2, :, 2, :]
+        for i in range(3):
+            K[i, :, i, :] += tr
+        out[(P, Q)] = K.reshape(ND, ND)
+    return out
+
+
+@pytest.mark.parametrize("p,theta", [(1, -1.0), (2, 0.0), (3, 1.0), (4, -1.0)])
+def test_decomposition_reproduces_the_neighbour_blocks(p, theta):
+    m = _mesh("dirichlet")
+    o = Oracle(m, p, 1e-3, theta=theta)
+    o.make_matrices()
+    blocks = o.block_dict(0)
+    bbox, hk = o.poly_geometry()
+    o.close()
+    pairs = [pq for pq in blocks if pq[0] != pq[1]][:40]
+    got = _decomposed_neighbour_blocks(m, p, bbox, hk, 10.0, theta, pairs)
+    worst = max(float(np.abs(got[pq] - blocks[pq]).max() / np.abs(blocks[pq]).max()) for pq in pairs)
+    print(f"p={p} theta={theta}: {len(pairs)} neighbour blocks, worst {worst:.2e}")
     assert worst <= 1e-12, worst
