@@ -179,7 +179,7 @@ int lymph_sizes(const lymph_ctx* ctx, int32_t* Np, int32_t* n_poly, int64_t* n_b
 
 /* MAKE_MATRICES_FREE (src/matrix_free.f90:27-464) followed by the Cholesky
  * factorisation of the mass matrices (src/Lymph3D.f90:264-271): assembles
- * K_loc, M_loc, M_modal_loc and their factors on the device (the FP32 self
+ * K_loc, M_loc, M_modal_loc and their factors on the device (the FP32
  * blocks of the mixed precisions on the tensor cores). */
 int lymph_make_matrices(lymph_ctx* ctx);
 
