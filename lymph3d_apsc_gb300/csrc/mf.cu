@@ -261,18 +261,18 @@ __device__ __forceinline__ void prefetch_l2(const void* base, int64_t total, con
 
 // One CTA per polyhedron P.  At the start the CTA reads P's record (its
 // triangles' range and neighbours, one coalesced load), and one thread
-// prefetches into L2 what the end of the CTA reads (the FP32 self block,
-// M^-1, the right-hand sides and the state rows), so those reads do not wait
-// on HBM.  Neighbour
+// prefetches into L2 what the CTA reads later (the FP32 self block, M^-1,
+// the right-hand sides and the state rows).  The self-block rows (thread
+// r < ND, K_PP streamed) are computed while the first chunk's copies are in
+// flight (p = 4) or after the face loop (p <= 3).  Neighbour
 // triangles, CT triangles at a time, their geometry, Q's box and Q's FP32
 // coefficients copied into shared memory with cp.async one chunk ahead
 // (double-buffered): thread t evaluates point t -- Q's field and gradient,
 // the three components together by sum factorisation, the three flux rows,
 // and P's Legendre values, kept in shared memory; then thread 3 k + i accumulates
 // row component i of P's test sums over the points k, k + 42, ... of the
-// chunk in Np registers (the sum-factorised transpose).  Then the self-block
-// rows (thread r < ND, K_PP streamed from L2) and the 42 slots' partial rows,
-// summed in a fixed order.
+// chunk in Np registers (the sum-factorised transpose).  Then the 42 slots'
+// partial rows are summed in a fixed order and added to the self-block rows.
 // Shared-memory layout of one polyhedron's pass; the face-loop buffers and
 // the final reduction share storage.
 template <int PD> struct MfSmem {
@@ -367,10 +367,32 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
     const MfPoly pP = A.poly[P];
     const int slot = tid / 3, ci = tid - 3 * (tid / 3);   // test phase: point slot, row component
     const bool tact = slot < MF_SLOTS;
+    if (ntri > 0) stage(0, 0);
+    // ---- self block (FP32) rows, thread r < ND, K_PP streamed: at p = 4
+    // while chunk 0's copies are in flight (its loads go out before the test
+    // sums take their registers: 1 % faster on the 46,767-polyhedron mesh),
+    // at p <= 3 after the face loop with the test sums parked (3 % faster
+    // there); the same sums in the same order either way ----
+    constexpr bool SELF_FIRST = PD >= 4;
+    auto self_rows = [&]() -> float {
+        float y = 0.0f;
+        if (tid < ND) {
+            const float* Kb = A.Kself + (int64_t)P * ND * ND + tid;
+            float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+            for (int c = 0; c < ND; c += 2) {
+                a0 = fmaf(__ldcs(Kb + (int64_t)c * ND), s_uP[c], a0);
+                if (c + 1 < ND) a1 = fmaf(__ldcs(Kb + (int64_t)(c + 1) * ND), s_uP[c + 1], a1);
+            }
+            y = a0 + a1;
+        }
+        return y;
+    };
+    float yself = 0.0f;
+    if constexpr (SELF_FIRST) yself = self_rows();
     float acc[NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) acc[i] = 0.0f;
-    if (ntri > 0) stage(0, 0);
     for (int c = 0, k = 0; c < ntri; c += CT, ++k) {
         const int b = k & 1, nt = (ntri - c) < CT ? ntri - c : CT;
         if (c + CT < ntri) stage(c + CT, b ^ 1);
@@ -469,19 +491,7 @@ __device__ __forceinline__ void mf_poly(const MfArgs& A, const StepArgs& sa, int
 #pragma unroll
         for (int i = 0; i < NP; ++i) s_w.fin.red[slot][ci * NP + i] = acc[i];
     }
-    // ---- self block (FP32, from L2; the test sums are parked, so the
-    // registers go to loads in flight) ----
-    float yself = 0.0f;
-    if (tid < ND) {
-        const float* Kb = A.Kself + (int64_t)P * ND * ND + tid;
-        float a0 = 0.0f, a1 = 0.0f;
-#pragma unroll
-        for (int c = 0; c < ND; c += 2) {
-            a0 = fmaf(__ldcs(Kb + (int64_t)c * ND), s_uP[c], a0);
-            if (c + 1 < ND) a1 = fmaf(__ldcs(Kb + (int64_t)(c + 1) * ND), s_uP[c + 1], a1);
-        }
-        yself = a0 + a1;
-    }
+    if constexpr (!SELF_FIRST) yself = self_rows();
     __syncthreads();
     double y = 0.0;
     if (tid < ND) {
