@@ -96,14 +96,17 @@ def test_tensor_core_self_block_of_a_large_polyhedron(require_gpu):
 
 
 @pytest.mark.parametrize("theta", [0.0, 1.0])
-def test_tensor_core_self_blocks_other_theta(require_gpu, theta):
+def test_tensor_core_blocks_other_theta(require_gpu, theta):
     """theta = 0 (IIPG) and 1 (NIPG): the symmetry terms enter O_D and O_S
-    with other weights, and the blocks are no longer symmetric."""
+    with other weights, and the blocks are no longer symmetric; the self
+    blocks of the matrix-free context and the whole FP32-block operator."""
     m = _mesh("bfs_lognormal")
-    K64, _, _ = _self_and_mass(m, 3, _lib.FP64, theta)
+    K64, _, _, B64, (rp, col) = _self_and_mass(m, 3, _lib.FP64, theta, blocks=True)
     Ktc, _, _ = _self_and_mass(m, 3, _lib.MIXED_MF, theta)
     e = _apply_rel(Ktc, K64, 3)
-    print(f"theta={theta}: {e:.2e}")
+    Bmx = _self_and_mass(m, 3, _lib.MIXED, theta, blocks=True)[3]
+    e_all = _operator_rel(Bmx, B64, rp, col, 4)
+    print(f"theta={theta}: self blocks {e:.2e}, whole FP32-block operator {e_all:.2e}")
     assert e <= TOL_SELF, e
-    if theta != -1.0:
-        assert not np.allclose(K64, np.transpose(K64, (0, 2, 1)), rtol=1e-3)
+    assert e_all <= TOL_SELF, e_all
+    assert not np.allclose(K64, np.transpose(K64, (0, 2, 1)), rtol=1e-3)
