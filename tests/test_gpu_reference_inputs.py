@@ -13,7 +13,10 @@ the benchmark configurations, against the CPU oracle.
     mass-matrix norm (the bars of tests/test_gpu_parity.py);
   - the full driver sequence to the deck's own STOPTIME (1,000 steps; 3,183
     for tet_100 at p = 3): step count and final time equal, L2 and DG errors
-    within 1e-10 relative of the oracle's committed values.
+    within 1e-10 relative of the oracle's committed values;
+  - the two mixed operators (tensor-core FP32 blocks, matrix-free FP32
+    neighbour terms) on tet_5 and tet_25 at p = 1..4: K u per polyhedron row
+    within 2e-6 of the oracle's FP64 K u.
 * The 125-polyhedron cube (5^3 hexahedra x 6 tetrahedra, one polyhedron per
   hexahedron, p = 2, rho = lambda = mu = 1, dt = 1e-4, T = 0.1: 1,000 steps by
   the `t <= T` rule of Lymph3D.f90:389-418): L2 / DG errors within 1e-10 of
@@ -123,3 +126,25 @@ def test_c1_scale_three_steps(require_gpu):
             print(f"c1 step {k}: relative {e:.2e}, mass norm {em:.2e}")
             assert e <= TOL_STATE and em <= TOL_STATE, (k, e, em)
         o.close()
+
+
+@pytest.mark.parametrize("name", ["tet_5", "tet_25"])
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_deck_mixed_operators(require_gpu, name, p):
+    """The two mixed operators on the reference's decks (Dirichlet and Neumann
+    faces, one tetrahedron per polyhedron): K u of every polyhedron row, FP32
+    blocks from the tensor cores and the matrix-free FP32 neighbour terms,
+    against the oracle's FP64 K u: <= TOL_APPLY_FP32 (2e-6) per row."""
+    from parity_util import TOL_APPLY_FP32, oracle_apply, row_rel_max
+    m, prm = deck(name)
+    o = Oracle(m, p, prm["dt"])
+    o.make_matrices()
+    u = np.random.default_rng(20 + p).standard_normal((o.n_poly, o.nd))
+    want = oracle_apply(o, u)
+    o.close()
+    for prec in (_lib.MIXED, _lib.MIXED_MF):
+        with MatrixFree(m, p, prm["dt"], precision=prec) as g:
+            g.MAKE_MATRICES_FREE()
+            e = row_rel_max(g.apply_operator(u), want)
+        print(f"{name} p={p} precision {prec}: {e:.2e}")
+        assert e <= TOL_APPLY_FP32, (prec, e)
