@@ -146,6 +146,7 @@ def test_create_rejects_bad_input_with_status_codes():
     assert lib.lymph_checkpoint_save(None, b"x.ckpt", 0.0, 0) == _lib.LYMPH_ERR_INVALID
     assert lib.lymph_checkpoint_load(None, b"x.ckpt", None, None) == _lib.LYMPH_ERR_INVALID
     assert lib.lymph_step(None, 0.0) == _lib.LYMPH_ERR_INVALID
+    assert lib.lymph_get_self_blocks(None, px) == _lib.LYMPH_ERR_INVALID
 
 
 def test_create_without_device_fails_loudly():
