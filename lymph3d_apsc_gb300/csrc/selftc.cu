@@ -330,8 +330,11 @@ __device__ __forceinline__ void block_tc(const SelfTcArgs& A) {
     const uint32_t sbase = smem_u32(smem);
     constexpr int ISSUER = 32;   // lane 0 of warp 1 waits on the barriers and issues the MMAs
     // after one CTA's wait ran out the launch has failed: the others return
-    // at once instead of waiting out their own limits
-    if (*(volatile int*)A.status & ST_TIMEOUT) return;
+    // at once instead of waiting out their own limits (one read, so the
+    // whole CTA takes the same branch)
+    if (t == 0) s_ok = (*(volatile int*)A.status & ST_TIMEOUT) ? 0 : 1;
+    __syncthreads();
+    if (!s_ok) return;
 
     int P, Q, t0, ntet;
     int64_t kblk;   // the block's slot in the block-CSR pattern
